@@ -1,0 +1,286 @@
+"""Extract known-answer vectors from cuSpatial's own tests into JSON fixtures.
+
+Run from the repository root with the cuSpatial sources available:
+
+    python tests/golden/make_golden.py /path/to/cuspatial
+
+It reads the reference test files as text (it never imports or runs them) and
+writes one JSON file per source test file next to this script.  The fixtures
+are committed; the tests read only the JSON files.
+
+Sources:
+  cpp/tests/index/point_quadtree_test.cu                        (quadtree KATs)
+  cpp/tests/join/quadtree_point_in_polygon_test_small.cu        (join + PiP KAT)
+  cpp/tests/join/quadtree_point_to_nearest_linestring_test_small.cu
+  cpp/tests/point_in_polygon/point_in_polygon_test.cu           (boundary rule)
+  python/cuspatial/cuspatial/tests/spatial/bounding/test_linestring_bounding_boxes.py
+"""
+
+import json
+import os
+import re
+import sys
+
+
+def strip_comments(text):
+    text = re.sub(r"//[^\n]*", "", text)
+    return re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+
+
+def parse_number(tok):
+    tok = tok.strip()
+    if tok in ("true", "false"):
+        return tok == "true"
+    if tok.startswith(("0b", "0B")):
+        return int(tok[2:], 2)
+    tok = tok.rstrip("fFuUlL") if not tok.startswith(("0x", "0X")) else tok
+    if tok.startswith(("0x", "0X")):
+        return int(tok, 16)
+    if re.fullmatch(r"[-+]?\d+", tok):
+        return int(tok)
+    return float(tok)
+
+
+def parse_braces(text, pos):
+    """Parse a C++ brace initializer starting at text[pos] == '{'.
+
+    Returns (value, next_pos).  Scalars become numbers, braces become lists.
+    """
+    assert text[pos] == "{", text[pos:pos + 40]
+    pos += 1
+    out = []
+    tok = ""
+    while True:
+        c = text[pos]
+        if c == "{":
+            val, pos = parse_braces(text, pos)
+            out.append(val)
+            continue
+        if c in ",}":
+            if tok.strip():
+                out.append(parse_number(tok))
+            tok = ""
+            pos += 1
+            if c == "}":
+                return out, pos
+            continue
+        tok += c
+        pos += 1
+
+
+def matching_paren(text, pos):
+    assert text[pos] == "("
+    depth = 0
+    for i in range(pos, len(text)):
+        if text[i] in "({":
+            depth += 1
+        elif text[i] in ")}":
+            depth -= 1
+            if depth == 0:
+                return i
+    raise ValueError("unbalanced")
+
+
+def split_top_level(args):
+    parts, depth, cur = [], 0, ""
+    for c in args:
+        if c in "({<" and not (c == "<" and depth == 0 and False):
+            depth += 1 if c != "<" else 0
+        if c in ")}":
+            depth -= 1
+        if c == "," and depth == 0:
+            parts.append(cur.strip())
+            cur = ""
+        else:
+            cur += c
+    if cur.strip():
+        parts.append(cur.strip())
+    return parts
+
+
+def first_braces(text):
+    i = text.index("{")
+    return parse_braces(text, i)[0]
+
+
+def test_bodies(text, fixture):
+    pat = re.compile(r"TYPED_TEST\(\s*%s\s*,\s*(\w+)\s*\)\s*\{" % fixture)
+    out = {}
+    for m in pat.finditer(text):
+        start = m.end() - 1
+        depth = 0
+        for i in range(start, len(text)):
+            if text[i] == "{":
+                depth += 1
+            elif text[i] == "}":
+                depth -= 1
+                if depth == 0:
+                    out[m.group(1)] = text[start:i + 1]
+                    break
+    return out
+
+
+def run_test_args(body, fn):
+    m = re.search(r"CUSPATIAL_RUN_TEST\(\s*this->%s\s*," % fn, body)
+    if not m:
+        return None
+    open_pos = body.index("(", m.start())
+    close = matching_paren(body, open_pos)
+    return split_top_level(body[m.end():close])
+
+
+def quadtree_kats(root):
+    path = os.path.join(root, "cpp/tests/index/point_quadtree_test.cu")
+    text = strip_comments(open(path).read())
+    cases = []
+    for name, body in test_bodies(text, "QuadtreeOnPointIndexingTest").items():
+        args = run_test_args(body, "test")
+        env = {}
+        for var in ("vertex_1", "vertex_2"):
+            m = re.search(r"%s\s*(\{[^}]*\})" % var, body)
+            env[var] = first_braces(m.group(1))
+        for var in ("max_depth", "max_size", "scale"):
+            m = re.search(r"%s\s*=\s*([-+0-9.eE]+)" % var, body)
+            if m:
+                env[var] = parse_number(m.group(1))
+
+        def val(a):
+            a = a.strip()
+            if a in env:
+                return env[a]
+            wrapped = a.startswith("thrust::host_vector")
+            a = re.sub(r"^thrust::host_vector\s*", "", a)
+            if a.startswith("{"):
+                v = first_braces(a)
+                # thrust::host_vector{{...}} wraps the list once more
+                if wrapped and len(v) == 1 and isinstance(v[0], list):
+                    v = v[0]
+                return v
+            return parse_number(a)
+
+        vals = [val(a) for a in args]
+        points, v1, v2, scale, max_depth, max_size = vals[:6]
+        key, level, internal, length, offset = vals[6:11]
+        cases.append(
+            dict(name=name, x=[p[0] for p in points], y=[p[1] for p in points],
+                 x_min=v1[0], y_min=v1[1], x_max=v2[0], y_max=v2[1], scale=scale,
+                 max_depth=max_depth, max_size=max_size, key=key, level=level,
+                 is_internal_node=[int(b) for b in internal], length=length,
+                 offset=offset))
+    return dict(source="cpp/tests/index/point_quadtree_test.cu", cases=cases)
+
+
+def device_vectors(body):
+    """All make_device_vector<...>( {...} ) literals in order."""
+    out = []
+    for m in re.finditer(r"make_device_vector<[^(]*>\(\s*\{", body):
+        out.append(parse_braces(body, m.end() - 1)[0])
+    return out
+
+
+def small_params(body):
+    env = {}
+    for var in ("v_min", "v_max"):
+        m = re.search(r"%s\s*(\{[^}]*\})" % var, body)
+        env[var] = first_braces(m.group(1))
+    for var in ("scale", "max_depth", "max_size", "expansion_radius"):
+        m = re.search(r"%s\s*\{\s*([-+0-9.eE]+)\s*\}" % var, body)
+        if m:
+            env[var] = parse_number(m.group(1))
+    return env
+
+
+def pip_small_kat(root):
+    rel = "cpp/tests/join/quadtree_point_in_polygon_test_small.cu"
+    text = strip_comments(open(os.path.join(root, rel)).read())
+    body = test_bodies(text, "PIPRefineTestSmall")["TestSmall"]
+    env = small_params(body)
+    vecs = device_vectors(body)
+    points = vecs[0]
+    m = re.search(r"make_multipolygon_array<T>\(", body)
+    open_pos = body.index("(", m.start())
+    args = split_top_level(body[open_pos + 1:matching_paren(body, open_pos)])
+    geom, part, ring, verts = [first_braces(a) for a in args]
+    exp_poly_join, exp_quad_join, exp_poly, exp_point = vecs[1:5]
+    return dict(source=rel, x=[p[0] for p in points], y=[p[1] for p in points],
+                x_min=env["v_min"][0], y_min=env["v_min"][1], x_max=env["v_max"][0],
+                y_max=env["v_max"][1], scale=env["scale"], max_depth=env["max_depth"],
+                max_size=env["max_size"], geometry_offset=geom, part_offset=part,
+                ring_offset=ring, px=[v[0] for v in verts], py=[v[1] for v in verts],
+                join_bbox_offset=exp_poly_join, join_quad_offset=exp_quad_join,
+                polygon_index=exp_poly, point_index=exp_point)
+
+
+def nearest_small_kat(root):
+    rel = "cpp/tests/join/quadtree_point_to_nearest_linestring_test_small.cu"
+    text = strip_comments(open(os.path.join(root, rel)).read())
+    body = test_bodies(text, "QuadtreePointToLinestringTestSmall")["TestSmall"]
+    env = small_params(body)
+    vecs = device_vectors(body)
+    points = vecs[0]
+    m = re.search(r"make_multilinestring_array<T>\(", body)
+    open_pos = body.index("(", m.start())
+    args = split_top_level(body[open_pos + 1:matching_paren(body, open_pos)])
+    geom, part, verts = [first_braces(a) for a in args]
+    join_ls, join_quad = vecs[1], vecs[2]
+    dist_f32, dist_f64 = vecs[3], vecs[4]
+    exp_point, exp_ls = vecs[5], vecs[6]
+    return dict(source=rel, x=[p[0] for p in points], y=[p[1] for p in points],
+                x_min=env["v_min"][0], y_min=env["v_min"][1], x_max=env["v_max"][0],
+                y_max=env["v_max"][1], scale=env["scale"], max_depth=env["max_depth"],
+                max_size=env["max_size"], expansion_radius=env["expansion_radius"],
+                geometry_offset=geom, part_offset=part, lx=[v[0] for v in verts],
+                ly=[v[1] for v in verts], join_bbox_offset=join_ls,
+                join_quad_offset=join_quad, point_index=exp_point,
+                linestring_index=exp_ls, distance_f32=dist_f32, distance_f64=dist_f64)
+
+
+def point_in_polygon_kats(root):
+    rel = "cpp/tests/point_in_polygon/point_in_polygon_test.cu"
+    text = strip_comments(open(os.path.join(root, rel)).read())
+    cases = []
+    for name, body in test_bodies(text, "PointInPolygonTest").items():
+        args = run_test_args(body, "run_test")
+        if args is None or len(args) != 5:
+            continue
+        points, poly_off, ring_off, verts, expected = [first_braces(a) for a in args]
+        cases.append(dict(name=name, x=[p[0] for p in points], y=[p[1] for p in points],
+                          poly_offsets=poly_off, ring_offsets=ring_off,
+                          px=[v[0] for v in verts], py=[v[1] for v in verts],
+                          expected=expected))
+    return dict(source=rel, note="expected[i] bit j = point i inside polygon j", cases=cases)
+
+
+def linestring_bbox_kat(root):
+    rel = "python/cuspatial/cuspatial/tests/spatial/bounding/test_linestring_bounding_boxes.py"
+    text = open(os.path.join(root, rel)).read()
+    m = re.search(r"def test_linestring_bounding_boxes_small\(dtype\):(.*?)\ndef ", text, re.S)
+    body = m.group(1)
+    series = re.findall(r"cudf\.Series\(\s*\[([^\]]*)\]", body)
+    nums = [[parse_number(t) for t in s.replace("\n", " ").split(",") if t.strip()]
+            for s in series]
+    xy, part, geom = nums[0], nums[1], nums[2]
+    radius = parse_number(re.search(r"s,\s*([0-9.]+),\s*#\s*expansion_radius", body).group(1))
+    minx, miny, maxx, maxy = nums[3:7]
+    return dict(source=rel, lx=xy[0::2], ly=xy[1::2], part_offset=part, geometry_offset=geom,
+                expansion_radius=radius, minx=minx, miny=miny, maxx=maxx, maxy=maxy)
+
+
+def main():
+    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    here = os.path.dirname(os.path.abspath(__file__))
+    outputs = {
+        "point_quadtree.json": quadtree_kats(root),
+        "quadtree_point_in_polygon_small.json": pip_small_kat(root),
+        "quadtree_point_to_nearest_linestring_small.json": nearest_small_kat(root),
+        "point_in_polygon.json": point_in_polygon_kats(root),
+        "linestring_bounding_boxes_small.json": linestring_bbox_kat(root),
+    }
+    for name, data in outputs.items():
+        with open(os.path.join(here, name), "w") as f:
+            json.dump(data, f, indent=1)
+        print("wrote", name)
+
+
+if __name__ == "__main__":
+    main()
