@@ -1,0 +1,24 @@
+"""GB300-native (sm_103a) quadtree spatial join with cuSpatial's API.
+
+Functions mirror cuspatial.quadtree_on_points, polygon_bounding_boxes,
+linestring_bounding_boxes, join_quadtree_and_bounding_boxes,
+quadtree_point_in_polygon and quadtree_point_to_nearest_linestring; they run
+hand-written CUDA kernels in libcuspatial_gb300.so through its C ABI.
+"""
+
+from .api import (join_quadtree_and_bounding_boxes, last_refined_count,
+                  linestring_bounding_boxes, polygon_bounding_boxes, quadtree_on_points,
+                  quadtree_point_in_polygon, quadtree_point_to_nearest_linestring)
+from .geoseries import GeoSeries, Table
+
+__all__ = [
+    "GeoSeries",
+    "Table",
+    "join_quadtree_and_bounding_boxes",
+    "last_refined_count",
+    "linestring_bounding_boxes",
+    "polygon_bounding_boxes",
+    "quadtree_on_points",
+    "quadtree_point_in_polygon",
+    "quadtree_point_to_nearest_linestring",
+]

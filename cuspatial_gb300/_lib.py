@@ -1,0 +1,167 @@
+"""ctypes binding of libcuspatial_gb300.so plus a torch-backed device allocator.
+
+All device memory the library asks for (outputs and scratch) is taken from
+torch's caching allocator on the current stream, so results come back as
+torch tensors without a copy.  There is no CPU fallback: when the shared
+library cannot be loaded or built, every call raises.
+"""
+
+import ctypes
+import os
+import threading
+
+import torch
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libcuspatial_gb300.so")
+
+OK, INVALID_ARGUMENT, OUT_OF_MEMORY, CUDA_ERROR, TIMEOUT, UNSUPPORTED = range(6)
+FLOAT32, FLOAT64 = 0, 1
+METHOD_EXACT, METHOD_FILTERED = 0, 1
+
+_vp = ctypes.c_void_p
+_sz = ctypes.c_size_t
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+
+ALLOC_FN = ctypes.CFUNCTYPE(_vp, _vp, _sz, _vp)
+FREE_FN = ctypes.CFUNCTYPE(None, _vp, _vp, _sz, _vp)
+
+
+class CsptAllocator(ctypes.Structure):
+    _fields_ = [("ctx", _vp), ("allocate", ALLOC_FN), ("deallocate", FREE_FN)]
+
+
+class CsptQuadtree(ctypes.Structure):
+    _fields_ = [("key", _vp), ("level", _vp), ("is_internal_node", _vp), ("length", _vp),
+                ("offset", _vp), ("num_nodes", _sz)]
+
+
+class CuspatialError(RuntimeError):
+    """Raised for CUDA, allocation and timeout failures reported by the library."""
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def _declare(lib):
+    lib.cspt_last_error_message.restype = ctypes.c_char_p
+    lib.cspt_version.restype = ctypes.c_char_p
+    lib.cspt_last_refined_count.restype = ctypes.c_uint64
+    lib.cspt_free.argtypes = [ctypes.POINTER(CsptAllocator), _vp, _sz, _vp]
+    lib.cspt_quadtree_free.argtypes = [ctypes.POINTER(CsptAllocator),
+                                       ctypes.POINTER(CsptQuadtree), _vp]
+    lib.cspt_quadtree_on_points.argtypes = [
+        _vp, _vp, _sz, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+        ctypes.c_double, ctypes.c_double, ctypes.c_int8, ctypes.c_int32,
+        ctypes.POINTER(CsptAllocator), _vp, ctypes.POINTER(_vp), ctypes.POINTER(CsptQuadtree)]
+    lib.cspt_polygon_bounding_boxes.argtypes = [
+        _vp, _sz, _vp, _sz, _vp, _vp, _sz, ctypes.c_int, ctypes.c_double, _vp, _vp, _vp, _vp, _vp]
+    lib.cspt_linestring_bounding_boxes.argtypes = [
+        _vp, _sz, _vp, _vp, _sz, ctypes.c_int, ctypes.c_double, _vp, _vp, _vp, _vp, _vp]
+    lib.cspt_join_quadtree_and_bounding_boxes.argtypes = [
+        ctypes.POINTER(CsptQuadtree), _vp, _vp, _vp, _vp, _sz, ctypes.c_int, ctypes.c_double,
+        ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int8,
+        ctypes.POINTER(CsptAllocator), _vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp),
+        ctypes.POINTER(_sz)]
+    lib.cspt_quadtree_point_in_polygon.argtypes = [
+        _vp, _vp, _sz, ctypes.POINTER(CsptQuadtree), _vp, _sz, _vp, _vp, _sz, _vp, _sz, _vp, _sz,
+        _vp, _vp, _sz, ctypes.c_int, ctypes.c_int, ctypes.POINTER(CsptAllocator), _vp,
+        ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_sz)]
+    lib.cspt_quadtree_point_to_nearest_linestring.argtypes = [
+        _vp, _vp, _sz, ctypes.POINTER(CsptQuadtree), _vp, _sz, _vp, _vp, _sz, _vp, _sz, _vp, _vp,
+        _sz, ctypes.c_int, ctypes.c_int, ctypes.POINTER(CsptAllocator), _vp, _vp, _vp, _vp,
+        ctypes.POINTER(_sz)]
+    for name in ("cspt_quadtree_on_points", "cspt_polygon_bounding_boxes",
+                 "cspt_linestring_bounding_boxes", "cspt_join_quadtree_and_bounding_boxes",
+                 "cspt_quadtree_point_in_polygon", "cspt_quadtree_point_to_nearest_linestring"):
+        getattr(lib, name).restype = ctypes.c_int
+    return lib
+
+
+def load(build_if_missing=True):
+    """Loads the shared library (building it in-tree first if needed)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        from . import build as _build
+        if build_if_missing and not _build.up_to_date():
+            _build.build()
+        if not os.path.exists(LIB_PATH):
+            raise CuspatialError("libcuspatial_gb300.so is not built (run cuspatial_gb300.build)")
+        _lib = _declare(ctypes.CDLL(LIB_PATH))
+        return _lib
+
+
+def check(status, lib=None):
+    if status == OK:
+        return
+    lib = lib or load()
+    msg = lib.cspt_last_error_message().decode()
+    if status == INVALID_ARGUMENT:
+        # cuspatial::logic_error surfaces as RuntimeError through Cython
+        raise RuntimeError(msg)
+    if status == UNSUPPORTED:
+        raise TypeError(msg)
+    if status == OUT_OF_MEMORY:
+        raise MemoryError(msg)
+    raise CuspatialError(msg)
+
+
+class TorchAllocator:
+    """cspt_allocator whose memory comes from torch's caching allocator.
+
+    Blocks handed to the library are kept alive in a dict until the library
+    frees them or the caller adopts them as output tensors.  An optional byte
+    budget makes allocations beyond it fail (the library then reports
+    OUT_OF_MEMORY), which lets callers admit work by memory.
+    """
+
+    def __init__(self, device=None, budget_bytes=None):
+        self.device = torch.device(device) if device is not None else torch.device(
+            "cuda", torch.cuda.current_device())
+        self.budget = budget_bytes
+        self.in_use = 0
+        self.peak = 0
+        self.blocks = {}
+        self._alloc_cb = ALLOC_FN(self._allocate)
+        self._free_cb = FREE_FN(self._deallocate)
+        self.struct = CsptAllocator(None, self._alloc_cb, self._free_cb)
+        self.ref = ctypes.byref(self.struct)
+
+    def _allocate(self, ctx, nbytes, stream):
+        try:
+            if self.budget is not None and self.in_use + nbytes > self.budget:
+                return None
+            t = torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=self.device)
+        except Exception:  # noqa: BLE001 - out of memory: report NULL to the library
+            return None
+        p = t.data_ptr()
+        self.blocks[p] = t
+        self.in_use += int(nbytes)
+        self.peak = max(self.peak, self.in_use)
+        return p
+
+    def _deallocate(self, ctx, ptr, nbytes, stream):
+        t = self.blocks.pop(ptr, None)
+        if t is not None:
+            self.in_use -= int(nbytes)
+
+    def adopt(self, ptr, count, dtype):
+        """Takes ownership of a library-allocated block as a typed tensor."""
+        if not ptr or count == 0:
+            return torch.empty(0, dtype=dtype, device=self.device)
+        t = self.blocks.pop(ptr)
+        nbytes = count * torch.empty(0, dtype=dtype).element_size()
+        self.in_use -= t.numel()
+        return t[:nbytes].view(dtype)
+
+
+def stream_ptr(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None and t.numel() else None

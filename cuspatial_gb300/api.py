@@ -1,0 +1,246 @@
+"""cuSpatial-compatible Python API over the C ABI.
+
+Signatures, argument handling (min/max swapping, scale clamping with a
+warning, geometry-type checks) and column names follow
+python/cuspatial/cuspatial/core/spatial/indexing.py:15-199,
+join.py:105-355 and bounding.py:19-140.  The `method` keyword (exact or
+filtered float32+float64 arithmetic) is an addition; it never changes results.
+"""
+
+import ctypes
+import warnings
+
+import torch
+
+from . import _lib
+from .geoseries import (GeoSeries, Table, as_device_tensor, contains_only_linestrings,
+                        contains_only_points, contains_only_polygons)
+
+_METHODS = {"exact": _lib.METHOD_EXACT, "filtered": _lib.METHOD_FILTERED}
+
+
+def _dtype_code(t):
+    if t.dtype == torch.float64:
+        return _lib.FLOAT64
+    if t.dtype == torch.float32:
+        return _lib.FLOAT32
+    raise TypeError("Only floating-point types are supported")
+
+
+def _tree_struct(quadtree):
+    """Table of the 5 quadtree columns -> (CsptQuadtree, tensors kept alive)."""
+    cols = [quadtree["key"], quadtree["level"], quadtree["is_internal_node"],
+            quadtree["length"], quadtree["offset"]]
+    key = as_device_tensor(cols[0], dtype=torch.int32).view(torch.int32)
+    lev = as_device_tensor(cols[1], dtype=torch.uint8)
+    isi = as_device_tensor(cols[2]).to(torch.uint8).contiguous()
+    ln = as_device_tensor(cols[3], dtype=torch.int32)
+    of = as_device_tensor(cols[4], dtype=torch.int32)
+    keep = (key, lev, isi, ln, of)
+    st = _lib.CsptQuadtree(key.data_ptr() or None, lev.data_ptr() or None,
+                           isi.data_ptr() or None, ln.data_ptr() or None,
+                           of.data_ptr() or None, int(key.numel()))
+    return st, keep
+
+
+def _u32(t):
+    """uint32 data carried in an int32 tensor (torch has limited uint32 ops)."""
+    return as_device_tensor(t).to(torch.int32) if t.dtype not in (torch.int32,) else t
+
+
+def _adopt_u32(alloc, p, n):
+    return alloc.adopt(p, n, torch.int32)
+
+
+def quadtree_on_points(points: GeoSeries, x_min, x_max, y_min, y_max, scale, max_depth,
+                       max_size):
+    """Construct a quadtree on points (reference: core/spatial/indexing.py:15).
+
+    Returns (point_indices, quadtree): point_indices maps sorted positions to
+    input point indices; quadtree holds key, level, is_internal_node, length
+    and offset.  uint32 columns are returned in int32 tensors (same bits).
+    """
+    if not len(points) == 0 and not contains_only_points(points):
+        raise ValueError("GeoSeries must contain only points.")
+    lib = _lib.load()
+    x_min, x_max, y_min, y_max = (min(x_min, x_max), max(x_min, x_max), min(y_min, y_max),
+                                  max(y_min, y_max))
+    min_scale = max(x_max - x_min, y_max - y_min) / ((1 << max_depth) + 2)
+    if scale < min_scale:
+        warnings.warn("scale {} is less than required minimum ".format(scale) +
+                      "scale {}. Clamping to minimum scale".format(min_scale))
+    xs = points.points.x if len(points) else torch.empty(0, dtype=torch.float64, device="cuda")
+    ys = points.points.y if len(points) else xs
+    alloc = _lib.TorchAllocator(xs.device)
+    pi = ctypes.c_void_p()
+    tree = _lib.CsptQuadtree()
+    _lib.check(lib.cspt_quadtree_on_points(
+        _lib.ptr(xs), _lib.ptr(ys), int(xs.numel()), _dtype_code(xs), float(x_min), float(x_max),
+        float(y_min), float(y_max), float(max(scale, min_scale)), int(max_depth), int(max_size),
+        alloc.ref, _lib.stream_ptr(), ctypes.byref(pi), ctypes.byref(tree)), lib)
+    n = int(xs.numel())
+    q = int(tree.num_nodes)
+    point_indices = alloc.adopt(pi.value, n, torch.int32)
+    qt = Table()
+    qt["key"] = alloc.adopt(tree.key, q, torch.int32)
+    qt["level"] = alloc.adopt(tree.level, q, torch.uint8)
+    qt["is_internal_node"] = alloc.adopt(tree.is_internal_node, q, torch.uint8).view(torch.bool)
+    qt["length"] = alloc.adopt(tree.length, q, torch.int32)
+    qt["offset"] = alloc.adopt(tree.offset, q, torch.int32)
+    return point_indices, qt
+
+
+def _empty_boxes(dtype):
+    t = Table()
+    for k in ("minx", "miny", "maxx", "maxy"):
+        t[k] = torch.empty(0, dtype=dtype, device="cuda")
+    return t
+
+
+def polygon_bounding_boxes(polygons: GeoSeries):
+    """Per-polygon bounding boxes (reference: core/spatial/bounding.py:19)."""
+    if len(polygons) == 0:
+        return _empty_boxes(torch.float64)
+    if not contains_only_polygons(polygons):
+        raise ValueError("Geoseries must contain only polygons.")
+    lib = _lib.load()
+    p = polygons.polygons
+    n = int(p.part_offset.numel()) - 1
+    out = Table()
+    for k in ("minx", "miny", "maxx", "maxy"):
+        out[k] = torch.empty(n, dtype=p.x.dtype, device=p.x.device)
+    _lib.check(lib.cspt_polygon_bounding_boxes(
+        _lib.ptr(p.part_offset), int(p.part_offset.numel()), _lib.ptr(p.ring_offset),
+        int(p.ring_offset.numel()), _lib.ptr(p.x), _lib.ptr(p.y), int(p.x.numel()),
+        _dtype_code(p.x), 0.0, *[_lib.ptr(v) for v in out.values()], _lib.stream_ptr()), lib)
+    return out
+
+
+def linestring_bounding_boxes(linestrings: GeoSeries, expansion_radius: float):
+    """Per-linestring bounding boxes expanded by a radius (bounding.py:89)."""
+    if len(linestrings) == 0:
+        return _empty_boxes(torch.float64)
+    if not contains_only_linestrings(linestrings):
+        raise ValueError("Geoseries must contain only linestrings.")
+    lib = _lib.load()
+    ls = linestrings.lines
+    # part offsets of the first part of each geometry (bounding.py:125-127)
+    offsets = ls.part_offset[ls.geometry_offset.long()].contiguous()
+    n = int(offsets.numel()) - 1
+    out = Table()
+    for k in ("minx", "miny", "maxx", "maxy"):
+        out[k] = torch.empty(n, dtype=ls.x.dtype, device=ls.x.device)
+    _lib.check(lib.cspt_linestring_bounding_boxes(
+        _lib.ptr(offsets), int(offsets.numel()), _lib.ptr(ls.x), _lib.ptr(ls.y),
+        int(ls.x.numel()), _dtype_code(ls.x), float(expansion_radius),
+        *[_lib.ptr(v) for v in out.values()], _lib.stream_ptr()), lib)
+    return out
+
+
+def join_quadtree_and_bounding_boxes(quadtree, bounding_boxes, x_min, x_max, y_min, y_max,
+                                     scale, max_depth):
+    """(bbox, leaf quadrant) pairs that intersect (reference: join.py:105)."""
+    lib = _lib.load()
+    x_min, x_max, y_min, y_max = (min(x_min, x_max), max(x_min, x_max), min(y_min, y_max),
+                                  max(y_min, y_max))
+    min_scale = max(x_max - x_min, y_max - y_min) / ((1 << max_depth) + 2)
+    if scale < min_scale:
+        warnings.warn("scale {} is less than required minimum ".format(scale) +
+                      "scale {}. Clamping to minimum scale".format(min_scale))
+    st, keep = _tree_struct(quadtree)
+    b = [as_device_tensor(bounding_boxes[k]) for k in ("minx", "miny", "maxx", "maxy")]
+    alloc = _lib.TorchAllocator(b[0].device)
+    ob, oq, nn = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_size_t()
+    _lib.check(lib.cspt_join_quadtree_and_bounding_boxes(
+        ctypes.byref(st), *[_lib.ptr(v) for v in b], int(b[0].numel()), _dtype_code(b[0]),
+        float(x_min), float(x_max), float(y_min), float(y_max), float(max(scale, min_scale)),
+        int(max_depth), alloc.ref, _lib.stream_ptr(), ctypes.byref(ob), ctypes.byref(oq),
+        ctypes.byref(nn)), lib)
+    del keep
+    n = int(nn.value)
+    out = Table()
+    out["bbox_offset"] = alloc.adopt(ob.value, n, torch.int32)
+    out["quad_offset"] = alloc.adopt(oq.value, n, torch.int32)
+    return out
+
+
+def quadtree_point_in_polygon(poly_quad_pairs, quadtree, point_indices, points: GeoSeries,
+                              polygons: GeoSeries, method="exact"):
+    """Points inside polygons, using (polygon, quadrant) pairs (join.py:177).
+
+    point_index in the result is a position in point_indices (an index to an
+    index), as in the reference.  method="filtered" runs the float32 filter
+    with float64 refinement; the pairs are identical to method="exact".
+    """
+    if not contains_only_points(points):
+        raise ValueError("`point` Geoseries must contains only point geometries.")
+    if not contains_only_polygons(polygons):
+        raise ValueError("`polygons` Geoseries must contains only polygons geometries.")
+    lib = _lib.load()
+    st, keep = _tree_struct(quadtree)
+    pp = as_device_tensor(poly_quad_pairs["bbox_offset"] if "bbox_offset" in poly_quad_pairs
+                          else poly_quad_pairs["polygon_index"], dtype=torch.int32)
+    pq = as_device_tensor(poly_quad_pairs["quad_offset"], dtype=torch.int32)
+    pi = as_device_tensor(point_indices, dtype=torch.int32)
+    pts = points.points
+    poly = polygons.polygons
+    alloc = _lib.TorchAllocator(pts.x.device)
+    op, oq, nn = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_size_t()
+    _lib.check(lib.cspt_quadtree_point_in_polygon(
+        _lib.ptr(pp), _lib.ptr(pq), int(pp.numel()), ctypes.byref(st), _lib.ptr(pi),
+        int(pi.numel()), _lib.ptr(pts.x), _lib.ptr(pts.y), int(pts.x.numel()),
+        _lib.ptr(poly.part_offset), int(poly.part_offset.numel()), _lib.ptr(poly.ring_offset),
+        int(poly.ring_offset.numel()), _lib.ptr(poly.x), _lib.ptr(poly.y), int(poly.x.numel()),
+        _dtype_code(pts.x), _METHODS[method], alloc.ref, _lib.stream_ptr(), ctypes.byref(op),
+        ctypes.byref(oq), ctypes.byref(nn)), lib)
+    del keep
+    n = int(nn.value)
+    out = Table()
+    out["polygon_index"] = alloc.adopt(op.value, n, torch.int32)
+    out["point_index"] = alloc.adopt(oq.value, n, torch.int32)
+    return out
+
+
+def quadtree_point_to_nearest_linestring(linestring_quad_pairs, quadtree, point_indices,
+                                         points: GeoSeries, linestrings: GeoSeries,
+                                         method="exact"):
+    """Nearest linestring of each point in the paired quadrants (join.py:265)."""
+    if not contains_only_points(points):
+        raise ValueError("`point` Geoseries must contains only point geometries.")
+    if not contains_only_linestrings(linestrings):
+        raise ValueError("`linestrings` Geoseries must contains only linestring geometries.")
+    ls = linestrings.lines
+    if int(ls.part_offset.numel()) != int(ls.geometry_offset.numel()):
+        raise ValueError("GeoSeries cannot contain multilinestrings.")
+    lib = _lib.load()
+    st, keep = _tree_struct(quadtree)
+    pl = as_device_tensor(linestring_quad_pairs["bbox_offset"] if "bbox_offset" in
+                          linestring_quad_pairs else linestring_quad_pairs["linestring_index"],
+                          dtype=torch.int32)
+    pq = as_device_tensor(linestring_quad_pairs["quad_offset"], dtype=torch.int32)
+    pi = as_device_tensor(point_indices, dtype=torch.int32)
+    pts = points.points
+    n = int(pi.numel())
+    o_pt = torch.empty(n, dtype=torch.int32, device=pts.x.device)
+    o_ls = torch.empty(n, dtype=torch.int32, device=pts.x.device)
+    o_d = torch.empty(n, dtype=pts.x.dtype, device=pts.x.device)
+    alloc = _lib.TorchAllocator(pts.x.device)
+    rows = ctypes.c_size_t()
+    _lib.check(lib.cspt_quadtree_point_to_nearest_linestring(
+        _lib.ptr(pl), _lib.ptr(pq), int(pl.numel()), ctypes.byref(st), _lib.ptr(pi), n,
+        _lib.ptr(pts.x), _lib.ptr(pts.y), int(pts.x.numel()), _lib.ptr(ls.part_offset),
+        int(ls.part_offset.numel()), _lib.ptr(ls.x), _lib.ptr(ls.y), int(ls.x.numel()),
+        _dtype_code(pts.x), _METHODS[method], alloc.ref, _lib.stream_ptr(), _lib.ptr(o_pt),
+        _lib.ptr(o_ls), _lib.ptr(o_d), ctypes.byref(rows)), lib)
+    del keep
+    r = int(rows.value)
+    out = Table()
+    out["point_index"] = o_pt[:r]
+    out["linestring_index"] = o_ls[:r]
+    out["distance"] = o_d[:r]
+    return out
+
+
+def last_refined_count():
+    """Candidates re-evaluated in float64 by the last filtered PiP call."""
+    return int(_lib.load().cspt_last_refined_count())

@@ -1,0 +1,355 @@
+// extern "C" entry points: argument validation and empty-input rules of the
+// libcuspatial column API, then dispatch to the kernels.
+#include <atomic>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+
+namespace cspt {
+
+// defined in the kernel translation units
+void quadtree_on_points(void const* x, void const* y, size_t n, cspt_dtype dtype, double x_min,
+                        double x_max, double y_min, double y_max, double scale, int max_depth,
+                        int32_t max_size, Allocator const& alloc, uint32_t** out_point_indices,
+                        cspt_quadtree* out_tree);
+void polygon_bounding_boxes(uint32_t const* poly_offsets, size_t npo,
+                            uint32_t const* ring_offsets, size_t nro, void const* x,
+                            void const* y, size_t nv, cspt_dtype dtype, double r, void* ominx,
+                            void* ominy, void* omaxx, void* omaxy, Allocator const& alloc);
+void linestring_bounding_boxes(uint32_t const* ls_offsets, size_t nlo, void const* x,
+                               void const* y, size_t nv, cspt_dtype dtype, double r, void* ominx,
+                               void* ominy, void* omaxx, void* omaxy, Allocator const& alloc);
+void join_quadtree_and_bounding_boxes(cspt_quadtree const* tree, void const* bminx,
+                                      void const* bminy, void const* bmaxx, void const* bmaxy,
+                                      size_t nb, cspt_dtype dtype, double x_min, double y_min,
+                                      double scale, int max_depth, Allocator const& alloc,
+                                      uint32_t** out_box, uint32_t** out_node, size_t* out_n);
+void quadtree_point_in_polygon(uint32_t const* pair_poly, uint32_t const* pair_quad,
+                               size_t npairs, cspt_quadtree const* tree,
+                               uint32_t const* point_indices, size_t npi, void const* x,
+                               void const* y, uint32_t const* po, size_t npo, uint32_t const* ro,
+                               size_t nro, void const* vx, void const* vy, size_t nv,
+                               cspt_dtype dtype, cspt_method method, Allocator const& alloc,
+                               uint32_t** out_poly, uint32_t** out_point, size_t* out_n,
+                               uint64_t* out_refined);
+void quadtree_point_to_nearest_linestring(uint32_t const* pair_ls, uint32_t const* pair_quad,
+                                          size_t npairs, cspt_quadtree const* tree,
+                                          uint32_t const* point_indices, size_t npi,
+                                          void const* x, void const* y, uint32_t const* lso,
+                                          size_t nlso, void const* lx, void const* ly,
+                                          cspt_dtype dtype, cspt_method method,
+                                          Allocator const& alloc, uint32_t* opt, uint32_t* ols,
+                                          void* od);
+
+namespace {
+thread_local std::string t_last_error;
+thread_local uint64_t t_last_refined = 0;
+
+void check_dtype(cspt_dtype dtype)
+{
+  if (dtype != CSPT_FLOAT32 && dtype != CSPT_FLOAT64)
+    throw Error{CSPT_UNSUPPORTED, "Only floating-point types are supported"};
+}
+cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+}  // namespace
+
+void set_last_error(std::string const& msg) { t_last_error = msg; }
+void clear_last_error() { t_last_error.clear(); }
+
+int num_sms()
+{
+  static int sms = [] {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 152;
+  }();
+  return sms;
+}
+
+uint64_t last_refined() { return t_last_refined; }
+
+namespace {
+std::atomic<uint64_t> g_launches{0};
+std::atomic<int> g_profile{0};
+std::mutex g_prof_mu;
+struct Pending {
+  std::string name;
+  cudaEvent_t start, stop;
+};
+std::vector<Pending> g_pending;
+std::map<std::string, std::pair<double, uint64_t>> g_totals;
+
+void resolve_pending()
+{
+  for (auto& p : g_pending) {
+    float ms = 0.0f;
+    if (cudaEventSynchronize(p.stop) == cudaSuccess &&
+        cudaEventElapsedTime(&ms, p.start, p.stop) == cudaSuccess) {
+      auto& t = g_totals[p.name];
+      t.first += ms;
+      t.second += 1;
+    }
+    cudaEventDestroy(p.start);
+    cudaEventDestroy(p.stop);
+  }
+  g_pending.clear();
+  (void)cudaGetLastError();
+}
+}  // namespace
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+KernelTimer::KernelTimer(char const* name, cudaStream_t stream) : name_(name), stream_(stream)
+{
+  if (!g_profile.load(std::memory_order_relaxed)) return;
+  if (cudaEventCreate(&start_) != cudaSuccess || cudaEventCreate(&stop_) != cudaSuccess) {
+    (void)cudaGetLastError();
+    start_ = stop_ = nullptr;
+    return;
+  }
+  cudaEventRecord(start_, stream_);
+}
+
+KernelTimer::~KernelTimer()
+{
+  if (!start_) return;
+  cudaEventRecord(stop_, stream_);
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_pending.push_back(Pending{name_, start_, stop_});
+}
+
+}  // namespace cspt
+
+using namespace cspt;
+
+extern "C" {
+
+const char* cspt_last_error_message(void) { return t_last_error.c_str(); }
+
+const char* cspt_version(void) { return "cuspatial_gb300 0.1 (sm_103a)"; }
+
+// Diagnostics without a reference counterpart: kernel launch counter and
+// event timing of the named kernels (pip_bits, pip_expand, join_count,
+// join_write, nearest, quadtree_build).
+uint64_t cspt_launch_count(void) { return g_launches.load(); }
+
+void cspt_profile_enable(int on)
+{
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  resolve_pending();
+  g_totals.clear();
+  g_profile.store(on ? 1 : 0);
+}
+
+int cspt_profile_read(const char* name, double* total_ms, uint64_t* launches)
+{
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  resolve_pending();
+  auto it = g_totals.find(name ? name : "");
+  if (it == g_totals.end()) {
+    if (total_ms) *total_ms = 0.0;
+    if (launches) *launches = 0;
+    return 0;
+  }
+  if (total_ms) *total_ms = it->second.first;
+  if (launches) *launches = it->second.second;
+  return 1;
+}
+
+// Candidates re-evaluated in float64 by the last filtered point-in-polygon
+// call on this thread (diagnostic; not part of the reference interface).
+uint64_t cspt_last_refined_count(void) { return t_last_refined; }
+
+void cspt_free(const cspt_allocator* mr, void* ptr, size_t bytes, void* stream)
+{
+  Allocator(mr, as_stream(stream)).deallocate(ptr, bytes);
+}
+
+void cspt_quadtree_free(const cspt_allocator* mr, cspt_quadtree* tree, void* stream)
+{
+  if (!tree) return;
+  Allocator a(mr, as_stream(stream));
+  size_t const q = tree->num_nodes;
+  a.deallocate(tree->key, q * 4);
+  a.deallocate(tree->level, q);
+  a.deallocate(tree->is_internal_node, q);
+  a.deallocate(tree->length, q * 4);
+  a.deallocate(tree->offset, q * 4);
+  *tree = cspt_quadtree{nullptr, nullptr, nullptr, nullptr, nullptr, 0};
+}
+
+cspt_status cspt_quadtree_on_points(const void* x, const void* y, size_t num_points,
+                                    cspt_dtype dtype, double x_min, double x_max, double y_min,
+                                    double y_max, double scale, int8_t max_depth,
+                                    int32_t max_size, const cspt_allocator* mr, void* stream,
+                                    uint32_t** out_point_indices, cspt_quadtree* out_tree)
+{
+  return guarded([&] {
+    CSPT_EXPECTS(out_point_indices && out_tree, "output pointers must not be null");
+    *out_point_indices = nullptr;
+    *out_tree          = cspt_quadtree{nullptr, nullptr, nullptr, nullptr, nullptr, 0};
+    check_dtype(dtype);
+    if (num_points == 0) return;  // point_quadtree.cu:167-177
+    CSPT_EXPECTS(x && y, "x and y columns must have the same length");
+    Allocator alloc(mr, as_stream(stream));
+    quadtree_on_points(x, y, num_points, dtype, x_min, x_max, y_min, y_max, scale, max_depth,
+                       max_size, alloc, out_point_indices, out_tree);
+  });
+}
+
+cspt_status cspt_polygon_bounding_boxes(const uint32_t* poly_offsets, size_t num_poly_offsets,
+                                        const uint32_t* ring_offsets, size_t num_ring_offsets,
+                                        const void* x, const void* y, size_t num_vertices,
+                                        cspt_dtype dtype, double expansion_radius,
+                                        void* out_min_x, void* out_min_y, void* out_max_x,
+                                        void* out_max_y, void* stream)
+{
+  return guarded([&] {
+    check_dtype(dtype);
+    size_t const np = num_poly_offsets > 0 ? num_poly_offsets - 1 : 0;
+    if (np == 0) return;  // polygon_bounding_boxes.cu:147-155
+    // CUSPATIAL_EXPECTS_VALID_POLYGON_SIZES (detail/utility/validation.hpp:87-92)
+    CSPT_EXPECTS(num_poly_offsets > 0, "Polygon offsets must contain at least one (1) value");
+    CSPT_EXPECTS(num_ring_offsets > 0,
+                 "Polygon ring offsets must contain at least one (1) value");
+    if (num_ring_offsets < 2 || num_vertices == 0) {
+      // bounding_boxes.cuh:166: no rings or no vertices -> nothing written
+      return;
+    }
+    Allocator alloc(nullptr, as_stream(stream));
+    polygon_bounding_boxes(poly_offsets, num_poly_offsets, ring_offsets, num_ring_offsets, x, y,
+                           num_vertices, dtype, expansion_radius, out_min_x, out_min_y,
+                           out_max_x, out_max_y, alloc);
+  });
+}
+
+cspt_status cspt_linestring_bounding_boxes(const uint32_t* linestring_offsets,
+                                           size_t num_linestring_offsets, const void* x,
+                                           const void* y, size_t num_vertices, cspt_dtype dtype,
+                                           double expansion_radius, void* out_min_x,
+                                           void* out_min_y, void* out_max_x, void* out_max_y,
+                                           void* stream)
+{
+  return guarded([&] {
+    check_dtype(dtype);
+    size_t const nl = num_linestring_offsets > 0 ? num_linestring_offsets - 1 : 0;
+    // linestring_bounding_boxes.cu:135-141
+    CSPT_EXPECTS(expansion_radius >= 0, "expansion radius must be greater or equal than 0");
+    CSPT_EXPECTS(num_vertices >= 2 * nl, "all linestrings must have at least 2 vertices");
+    if (num_linestring_offsets == 0 || num_vertices == 0 || nl == 0) return;
+    Allocator alloc(nullptr, as_stream(stream));
+    linestring_bounding_boxes(linestring_offsets, num_linestring_offsets, x, y, num_vertices,
+                              dtype, expansion_radius, out_min_x, out_min_y, out_max_x,
+                              out_max_y, alloc);
+  });
+}
+
+cspt_status cspt_join_quadtree_and_bounding_boxes(
+  const cspt_quadtree* tree, const void* bbox_min_x, const void* bbox_min_y,
+  const void* bbox_max_x, const void* bbox_max_y, size_t num_bboxes, cspt_dtype dtype,
+  double x_min, double x_max, double y_min, double y_max, double scale, int8_t max_depth,
+  const cspt_allocator* mr, void* stream, uint32_t** out_bbox_offset,
+  uint32_t** out_quad_offset, size_t* out_num_pairs)
+{
+  return guarded([&] {
+    CSPT_EXPECTS(out_bbox_offset && out_quad_offset && out_num_pairs,
+                 "output pointers must not be null");
+    *out_bbox_offset = nullptr;
+    *out_quad_offset = nullptr;
+    *out_num_pairs   = 0;
+    CSPT_EXPECTS(tree, "quadtree table must have 5 columns");
+    check_dtype(dtype);
+    // quadtree_bbox_filtering.cu:100-106
+    CSPT_EXPECTS(scale > 0, "scale must be positive");
+    CSPT_EXPECTS(x_min < x_max && y_min < y_max,
+                 "invalid bounding box (x_min, x_max, y_min, y_max)");
+    CSPT_EXPECTS(max_depth > 0 && max_depth < 16,
+                 "maximum depth must be positive and less than 16");
+    if (tree->num_nodes == 0 || num_bboxes == 0) return;  // :108-114
+    Allocator alloc(mr, as_stream(stream));
+    join_quadtree_and_bounding_boxes(tree, bbox_min_x, bbox_min_y, bbox_max_x, bbox_max_y,
+                                     num_bboxes, dtype, x_min, y_min, scale, max_depth, alloc,
+                                     out_bbox_offset, out_quad_offset, out_num_pairs);
+  });
+}
+
+cspt_status cspt_quadtree_point_in_polygon(
+  const uint32_t* pair_polygon, const uint32_t* pair_quad, size_t num_pairs,
+  const cspt_quadtree* tree, const uint32_t* point_indices, size_t num_point_indices,
+  const void* x, const void* y, size_t num_points, const uint32_t* poly_offsets,
+  size_t num_poly_offsets, const uint32_t* ring_offsets, size_t num_ring_offsets,
+  const void* poly_x, const void* poly_y, size_t num_poly_vertices, cspt_dtype dtype,
+  cspt_method method, const cspt_allocator* mr, void* stream, uint32_t** out_polygon_index,
+  uint32_t** out_point_index, size_t* out_num_pairs)
+{
+  return guarded([&] {
+    CSPT_EXPECTS(out_polygon_index && out_point_index && out_num_pairs,
+                 "output pointers must not be null");
+    *out_polygon_index = nullptr;
+    *out_point_index   = nullptr;
+    *out_num_pairs     = 0;
+    t_last_refined     = 0;
+    CSPT_EXPECTS(tree, "a quadtree table must have 5 columns");
+    check_dtype(dtype);
+    // quadtree_point_in_polygon.cu:154-169
+    CSPT_EXPECTS(num_point_indices == num_points,
+                 "number of points must be the same for both x and y columns");
+    CSPT_EXPECTS(method == CSPT_METHOD_EXACT || method == CSPT_METHOD_FILTERED,
+                 "unknown point-in-polygon method");
+    // :171-178
+    if (num_pairs == 0 || tree->num_nodes == 0 || num_point_indices == 0 ||
+        num_poly_offsets == 0)
+      return;
+    CSPT_EXPECTS(num_ring_offsets > 0,
+                 "Polygon ring offsets must contain at least one (1) value");
+    Allocator alloc(mr, as_stream(stream));
+    uint64_t refined = 0;
+    quadtree_point_in_polygon(pair_polygon, pair_quad, num_pairs, tree, point_indices,
+                              num_point_indices, x, y, poly_offsets, num_poly_offsets,
+                              ring_offsets, num_ring_offsets, poly_x, poly_y, num_poly_vertices,
+                              dtype, method, alloc, out_polygon_index, out_point_index,
+                              out_num_pairs, &refined);
+    t_last_refined = refined;
+  });
+}
+
+cspt_status cspt_quadtree_point_to_nearest_linestring(
+  const uint32_t* pair_linestring, const uint32_t* pair_quad, size_t num_pairs,
+  const cspt_quadtree* tree, const uint32_t* point_indices, size_t num_point_indices,
+  const void* x, const void* y, size_t num_points, const uint32_t* linestring_offsets,
+  size_t num_linestring_offsets, const void* ls_x, const void* ls_y, size_t num_ls_vertices,
+  cspt_dtype dtype, cspt_method method, const cspt_allocator* mr, void* stream,
+  uint32_t* out_point_index, uint32_t* out_linestring_index, void* out_distance,
+  size_t* out_num_rows)
+{
+  return guarded([&] {
+    (void)num_ls_vertices;
+    CSPT_EXPECTS(out_num_rows, "output pointers must not be null");
+    *out_num_rows = 0;
+    CSPT_EXPECTS(tree, "a quadtree table must have 5 columns");
+    check_dtype(dtype);
+    // quadtree_point_to_nearest_linestring.cu:153-165
+    CSPT_EXPECTS(num_point_indices == num_points,
+                 "number of points must be the same for both x and y columns");
+    CSPT_EXPECTS(method == CSPT_METHOD_EXACT || method == CSPT_METHOD_FILTERED,
+                 "unknown nearest-linestring method");
+    // :167-175
+    if (num_pairs == 0 || tree->num_nodes == 0 || num_point_indices == 0 ||
+        num_linestring_offsets == 0)
+      return;
+    CSPT_EXPECTS(out_point_index && out_linestring_index && out_distance,
+                 "output pointers must not be null");
+    Allocator alloc(mr, as_stream(stream));
+    quadtree_point_to_nearest_linestring(pair_linestring, pair_quad, num_pairs, tree,
+                                         point_indices, num_point_indices, x, y,
+                                         linestring_offsets, num_linestring_offsets, ls_x, ls_y,
+                                         dtype, method, alloc, out_point_index,
+                                         out_linestring_index, out_distance);
+    *out_num_rows = num_point_indices;
+  });
+}
+
+}  // extern "C"

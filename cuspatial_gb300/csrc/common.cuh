@@ -1,0 +1,267 @@
+// Shared host/device infrastructure of the sm_103a spatial-join library:
+// status handling, the caller-supplied allocator, and small device helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <type_traits>
+#include <utility>
+
+#include "../../include/cuspatial_gb300.h"
+
+namespace cspt {
+
+// ---------------------------------------------------------------------------
+// errors: the reference throws cuspatial::logic_error (CUSPATIAL_EXPECTS,
+// cpp/include/cuspatial/error.hpp:76) and cuspatial::cuda_error
+// (CUSPATIAL_CUDA_TRY, error.hpp:143); here they become a status plus a
+// per-thread message.
+// ---------------------------------------------------------------------------
+struct Error {
+  cspt_status status;
+  std::string message;
+};
+
+void set_last_error(std::string const& msg);
+void clear_last_error();
+
+#define CSPT_EXPECTS(cond, msg)                                               \
+  do {                                                                        \
+    if (!(cond)) throw ::cspt::Error{CSPT_INVALID_ARGUMENT, std::string(msg)}; \
+  } while (0)
+
+#define CSPT_CUDA_TRY(call)                                                          \
+  do {                                                                               \
+    cudaError_t const e_ = (call);                                                   \
+    if (e_ != cudaSuccess) {                                                         \
+      (void)cudaGetLastError();                                                      \
+      throw ::cspt::Error{e_ == cudaErrorMemoryAllocation ? CSPT_OUT_OF_MEMORY        \
+                                                          : CSPT_CUDA_ERROR,          \
+                          std::string("CUDA error at " __FILE__ ":") +               \
+                            std::to_string(__LINE__) + ": " + cudaGetErrorString(e_)}; \
+    }                                                                                \
+  } while (0)
+
+// Every kernel launch site is followed by CSPT_CHECK_LAUNCH(), which also
+// counts the launch (cspt_launch_count()).
+void count_launch();
+#define CSPT_CHECK_LAUNCH()                     \
+  do {                                          \
+    ::cspt::count_launch();                     \
+    CSPT_CUDA_TRY(cudaPeekAtLastError());       \
+  } while (0)
+
+// Optional event timing of named kernels on their launching stream
+// (cspt_profile_*): a no-op unless profiling is enabled.
+class KernelTimer {
+ public:
+  KernelTimer(char const* name, cudaStream_t stream);
+  ~KernelTimer();
+  KernelTimer(KernelTimer const&)            = delete;
+  KernelTimer& operator=(KernelTimer const&) = delete;
+
+ private:
+  char const* name_;
+  cudaStream_t stream_;
+  cudaEvent_t start_ = nullptr;
+  cudaEvent_t stop_  = nullptr;
+};
+
+// Runs `body`, turning exceptions into a status and the thread's message.
+template <typename F>
+cspt_status guarded(F&& body)
+{
+  try {
+    clear_last_error();
+    body();
+    return CSPT_OK;
+  } catch (Error const& e) {
+    set_last_error(e.message);
+    return e.status;
+  } catch (std::exception const& e) {
+    set_last_error(e.what());
+    return CSPT_CUDA_ERROR;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// memory: every device allocation goes through the caller's allocator, or
+// cudaMallocAsync/cudaFreeAsync when none is given.
+// ---------------------------------------------------------------------------
+class Allocator {
+ public:
+  Allocator(cspt_allocator const* mr, cudaStream_t stream) : mr_(mr), stream_(stream) {}
+  void* allocate(size_t bytes) const
+  {
+    if (bytes == 0) return nullptr;
+    void* p = nullptr;
+    if (mr_ && mr_->allocate) {
+      p = mr_->allocate(mr_->ctx, bytes, stream_);
+      if (!p) throw Error{CSPT_OUT_OF_MEMORY, "allocation of " + std::to_string(bytes) +
+                                                 " bytes failed (caller allocator)"};
+    } else {
+      cudaError_t const e = cudaMallocAsync(&p, bytes, stream_);
+      if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        throw Error{CSPT_OUT_OF_MEMORY,
+                    "allocation of " + std::to_string(bytes) + " bytes failed: " +
+                      cudaGetErrorString(e)};
+      }
+    }
+    return p;
+  }
+  void deallocate(void* p, size_t bytes) const
+  {
+    if (!p) return;
+    if (mr_ && mr_->deallocate) {
+      mr_->deallocate(mr_->ctx, p, bytes, stream_);
+    } else {
+      (void)cudaFreeAsync(p, stream_);
+    }
+  }
+  cudaStream_t stream() const { return stream_; }
+
+ private:
+  cspt_allocator const* mr_;
+  cudaStream_t stream_;
+};
+
+// Owning typed device buffer (freed on scope exit unless released).
+template <typename T>
+class Buffer {
+ public:
+  Buffer() = default;
+  Buffer(Allocator const& a, size_t n) : a_(&a), n_(n)
+  {
+    p_ = static_cast<T*>(a.allocate(n * sizeof(T)));
+  }
+  Buffer(Buffer&& o) noexcept : a_(o.a_), p_(o.p_), n_(o.n_)
+  {
+    o.p_ = nullptr;
+    o.n_ = 0;
+  }
+  Buffer& operator=(Buffer&& o) noexcept
+  {
+    reset();
+    a_   = o.a_;
+    p_   = o.p_;
+    n_   = o.n_;
+    o.p_ = nullptr;
+    o.n_ = 0;
+    return *this;
+  }
+  Buffer(Buffer const&)            = delete;
+  Buffer& operator=(Buffer const&) = delete;
+  ~Buffer() { reset(); }
+  void reset()
+  {
+    if (p_ && a_) a_->deallocate(p_, n_ * sizeof(T));
+    p_ = nullptr;
+    n_ = 0;
+  }
+  T* release()
+  {
+    T* p = p_;
+    p_   = nullptr;
+    n_   = 0;
+    return p;
+  }
+  T* data() const { return p_; }
+  size_t size() const { return n_; }
+
+ private:
+  Allocator const* a_ = nullptr;
+  T* p_               = nullptr;
+  size_t n_           = 0;
+};
+
+// Reads one device value back to the host (synchronises the stream).
+template <typename T>
+T read_back(T const* dev, cudaStream_t stream)
+{
+  T h{};
+  CSPT_CUDA_TRY(cudaMemcpyAsync(&h, dev, sizeof(T), cudaMemcpyDeviceToHost, stream));
+  CSPT_CUDA_TRY(cudaStreamSynchronize(stream));
+  return h;
+}
+
+inline unsigned grid_for(size_t n, unsigned block, unsigned cap = 1u << 20)
+{
+  size_t g = (n + block - 1) / block;
+  if (g < 1) g = 1;
+  if (g > cap) g = cap;
+  return static_cast<unsigned>(g);
+}
+
+int num_sms();
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+template <typename T>
+struct uint_of;
+template <>
+struct uint_of<float> {
+  using type = uint32_t;
+};
+template <>
+struct uint_of<double> {
+  using type = uint64_t;
+};
+
+// cpp/include/cuspatial/detail/utility/floating_point.cuh:97-129: two values
+// are equal when their biased integer images are at most 4 apart; NaN never
+// equals anything.
+template <typename T>
+__host__ __device__ inline bool float_equal(T a, T b)
+{
+  using U = typename uint_of<T>::type;
+  if (a != a || b != b) return false;
+  U ua, ub;
+  memcpy(&ua, &a, sizeof(T));
+  memcpy(&ub, &b, sizeof(T));
+  U const sign = U{1} << (8 * sizeof(U) - 1);
+  U const ba   = (ua & sign) ? U(~ua + 1) : U(ua | sign);
+  U const bb   = (ub & sign) ? U(~ub + 1) : U(ub | sign);
+  return (ba >= bb ? ba - bb : bb - ba) <= 4u;
+}
+
+// Morton interleave (cpp/include/cuspatial/detail/utility/z_order.cuh:69-94),
+// computed with shifts and masks.
+__host__ __device__ inline uint32_t spread16(uint32_t v)
+{
+  v &= 0xFFFFu;
+  v = (v | (v << 8)) & 0x00FF00FFu;
+  v = (v | (v << 4)) & 0x0F0F0F0Fu;
+  v = (v | (v << 2)) & 0x33333333u;
+  v = (v | (v << 1)) & 0x55555555u;
+  return v;
+}
+__host__ __device__ inline uint32_t gather16(uint32_t v)
+{
+  v &= 0x55555555u;
+  v = (v | (v >> 1)) & 0x33333333u;
+  v = (v | (v >> 2)) & 0x0F0F0F0Fu;
+  v = (v | (v >> 4)) & 0x00FF00FFu;
+  v = (v | (v >> 8)) & 0x0000FFFFu;
+  return v;
+}
+
+// Explicitly rounded arithmetic: the library is compiled with -fmad=false,
+// and the few products the reference's build contracts into FMAs are written
+// as fma_rn.
+__device__ inline double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ inline float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+template <typename T>
+__device__ inline T ldg(T const* p)
+{
+  return __ldg(p);
+}
+
+}  // namespace cspt

@@ -1,0 +1,87 @@
+// Device-resident polygon index used by the point-in-polygon join.
+//
+// For every polygon the index holds
+//   * its vertex bounding box and an anchor (box centre),
+//   * each vertex's edge (previous vertex -> vertex, ring-cyclic) as float32
+//     offsets from the anchor, plus the largest offset magnitude,
+//   * a partition of [ymin, ymax) into slabs, each listing the edges whose
+//     y-range (widened by a margin) meets the slab,
+//   * the sorted x values of its exactly vertical edges.
+//
+// Why this is exact against the reference's ring walk
+// (detail/algorithm/is_point_in_polygon.cuh:45-100):
+//   1. For coordinates of normal magnitude, float_equal(b - a, 0) holds only
+//      for b == a, and equality is transitive, so the reference's skipped
+//      vertices are exactly those equal to their predecessor and its edges
+//      are (p[i-1], p[i]) for the other vertices.  Polygons where a vertex
+//      difference is non-zero but within 4 ULP of zero (denormal scale) are
+//      flagged and always walked with the reference loop.
+//   2. The result is "no on-edge hit" AND the XOR of per-edge toggles, so the
+//      edges can be visited in any order and any subset that contains every
+//      edge able to toggle or to hit is enough.
+//   3. A point with py outside [ymin, ymax) sees equal y-flags on every edge:
+//      no toggle, result false.
+//   4. An edge toggles only if its y-range contains py; a non-vertical edge
+//      can be "collinear and within x-range" only if py lies within
+//      2^-48 * |rise| of its y-range.  The slab margin (2^-36 of the edge
+//      height plus 2^-40 of the polygon height, the latter also absorbing
+//      the slab-index rounding) covers both.
+//   5. An exactly vertical edge reports "on edge" for any py whenever
+//      px == its x (x-range check only, is_point_in_polygon.cuh:75-83); that
+//      case is caught by a lookup in the sorted vertical-x list.
+#pragma once
+
+#include "common.cuh"
+
+namespace cspt {
+
+template <typename T>
+struct PolygonIndexView {
+  // polygon topology (caller's arrays)
+  uint32_t const* poly_offsets;
+  uint32_t const* ring_offsets;
+  T const* vx;
+  T const* vy;
+  size_t num_polygons;
+  // per polygon
+  T const* pminx;
+  T const* pminy;
+  T const* pmaxx;
+  T const* pmaxy;
+  T const* anchor_x;
+  T const* anchor_y;
+  T const* inv_slab_h;       // slabs per unit of y
+  float const* max_offset;   // largest |float32 offset| over the polygon's vertices
+  uint32_t const* num_slabs;
+  uint32_t const* slab_base;  // first slab of the polygon in slab_start
+  uint8_t const* exact_only;  // 1: walk the reference loop, no index
+  uint32_t const* vert_begin;  // sorted vertical-edge x values, per polygon range
+  uint32_t const* vert_end;
+  T const* vert_x;
+  float const* vert_x32;
+  // per slab: entries [slab_start[s], slab_start[s+1])
+  uint32_t const* slab_start;
+  uint32_t const* slab_edges;  // vertex index of the edge's end point
+  // per vertex
+  uint32_t const* prev_vertex;
+  float4 const* edge32;  // (ax, ay, bx, by) offsets from the anchor
+};
+
+template <typename T>
+class PolygonIndex {
+ public:
+  PolygonIndex(uint32_t const* poly_offsets, size_t num_poly_offsets,
+               uint32_t const* ring_offsets, size_t num_ring_offsets, T const* vx, T const* vy,
+               size_t num_vertices, bool build_float32, Allocator const& alloc);
+  PolygonIndexView<T> view() const { return v_; }
+
+ private:
+  Buffer<T> pminx_, pminy_, pmaxx_, pmaxy_, ax_, ay_, invh_, vert_x_;
+  Buffer<float> maxoff_, vert_x32_;
+  Buffer<uint32_t> nslab_, slab_base_, vbeg_, vend_, slab_start_, slab_edges_, prev_;
+  Buffer<uint8_t> exact_;
+  Buffer<float4> edge32_;
+  PolygonIndexView<T> v_{};
+};
+
+}  // namespace cspt

@@ -1,0 +1,217 @@
+"""Seeded synthetic inputs with the shapes of the benchmark configurations.
+
+No public dataset is involved; every array is drawn from numpy's PCG64 with
+seed 20261203 + config id, so the same call gives the same bytes on any
+machine.  All sizes can be scaled down (same distributions) for tests.
+
+  plain_small          1,000,000 uniform points in [0,1000)^2, 256 star
+                       polygons (8-64 vertices, per-vertex radius U[5,40]).
+  precision_at_scale   100,000,000 points from a 64-component Gaussian
+                       mixture, 1% of them on polygon vertices or within 1e-9
+                       of an edge; 100,000 star polygons (8-512 vertices,
+                       radius U[2,60] per polygon with per-vertex factor
+                       U[0.5,1]), 10% with a reversed hole at 0.4 scale.
+  nearest_linestring   50,000,000 uniform points in [0,10000)^2, 200,000
+                       random-walk linestrings (2-256 segments, step U[1,20],
+                       heading change N(0, 0.3 rad)).
+"""
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+SEED = 20261203
+
+
+@dataclass
+class Polygons:
+    x: np.ndarray
+    y: np.ndarray
+    ring_offset: np.ndarray    # ring -> first vertex
+    part_offset: np.ndarray    # polygon -> first ring
+    geometry_offset: np.ndarray  # multipolygon -> first polygon (identity)
+
+    @property
+    def num_polygons(self):
+        return len(self.part_offset) - 1
+
+
+@dataclass
+class Linestrings:
+    x: np.ndarray
+    y: np.ndarray
+    part_offset: np.ndarray
+    geometry_offset: np.ndarray
+
+
+@dataclass
+class Workload:
+    name: str
+    x: np.ndarray
+    y: np.ndarray
+    x_min: float
+    x_max: float
+    y_min: float
+    y_max: float
+    scale: float
+    max_depth: int
+    max_size: int
+    polygons: Polygons = None
+    linestrings: Linestrings = None
+    expansion_radius: float = 0.0
+    extra: dict = field(default_factory=dict)
+
+
+def star_polygons(rng, centers, nverts, radius_fn, hole_fraction=0.0, hole_scale=0.4):
+    """Star-shaped single-ring polygons (optionally with one reversed hole).
+
+    Vertex angles are the sorted order statistics of nverts uniforms on
+    [0, 2pi) plus a random rotation; rings are closed by repeating vertex 0.
+    radius_fn(rng, polygon_ids) returns one radius per vertex.
+    """
+    p = len(centers)
+    nverts = np.asarray(nverts, dtype=np.int64)
+    pid = np.repeat(np.arange(p), nverts)
+    # sorted uniforms via normalised cumulative exponential spacings
+    e = rng.exponential(size=len(pid) + p)
+    starts = np.concatenate([[0], np.cumsum(nverts + 1)])
+    cs = np.cumsum(e)
+    base = np.concatenate([[0.0], cs[starts[1:-1] - 1]])
+    tot = cs[starts[1:] - 1] - base
+    local = np.arange(len(pid)) - np.repeat(np.cumsum(nverts) - nverts, nverts)
+    idx = np.repeat(starts[:-1], nverts) + local
+    ang = (cs[idx] - np.repeat(base, nverts)) / np.repeat(tot, nverts) * 2 * math.pi
+    ang += np.repeat(rng.uniform(0, 2 * math.pi, p), nverts)
+    r = radius_fn(rng, pid)
+    vx = np.repeat(centers[:, 0], nverts) + r * np.cos(ang)
+    vy = np.repeat(centers[:, 1], nverts) + r * np.sin(ang)
+    has_hole = rng.random(p) < hole_fraction
+    # assemble rings: outer (closed), optional hole (reversed, closed)
+    xs, ys, ring_len, rings_per_poly = [], [], [], np.where(has_hole, 2, 1)
+    vstart = np.concatenate([[0], np.cumsum(nverts)])
+    ring_sizes = []
+    out_x = []
+    out_y = []
+    for i in range(p):
+        a, b = vstart[i], vstart[i + 1]
+        ox = np.append(vx[a:b], vx[a])
+        oy = np.append(vy[a:b], vy[a])
+        out_x.append(ox)
+        out_y.append(oy)
+        ring_sizes.append(len(ox))
+        if has_hole[i]:
+            cx, cy = centers[i]
+            hx = (cx + hole_scale * (ox - cx))[::-1]
+            hy = (cy + hole_scale * (oy - cy))[::-1]
+            out_x.append(hx)
+            out_y.append(hy)
+            ring_sizes.append(len(hx))
+    del xs, ys, ring_len
+    x = np.concatenate(out_x)
+    y = np.concatenate(out_y)
+    ring_offset = np.concatenate([[0], np.cumsum(ring_sizes)]).astype(np.int32)
+    part_offset = np.concatenate([[0], np.cumsum(rings_per_poly)]).astype(np.int32)
+    geometry_offset = np.arange(p + 1, dtype=np.int32)
+    return Polygons(x, y, ring_offset, part_offset, geometry_offset)
+
+
+def plain_small(n_points=1_000_000, n_polygons=256, seed_offset=0):
+    rng = np.random.Generator(np.random.PCG64(SEED + 0 + seed_offset))
+    x = rng.uniform(0, 1000, n_points)
+    y = rng.uniform(0, 1000, n_points)
+    centers = rng.uniform(50, 950, (n_polygons, 2))
+    k = rng.integers(8, 65, n_polygons)
+    polys = star_polygons(rng, centers, k, lambda g, pid: g.uniform(5, 40, len(pid)))
+    return Workload("plain_small", x, y, 0.0, 1000.0, 0.0, 1000.0, 1000.0 / 128, 7, 128,
+                    polygons=polys)
+
+
+def _near_boundary(rng, polys, count):
+    """Points on polygon vertices (half) or within 1e-9 of an edge (half)."""
+    nring = len(polys.ring_offset) - 1
+    ring = rng.integers(0, nring, count)
+    rb = polys.ring_offset[ring].astype(np.int64)
+    rl = polys.ring_offset[ring + 1].astype(np.int64) - rb
+    j = rb + (rng.random(count) * (rl - 1)).astype(np.int64)  # edge j -> j+1 (closed ring)
+    ax, ay = polys.x[j], polys.y[j]
+    bx, by = polys.x[j + 1], polys.y[j + 1]
+    on_vertex = rng.random(count) < 0.5
+    t = rng.random(count)
+    dx, dy = bx - ax, by - ay
+    ln = np.hypot(dx, dy)
+    ln[ln == 0] = 1.0
+    off = rng.uniform(-1e-9, 1e-9, count)
+    px = ax + t * dx - dy / ln * off
+    py = ay + t * dy + dx / ln * off
+    px = np.where(on_vertex, ax, px)
+    py = np.where(on_vertex, ay, py)
+    return px, py
+
+
+def precision_at_scale(n_points=100_000_000, n_polygons=100_000, n_components=64,
+                       boundary_fraction=0.01, extent=10000.0, max_vertices=512,
+                       seed_offset=0):
+    rng = np.random.Generator(np.random.PCG64(SEED + 1 + seed_offset))
+    centers = rng.uniform(0, extent, (n_components, 2))
+    sigma = rng.uniform(10, 200, n_components)
+    comp = rng.integers(0, n_components, n_points)
+    x = centers[comp, 0] + sigma[comp] * rng.standard_normal(n_points)
+    y = centers[comp, 1] + sigma[comp] * rng.standard_normal(n_points)
+    del comp
+    hi = np.nextafter(extent, 0.0)
+    np.clip(x, 0.0, hi, out=x)
+    np.clip(y, 0.0, hi, out=y)
+    pc = rng.uniform(0, extent, (n_polygons, 2))
+    k = rng.integers(8, max_vertices + 1, n_polygons)
+    prad = rng.uniform(2, 60, n_polygons)
+    polys = star_polygons(rng, pc, k, lambda g, pid: prad[pid] * g.uniform(0.5, 1.0, len(pid)),
+                          hole_fraction=0.10)
+    nb = int(round(boundary_fraction * n_points))
+    if nb:
+        sel = rng.choice(n_points, nb, replace=False)
+        bx, by = _near_boundary(rng, polys, nb)
+        x[sel] = bx
+        y[sel] = by
+    # cells stay below 2^15 for points in [0, extent)
+    return Workload("precision_at_scale", x, y, 0.0, extent, 0.0, extent, extent / 32768, 15,
+                    256, polygons=polys, extra=dict(boundary_points=nb))
+
+
+def nearest_linestring(n_points=50_000_000, n_linestrings=200_000, extent=10000.0,
+                       seed_offset=0):
+    rng = np.random.Generator(np.random.PCG64(SEED + 4 + seed_offset))
+    x = rng.uniform(0, extent, n_points)
+    y = rng.uniform(0, extent, n_points)
+    nseg = rng.integers(2, 257, n_linestrings)
+    nv = nseg + 1
+    start = rng.uniform(0, extent, (n_linestrings, 2))
+    lid = np.repeat(np.arange(n_linestrings), nseg)
+    step = rng.uniform(1, 20, len(lid))
+    dtheta = rng.normal(0, 0.3, len(lid))
+    h0 = rng.uniform(0, 2 * math.pi, n_linestrings)
+    # heading = initial heading + cumulative turn within each linestring
+    cum = np.cumsum(dtheta)
+    seg_start = np.concatenate([[0], np.cumsum(nseg)[:-1]])
+    base = np.where(seg_start > 0, cum[seg_start - 1], 0.0)
+    heading = np.repeat(h0, nseg) + cum - np.repeat(base, nseg)
+    sx = np.cumsum(step * np.cos(heading))
+    sy = np.cumsum(step * np.sin(heading))
+    bx = np.where(seg_start > 0, sx[seg_start - 1], 0.0)
+    by = np.where(seg_start > 0, sy[seg_start - 1], 0.0)
+    rel_x = sx - np.repeat(bx, nseg)
+    rel_y = sy - np.repeat(by, nseg)
+    # vertices: start point, then the walk
+    voff = np.concatenate([[0], np.cumsum(nv)])
+    lx = np.empty(voff[-1])
+    ly = np.empty(voff[-1])
+    first = voff[:-1]
+    lx[first] = start[:, 0]
+    ly[first] = start[:, 1]
+    rest = np.ones(voff[-1], bool)
+    rest[first] = False
+    lx[rest] = np.repeat(start[:, 0], nseg) + rel_x
+    ly[rest] = np.repeat(start[:, 1], nseg) + rel_y
+    ls = Linestrings(lx, ly, voff.astype(np.int32), np.arange(n_linestrings + 1, dtype=np.int32))
+    return Workload("nearest_linestring", x, y, 0.0, extent, 0.0, extent, extent / 16384, 14,
+                    256, linestrings=ls, expansion_radius=25.0)

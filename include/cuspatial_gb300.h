@@ -1,0 +1,196 @@
+/*
+ * cuspatial_gb300 — C ABI of the GB300 (sm_103a) quadtree spatial join.
+ *
+ * Each entry point replaces one libcuspatial column-API function; the comment
+ * on each names the reference declaration it stands in for (paths relative to
+ * the cuSpatial 25.06 source tree).  Differences from the reference:
+ *   - columns are raw device pointers plus element counts; coordinates carry a
+ *     dtype code (float32 / float64) where cuDF columns carried a type id;
+ *   - offsets are 32-bit unsigned (cuDF INT32 offsets are accepted as-is: the
+ *     values are non-negative, so the bits are the same);
+ *   - cuspatial::logic_error / cuda_error become status codes, with the
+ *     reference's message text available from cspt_last_error_message();
+ *   - outputs whose size is only known on the device are allocated through a
+ *     caller-supplied allocator (rmm's device_async_resource_ref in the
+ *     reference); passing NULL uses cudaMallocAsync / cudaFreeAsync;
+ *   - every call takes an explicit stream (a cudaStream_t passed as void*).
+ *     Calls that return a size the host must know (quadtree node count, pair
+ *     counts) synchronise that stream once; the others are asynchronous.
+ *
+ * Thread safety: calls are reentrant; the last-error message is per thread.
+ */
+#ifndef CUSPATIAL_GB300_H
+#define CUSPATIAL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  CSPT_OK               = 0,
+  CSPT_INVALID_ARGUMENT = 1, /* cuspatial::logic_error */
+  CSPT_OUT_OF_MEMORY    = 2, /* rmm::out_of_memory */
+  CSPT_CUDA_ERROR       = 3, /* cuspatial::cuda_error */
+  CSPT_TIMEOUT          = 4, /* a bounded device-side wait gave up */
+  CSPT_UNSUPPORTED      = 5  /* non-floating-point coordinates (CUDF_FAIL) */
+} cspt_status;
+
+typedef enum { CSPT_FLOAT32 = 0, CSPT_FLOAT64 = 1 } cspt_dtype;
+
+/* Point-in-polygon / nearest-linestring arithmetic.
+ *   CSPT_METHOD_EXACT    : every edge test in the input precision, evaluated
+ *                          exactly as the reference does (the drop-in).
+ *   CSPT_METHOD_FILTERED : float64 inputs are first tested in float32 with a
+ *                          forward error bound; only undecided candidates are
+ *                          re-evaluated with the float64 reference expression.
+ *                          Results are identical to CSPT_METHOD_EXACT.
+ */
+typedef enum { CSPT_METHOD_EXACT = 0, CSPT_METHOD_FILTERED = 1 } cspt_method;
+
+/* Device allocator.  allocate must return 256-byte aligned device memory or
+ * NULL; deallocate receives the same size and stream. */
+typedef struct {
+  void* ctx;
+  void* (*allocate)(void* ctx, size_t bytes, void* stream);
+  void (*deallocate)(void* ctx, void* ptr, size_t bytes, void* stream);
+} cspt_allocator;
+
+/* Quadtree columns (cpp/include/cuspatial/point_quadtree.hpp:40-58):
+ * key u32, level u8, is_internal_node u8 (0/1), length u32, offset u32. */
+typedef struct {
+  uint32_t* key;
+  uint8_t* level;
+  uint8_t* is_internal_node;
+  uint32_t* length;
+  uint32_t* offset;
+  size_t num_nodes;
+} cspt_quadtree;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* cspt_last_error_message(void);
+
+/* Library version string. */
+const char* cspt_version(void);
+
+/* Number of candidates that the last CSPT_METHOD_FILTERED point-in-polygon
+ * call on this thread re-evaluated in float64.  Diagnostic with no
+ * counterpart in the reference. */
+uint64_t cspt_last_refined_count(void);
+
+/* Number of kernels this library has launched since load.  Diagnostic with
+ * no counterpart in the reference. */
+uint64_t cspt_launch_count(void);
+
+/* Event timing of the library's named kernels on their launching streams
+ * ("pip_bits", "pip_expand", "join_count", "join_write", "nearest",
+ * "quadtree_build").  Enabling (or disabling) clears the totals; reading
+ * waits for the recorded events.  Diagnostics with no counterpart in the
+ * reference. */
+void cspt_profile_enable(int on);
+int cspt_profile_read(const char* name, double* total_ms, uint64_t* launches);
+
+/* Releases a buffer returned by this library (same allocator as the call). */
+void cspt_free(const cspt_allocator* mr, void* ptr, size_t bytes, void* stream);
+
+/* Releases the five columns of a quadtree returned by cspt_quadtree_on_points. */
+void cspt_quadtree_free(const cspt_allocator* mr, cspt_quadtree* tree, void* stream);
+
+/*
+ * Replaces cuspatial::quadtree_on_points
+ * (cpp/include/cuspatial/point_quadtree.hpp:68-78; behaviour
+ * cpp/src/indexing/point_quadtree.cu:154-180 and
+ * cpp/include/cuspatial/detail/point_quadtree.cuh:237-272).
+ * Outputs point_indices[num_points] and the quadtree, both allocated with mr.
+ * max_depth is clamped to [0, 15], max_size to >= 1 and scale to
+ * >= max(dx, dy) / ((1 << max_depth) + 2), as the reference does.
+ */
+cspt_status cspt_quadtree_on_points(const void* x, const void* y, size_t num_points,
+                                    cspt_dtype dtype, double x_min, double x_max, double y_min,
+                                    double y_max, double scale, int8_t max_depth,
+                                    int32_t max_size, const cspt_allocator* mr, void* stream,
+                                    uint32_t** out_point_indices, cspt_quadtree* out_tree);
+
+/*
+ * Replaces cuspatial::polygon_bounding_boxes
+ * (cpp/include/cuspatial/bounding_boxes.hpp:79-85;
+ * cpp/src/bounding_boxes/polygon_bounding_boxes.cu:132-159).
+ * poly_offsets[num_poly_offsets] index rings, ring_offsets[num_ring_offsets]
+ * index vertices.  Writes num_poly_offsets-1 rows to the caller's four
+ * arrays (dtype of x/y).  A polygon without vertices yields no row and later
+ * rows move up, as reduce_by_key does in the reference; left-over rows are NaN.
+ */
+cspt_status cspt_polygon_bounding_boxes(const uint32_t* poly_offsets, size_t num_poly_offsets,
+                                        const uint32_t* ring_offsets, size_t num_ring_offsets,
+                                        const void* x, const void* y, size_t num_vertices,
+                                        cspt_dtype dtype, double expansion_radius,
+                                        void* out_min_x, void* out_min_y, void* out_max_x,
+                                        void* out_max_y, void* stream);
+
+/*
+ * Replaces cuspatial::linestring_bounding_boxes
+ * (cpp/include/cuspatial/bounding_boxes.hpp:52-57;
+ * cpp/src/bounding_boxes/linestring_bounding_boxes.cu).
+ */
+cspt_status cspt_linestring_bounding_boxes(const uint32_t* linestring_offsets,
+                                           size_t num_linestring_offsets, const void* x,
+                                           const void* y, size_t num_vertices, cspt_dtype dtype,
+                                           double expansion_radius, void* out_min_x,
+                                           void* out_min_y, void* out_max_x, void* out_max_y,
+                                           void* stream);
+
+/*
+ * Replaces cuspatial::join_quadtree_and_bounding_boxes
+ * (cpp/include/cuspatial/spatial_join.hpp:66-75;
+ * cpp/src/join/quadtree_bbox_filtering.cu:90-126).
+ * Output pairs (bbox_offset, quad_offset) sorted by the leaf's first point,
+ * then by bbox index — the reference's order.  Allocated with mr.
+ */
+cspt_status cspt_join_quadtree_and_bounding_boxes(
+  const cspt_quadtree* tree, const void* bbox_min_x, const void* bbox_min_y,
+  const void* bbox_max_x, const void* bbox_max_y, size_t num_bboxes, cspt_dtype dtype,
+  double x_min, double x_max, double y_min, double y_max, double scale, int8_t max_depth,
+  const cspt_allocator* mr, void* stream, uint32_t** out_bbox_offset,
+  uint32_t** out_quad_offset, size_t* out_num_pairs);
+
+/*
+ * Replaces cuspatial::quadtree_point_in_polygon
+ * (cpp/include/cuspatial/spatial_join.hpp:116-126;
+ * cpp/src/join/quadtree_point_in_polygon.cu:143-191).
+ * Output (polygon_index, point_index) in (pair order, point position) order;
+ * point_index is a position in point_indices.  Allocated with mr.
+ */
+cspt_status cspt_quadtree_point_in_polygon(
+  const uint32_t* pair_polygon, const uint32_t* pair_quad, size_t num_pairs,
+  const cspt_quadtree* tree, const uint32_t* point_indices, size_t num_point_indices,
+  const void* x, const void* y, size_t num_points, const uint32_t* poly_offsets,
+  size_t num_poly_offsets, const uint32_t* ring_offsets, size_t num_ring_offsets,
+  const void* poly_x, const void* poly_y, size_t num_poly_vertices, cspt_dtype dtype,
+  cspt_method method, const cspt_allocator* mr, void* stream, uint32_t** out_polygon_index,
+  uint32_t** out_point_index, size_t* out_num_pairs);
+
+/*
+ * Replaces cuspatial::quadtree_point_to_nearest_linestring
+ * (cpp/include/cuspatial/spatial_join.hpp:166-175;
+ * cpp/src/join/quadtree_point_to_nearest_linestring.cu:142-187).
+ * Writes num_point_indices rows into the caller's arrays and sets *out_num_rows
+ * to num_point_indices (0 for the reference's empty-input cases).  Rows of
+ * points that have no candidate get (position, 0xFFFFFFFF, 0).  Scratch
+ * memory comes from mr.
+ */
+cspt_status cspt_quadtree_point_to_nearest_linestring(
+  const uint32_t* pair_linestring, const uint32_t* pair_quad, size_t num_pairs,
+  const cspt_quadtree* tree, const uint32_t* point_indices, size_t num_point_indices,
+  const void* x, const void* y, size_t num_points, const uint32_t* linestring_offsets,
+  size_t num_linestring_offsets, const void* ls_x, const void* ls_y, size_t num_ls_vertices,
+  cspt_dtype dtype, cspt_method method, const cspt_allocator* mr, void* stream,
+  uint32_t* out_point_index, uint32_t* out_linestring_index, void* out_distance,
+  size_t* out_num_rows);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUSPATIAL_GB300_H */
