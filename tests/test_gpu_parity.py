@@ -239,6 +239,7 @@ def test_axis_aligned_adversarial(method):
 @pytest.mark.parametrize("method", METHODS)
 def test_nearest_linestring_shape_vs_oracle(dtype, method):
     w = D.nearest_linestring(n_points=60_000, n_linestrings=300, extent=1000.0)
+    w.scale = (w.x_max - w.x_min) / 256  # depth 8: no clamping anywhere
     pts = gpu_points(w, dtype)
     pi, t = cs.quadtree_on_points(pts, w.x_min, w.x_max, w.y_min, w.y_max, w.scale, 8, 64)
     lines = gpu_linestrings(w.linestrings, dtype)
