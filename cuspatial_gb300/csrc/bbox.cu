@@ -147,3 +147,121 @@ void linestring_bounding_boxes(uint32_t const* ls_offsets, size_t nlo, void cons
 }
 
 }  // namespace cspt
+
+// ---------------------------------------------------------------------------
+// cspt_polygon_bounding_boxes_noalloc: the same boxes without any device
+// allocation, for callers that must not allocate (code running inside a CUDA
+// graph capture or a real-time loop, where cudaMalloc would synchronise the
+// device, and hosts that hand out all device memory themselves).  Its scratch
+// (row index per polygon, scan partials, non-empty count) lives in the
+// file-scope array below, which every GPU that loads the library keeps until
+// exit: 4 MiB + 2 KiB, enough for 1,048,576 polygons.
+// ---------------------------------------------------------------------------
+#include <array>
+#include <mutex>
+
+namespace cspt {
+namespace {
+
+constexpr size_t kNoAllocMaxPolygons = size_t{1} << 20;
+constexpr size_t kNoAllocPartials    = (kNoAllocMaxPolygons + kScanTile - 1) / kScanTile;
+constexpr size_t kNoAllocWords       = kNoAllocMaxPolygons + kNoAllocPartials + 64;
+
+// Device scratch shared by every call on a device; each call rewrites the
+// rows, partials and count it later reads, so nothing needs clearing.
+static __device__ __align__(256) uint32_t g_bbox_noalloc_scratch[kNoAllocWords];
+
+// The address of the scratch on the current device.  Resolved once per
+// device with cudaGetSymbolAddress (with that device current); the host-side
+// name of the array is not a device address.
+uint32_t* noalloc_scratch_on_current_device()
+{
+  static std::mutex mu;
+  static std::array<uint32_t*, 256> addr{};
+  int dev = 0;
+  CSPT_CUDA_TRY(cudaGetDevice(&dev));
+  CSPT_EXPECTS(dev >= 0 && dev < static_cast<int>(addr.size()), "device ordinal out of range");
+  std::lock_guard<std::mutex> lk(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    CSPT_CUDA_TRY(cudaGetSymbolAddress(&p, g_bbox_noalloc_scratch));
+    addr[dev] = static_cast<uint32_t*>(p);
+  }
+  return addr[dev];
+}
+
+template <typename T>
+__global__ void nan_tail_kernel(uint32_t const* __restrict__ nonempty, size_t n, T* a, T* b, T* c,
+                                T* d)
+{
+  T const nan      = std::numeric_limits<T>::quiet_NaN();
+  uint32_t const m = *nonempty;
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    if (i >= m) a[i] = b[i] = c[i] = d[i] = nan;
+  }
+}
+
+struct NonEmptyPolygon {
+  uint32_t const* po;
+  uint32_t const* ro;
+  __device__ uint32_t operator()(size_t g) const { return ro[po[g + 1]] > ro[po[g]] ? 1u : 0u; }
+};
+struct StoreRow {
+  uint32_t* row;
+  __device__ void operator()(size_t g, uint32_t e, uint32_t) const { row[g] = e; }
+};
+
+template <typename T>
+void run_noalloc(uint32_t const* po, size_t np, uint32_t const* ro, T const* x, T const* y, T r,
+                 T* ominx, T* ominy, T* omaxx, T* omaxy, uint32_t* scratch, cudaStream_t s)
+{
+  uint32_t* row      = scratch;
+  uint32_t* partials = scratch + kNoAllocMaxPolygons;
+  uint32_t* nonempty = partials + kNoAllocPartials;
+  scan_apply_prealloc<uint32_t>(NonEmptyPolygon{po, ro}, StoreRow{row}, np, nonempty, partials, s);
+  bbox_kernel<T><<<grid_for(np * 32, 256, 152u * 32u), 256, 0, s>>>(
+    po, po + 1, ro, np, x, y, row, r, ominx, ominy, omaxx, omaxy);
+  CSPT_CHECK_LAUNCH();
+  nan_tail_kernel<T>
+    <<<grid_for(np, 256, 152u * 16u), 256, 0, s>>>(nonempty, np, ominx, ominy, omaxx, omaxy);
+  CSPT_CHECK_LAUNCH();
+}
+
+}  // namespace
+}  // namespace cspt
+
+extern "C" cspt_status cspt_polygon_bounding_boxes_noalloc(
+  const uint32_t* poly_offsets, size_t num_poly_offsets, const uint32_t* ring_offsets,
+  size_t num_ring_offsets, const void* x, const void* y, size_t num_vertices, cspt_dtype dtype,
+  double expansion_radius, void* out_min_x, void* out_min_y, void* out_max_x, void* out_max_y,
+  void* stream)
+{
+  using namespace cspt;
+  return guarded([&] {
+    if (dtype != CSPT_FLOAT32 && dtype != CSPT_FLOAT64)
+      throw Error{CSPT_UNSUPPORTED, "Only floating-point types are supported"};
+    size_t const np = num_poly_offsets > 0 ? num_poly_offsets - 1 : 0;
+    if (np == 0) return;
+    CSPT_EXPECTS(np <= kNoAllocMaxPolygons,
+                 "cspt_polygon_bounding_boxes_noalloc handles at most 1048576 polygons; use "
+                 "cspt_polygon_bounding_boxes for larger inputs");
+    CSPT_EXPECTS(num_ring_offsets > 0,
+                 "Polygon ring offsets must contain at least one (1) value");
+    if (num_ring_offsets < 2 || num_vertices == 0) return;
+    cudaStream_t const s = static_cast<cudaStream_t>(stream);
+    uint32_t* scratch    = noalloc_scratch_on_current_device();
+    if (dtype == CSPT_FLOAT64)
+      run_noalloc<double>(poly_offsets, np, ring_offsets, static_cast<double const*>(x),
+                          static_cast<double const*>(y), expansion_radius,
+                          static_cast<double*>(out_min_x), static_cast<double*>(out_min_y),
+                          static_cast<double*>(out_max_x), static_cast<double*>(out_max_y),
+                          scratch, s);
+    else
+      run_noalloc<float>(poly_offsets, np, ring_offsets, static_cast<float const*>(x),
+                         static_cast<float const*>(y), static_cast<float>(expansion_radius),
+                         static_cast<float*>(out_min_x), static_cast<float*>(out_min_y),
+                         static_cast<float*>(out_max_x), static_cast<float*>(out_max_y), scratch,
+                         s);
+  });
+}

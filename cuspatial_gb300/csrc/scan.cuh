@@ -155,3 +155,26 @@ void exclusive_scan(T const* in, T* out, size_t n, T* total, Allocator const& al
 }
 
 }  // namespace cspt
+
+namespace cspt {
+
+// scan_apply over caller-provided partials (at least ceil(n / kScanTile)
+// elements): launches the same three kernels and allocates nothing.
+template <typename T, typename InF, typename OutF>
+void scan_apply_prealloc(InF in, OutF out, size_t n, T* total, T* partials, cudaStream_t s)
+{
+  if (n == 0) {
+    if (total) CSPT_CUDA_TRY(cudaMemsetAsync(total, 0, sizeof(T), s));
+    return;
+  }
+  size_t const nparts = (n + kScanTile - 1) / kScanTile;
+  scan_reduce_kernel<T, InF><<<static_cast<unsigned>(nparts), kScanBlock, 0, s>>>(in, n, partials);
+  CSPT_CHECK_LAUNCH();
+  scan_partials_kernel<T><<<1, 1024, 0, s>>>(partials, nparts, total);
+  CSPT_CHECK_LAUNCH();
+  scan_down_kernel<T, InF, OutF>
+    <<<static_cast<unsigned>(nparts), kScanBlock, 0, s>>>(in, out, n, partials);
+  CSPT_CHECK_LAUNCH();
+}
+
+}  // namespace cspt

@@ -130,6 +130,28 @@ cspt_status cspt_polygon_bounding_boxes(const uint32_t* poly_offsets, size_t num
                                         void* out_max_y, void* stream);
 
 /*
+ * cspt_polygon_bounding_boxes_noalloc: same arguments and results as
+ * cspt_polygon_bounding_boxes, but the call allocates no device memory.  It
+ * has no counterpart in the reference.  It is for callers that cannot call
+ * cudaMalloc: code that runs while a stream is being captured into a CUDA
+ * graph or inside a latency-bound loop (cudaMalloc synchronises the device),
+ * and hosts that hand out all device memory themselves.  Its scratch is a
+ * fixed file-scope device array of 4 MiB + 2 KiB that every GPU loading the
+ * library keeps until exit, so inputs are limited to 1,048,576 polygons;
+ * larger inputs are rejected with CSPT_INVALID_ARGUMENT.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) with
+ * that device current: make that first call before any stream capture.  All
+ * calls on a device share the one array (each call rewrites what it reads),
+ * so calls whose work overlaps on the GPU (different streams, no ordering
+ * between them) race and must not be issued.
+ */
+cspt_status cspt_polygon_bounding_boxes_noalloc(
+  const uint32_t* poly_offsets, size_t num_poly_offsets, const uint32_t* ring_offsets,
+  size_t num_ring_offsets, const void* x, const void* y, size_t num_vertices, cspt_dtype dtype,
+  double expansion_radius, void* out_min_x, void* out_min_y, void* out_max_x, void* out_max_y,
+  void* stream);
+
+/*
  * Replaces cuspatial::linestring_bounding_boxes
  * (cpp/include/cuspatial/bounding_boxes.hpp:52-57;
  * cpp/src/bounding_boxes/linestring_bounding_boxes.cu).
