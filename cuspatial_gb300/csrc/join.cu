@@ -81,43 +81,135 @@ __device__ inline bool walk(TreeView const& t, uint32_t L0, T bminx, T bminy, T 
   return true;
 }
 
-template <typename T>
-__global__ void join_count_kernel(TreeView t, uint32_t const* __restrict__ L0p,
-                                  T const* __restrict__ bminx, T const* __restrict__ bminy,
-                                  T const* __restrict__ bmaxx, T const* __restrict__ bmaxy,
-                                  size_t nb, T vminx, T vminy, T scale, int max_depth,
-                                  uint32_t* __restrict__ counts, int* __restrict__ error)
-{
-  uint32_t const L0 = *L0p;
-  for (size_t b = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; b < nb;
-       b += static_cast<size_t>(gridDim.x) * blockDim.x) {
-    uint32_t c   = 0;
-    bool const ok = walk<T>(t, L0, bminx[b], bminy[b], bmaxx[b], bmaxy[b], vminx, vminy, scale,
-                            max_depth, [&](uint32_t) { ++c; });
-    if (!ok) atomicExch(error, 1);
-    counts[b] = c;
-  }
-}
+constexpr int kJoinWarps = 4;       // warps per block
+constexpr int kWarpStack = 2048;    // stack entries per warp (shared memory)
 
-template <typename T>
-__global__ void join_write_kernel(TreeView t, uint32_t const* __restrict__ L0p,
-                                  T const* __restrict__ bminx, T const* __restrict__ bminy,
-                                  T const* __restrict__ bmaxx, T const* __restrict__ bmaxy,
-                                  size_t nb, T vminx, T vminy, T scale, int max_depth,
-                                  uint32_t const* __restrict__ pos, uint32_t* __restrict__ okey,
-                                  uint32_t* __restrict__ onode, uint32_t* __restrict__ obox)
+// One warp per box.  Each round pops up to 32 entries (node << 4 | depth)
+// from the warp's shared stack, one per lane, classifies them, counts or
+// writes the leaves with a ballot, and pushes the children of internal nodes
+// (warp scan of the child counts).  If the stack would overflow the warp
+// restarts the box on lane 0 with the private-stack walk above.  Seeds (the
+// level-0 nodes) are fed 32 at a time whenever the stack runs empty.
+template <typename T, bool Write>
+__global__ void __launch_bounds__(kJoinWarps * 32)
+  join_warp_kernel(TreeView t, uint32_t const* __restrict__ L0p, T const* __restrict__ bminx,
+                   T const* __restrict__ bminy, T const* __restrict__ bmaxx,
+                   T const* __restrict__ bmaxy, size_t nb, T vminx, T vminy, T scale,
+                   int max_depth, uint32_t* __restrict__ counts, uint32_t* __restrict__ maxkey,
+                   uint32_t const* __restrict__ pos, uint32_t* __restrict__ okey,
+                   uint32_t* __restrict__ onode, uint32_t* __restrict__ obox,
+                   int* __restrict__ error)
 {
-  uint32_t const L0 = *L0p;
-  for (size_t b = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; b < nb;
-       b += static_cast<size_t>(gridDim.x) * blockDim.x) {
-    uint32_t p = pos[b];
-    walk<T>(t, L0, bminx[b], bminy[b], bmaxx[b], bmaxy[b], vminx, vminy, scale, max_depth,
-            [&](uint32_t node) {
-              okey[p]  = t.offset[node];
-              onode[p] = node;
-              obox[p]  = static_cast<uint32_t>(b);
-              ++p;
-            });
+  __shared__ uint32_t stack_s[kJoinWarps][kWarpStack];
+  uint32_t* stack      = stack_s[threadIdx.x >> 5];
+  int const lane       = threadIdx.x & 31;
+  unsigned const lt    = (1u << lane) - 1u;
+  uint32_t const L0    = *L0p;
+  size_t const nwarps  = (static_cast<size_t>(gridDim.x) * blockDim.x) >> 5;
+  uint32_t local_max   = 0;
+  for (size_t b = (blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5; b < nb;
+       b += nwarps) {
+    T const x0 = bminx[b], y0 = bminy[b], x1 = bmaxx[b], y1 = bmaxy[b];
+    uint32_t found = 0;
+    uint32_t p     = Write ? pos[b] : 0u;
+    int sp         = 0;
+    uint32_t seed  = 0;
+    bool overflow  = false;
+    bool bad       = false;
+    while (sp > 0 || seed < L0) {
+      uint32_t e     = 0;
+      bool have      = false;
+      int const take = sp > 0 ? (sp < 32 ? sp : 32) : 0;
+      if (take > 0) {
+        if (lane < take) {
+          e    = stack[sp - 1 - lane];
+          have = true;
+        }
+        sp -= take;
+      } else {
+        uint32_t const s = seed + lane;
+        if (s < L0) {
+          e    = s << 4;
+          have = true;
+        }
+        seed += 32;
+      }
+      __syncwarp();
+      uint32_t const node = e >> 4;
+      int const depth     = e & 15;
+      int c               = 2;
+      if (have) {
+        if (node >= t.nq) {
+          bad = true;
+        } else {
+          c = classify<T>(t, node, x0, y0, x1, y1, vminx, vminy, scale, max_depth);
+        }
+      }
+      unsigned const leaves = __ballot_sync(0xFFFFFFFFu, c == 0);
+      if (c == 0) {
+        uint32_t const key = t.offset[node];
+        if (Write) {
+          uint32_t const d = p + __popc(leaves & lt);
+          okey[d]          = key;
+          onode[d]         = node;
+          obox[d]          = static_cast<uint32_t>(b);
+        } else {
+          local_max = key > local_max ? key : local_max;
+        }
+      }
+      p += __popc(leaves);
+      found += __popc(leaves);
+      uint32_t nchild = 0, first = 0;
+      if (c == 1 && depth + 1 < max_depth) {
+        first  = t.offset[node];
+        nchild = t.length[node];
+      }
+      uint32_t const incl  = warp_inclusive_scan(nchild);
+      uint32_t const total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+      if (sp + static_cast<int>(total) > kWarpStack) {
+        overflow = true;
+        break;
+      }
+      uint32_t const at = sp + incl - nchild;
+      for (uint32_t k = 0; k < nchild; ++k) stack[at + k] = ((first + k) << 4) | (depth + 1);
+      sp += static_cast<int>(total);
+      __syncwarp();
+    }
+    if (__any_sync(0xFFFFFFFFu, bad)) {
+      if (lane == 0) atomicExch(error, 1);
+      continue;
+    }
+    if (overflow) {
+      // rare: restart the box serially on lane 0
+      if (lane == 0) {
+        uint32_t q = Write ? pos[b] : 0u;
+        found      = 0;
+        bool const ok =
+          walk<T>(t, L0, x0, y0, x1, y1, vminx, vminy, scale, max_depth, [&](uint32_t node) {
+            uint32_t const key = t.offset[node];
+            if (Write) {
+              okey[q]  = key;
+              onode[q] = node;
+              obox[q]  = static_cast<uint32_t>(b);
+            } else {
+              local_max = key > local_max ? key : local_max;
+            }
+            ++q;
+            ++found;
+          });
+        if (!ok) atomicExch(error, 1);
+      }
+      found = __shfl_sync(0xFFFFFFFFu, found, 0);
+    }
+    if (!Write && lane == 0) counts[b] = found;
+  }
+  if (!Write) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      uint32_t const o = __shfl_xor_sync(0xFFFFFFFFu, local_max, off);
+      local_max        = o > local_max ? o : local_max;
+    }
+    if (lane == 0 && local_max) atomicMax(maxkey, local_max);
   }
 }
 
@@ -149,34 +241,43 @@ void run(cspt_quadtree const* tree, T const* bminx, T const* bminy, T const* bma
                        [] __device__(size_t, uint32_t, uint32_t) {}, tree->num_nodes, L0.data(),
                        alloc);
   Buffer<uint32_t> counts(alloc, nb + 1);
-  Buffer<int> err(alloc, 1);
-  CSPT_CUDA_TRY(cudaMemsetAsync(err.data(), 0, sizeof(int), s));
-  unsigned const blk = 128;
-  unsigned const grd = grid_for(nb, blk, 152u * 64u);
+  Buffer<uint32_t> status(alloc, 2);  // [0] max leaf offset, [1] error flag
+  CSPT_CUDA_TRY(cudaMemsetAsync(status.data(), 0, 2 * sizeof(uint32_t), s));
+  int* err           = reinterpret_cast<int*>(status.data() + 1);
+  unsigned const blk = kJoinWarps * 32;
+  unsigned const grd = grid_for(nb * 32, blk, 152u * 16u);
   {
     KernelTimer timer("join_count", s);
-    join_count_kernel<T><<<grd, blk, 0, s>>>(tv, L0.data(), bminx, bminy, bmaxx, bmaxy, nb,
-                                             vminx, vminy, scale, max_depth, counts.data(),
-                                             err.data());
+    join_warp_kernel<T, false><<<grd, blk, 0, s>>>(
+      tv, L0.data(), bminx, bminy, bmaxx, bmaxy, nb, vminx, vminy, scale, max_depth,
+      counts.data(), status.data(), nullptr, nullptr, nullptr, nullptr, err);
     CSPT_CHECK_LAUNCH();
   }
   exclusive_scan<uint32_t>(counts.data(), counts.data(), nb, counts.data() + nb, alloc);
-  size_t const k = read_back(counts.data() + nb, s);
-  CSPT_EXPECTS(read_back(err.data(), s) == 0,
-               "quadtree is malformed: a node has more children than a quadtree allows");
+  uint32_t host[3];
+  CSPT_CUDA_TRY(cudaMemcpyAsync(host, counts.data() + nb, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                s));
+  CSPT_CUDA_TRY(
+    cudaMemcpyAsync(host + 1, status.data(), 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  CSPT_CUDA_TRY(cudaStreamSynchronize(s));
+  size_t const k = host[0];
+  CSPT_EXPECTS(host[2] == 0,
+               "quadtree is malformed: a node index or child count is out of range");
   *out_n = k;
   if (k == 0) return;
+  int key_bits = 1;
+  while (key_bits < 32 && (host[1] >> key_bits) != 0) ++key_bits;
   Buffer<uint32_t> key(alloc, k), key_alt(alloc, k), node(alloc, k), box(alloc, k),
     perm(alloc, k), perm_alt(alloc, k);
   {
     KernelTimer timer("join_write", s);
-    join_write_kernel<T><<<grd, blk, 0, s>>>(tv, L0.data(), bminx, bminy, bmaxx, bmaxy, nb,
-                                             vminx, vminy, scale, max_depth, counts.data(),
-                                             key.data(), node.data(), box.data());
+    join_warp_kernel<T, true><<<grd, blk, 0, s>>>(
+      tv, L0.data(), bminx, bminy, bmaxx, bmaxy, nb, vminx, vminy, scale, max_depth, nullptr,
+      nullptr, counts.data(), key.data(), node.data(), box.data(), err);
     CSPT_CHECK_LAUNCH();
   }
   bool const alt = radix_sort_pairs<uint32_t>(key.data(), perm.data(), key_alt.data(),
-                                              perm_alt.data(), k, 0, 32, true, alloc);
+                                              perm_alt.data(), k, 0, key_bits, true, alloc);
   Buffer<uint32_t> ob(alloc, k), on(alloc, k);
   gather_pairs_kernel<<<grid_for(k, 256, 152u * 16u), 256, 0, s>>>(
     alt ? perm_alt.data() : perm.data(), node.data(), box.data(), k, ob.data(), on.data());

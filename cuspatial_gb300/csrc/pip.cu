@@ -132,62 +132,272 @@ __device__ bool pip_exact(T px, T py, PolygonIndexView<T> const& ix, uint32_t po
 }
 
 constexpr int kUndecided = 2;
+// float32 filter, in the leaf's frame (used by pip_group_kernel below).
+//
+// Maps: a point goes through f_l(v) = fl32(fl32(v - A_l) - d) with d the
+// exact offset between the grid-rounded polygon and leaf anchors, so
+// |f_l(p) - (p - A_p)| <= 2 u32 M; edge ends were stored as
+// f_p(v) = fl32(v - A_p), |f_p(v) - (v - A_p)| <= u32 M, where M bounds the
+// offsets involved (the polygon's, the leaf's and the point's).  Hence:
+//   * the box reject compares f_l with f_l (monotone) and needs px beyond the
+//     box by more than the float64 rounding of the reference's comparison
+//     (2^-44 M): tol = 2^-21 M covers it and the mapping error;
+//   * f_l against f_p comparisons (y-flags, x-ranges, vertical x) are certain
+//     beyond tol (> 3 u32 M) and undecided within it;
+//   * |cross32 - (lhs64 - rhs64)| <= 56 u32 M^2 (point and edge roundings
+//     through the differences, products and FMA) + 2^-49 M^2 (float64
+//     rounding and the 4-ULP collinear band); the test uses
+//     2^-17 M^2 = 128 u32 M^2, plus 2^-120 for float32 underflow;
+//   * the float32 slab index is off by at most 8 u32 M invh + 2 u32 nslab
+//     slabs; edges are binned 1/64 slab wide of their range, so the filter
+//     requires M invh <= 2^14.
+// Undecided points are re-evaluated with pip_exact.  The polygon box is kept
+// in the polygon's frame (f_p), so the box reject is a cross-frame comparison
+// with tol as well.
 
-// float32 filter: returns 0/1 when every edge of the slab is decided, else
-// kUndecided.  Bound on |cross32 - (lhs64 - rhs64)|: 48 u32 M^2 for offsets of
-// magnitude <= M (input rounding of the anchored coordinates, the
-// differences, the products and the FMA), plus the float64 rounding and the
-// 4-ULP collinear band (< 2^-49 M^2); 2^-18 M^2 = 64 u32 M^2 covers all of it,
-// and 2^-120 covers float32 underflow.
-__device__ int pip_filter32(double px, double py, PolygonIndexView<double> const& ix,
-                            uint32_t poly)
+__device__ inline float warp_max(float v)
 {
-  if (!(py >= ix.pminy[poly]) || !(py < ix.pmaxy[poly])) return 0;
-  if (ix.exact_only[poly] || !isfinite(px)) return kUndecided;
-  float const qx = static_cast<float>(px - ix.anchor_x[poly]);
-  float const qy = static_cast<float>(py - ix.anchor_y[poly]);
-  if (!isfinite(qx) || !isfinite(qy)) return kUndecided;
-  uint32_t const vb = ix.vert_begin[poly], ve = ix.vert_end[poly];
-  if (vb < ve && sorted_has<float>(ix.vert_x32, vb, ve, qx)) return kUndecided;
-  float const m  = fmaxf(ix.max_offset[poly], fmaxf(fabsf(qx), fabsf(qy)));
-  float const eb = __fmaf_rn(3.814697265625e-06f * m, m, 7.52316384526264e-37f);
-  uint32_t const s  = ix.slab_base[poly] + point_slab<double>(py, ix, poly);
-  uint32_t const e0 = ix.slab_start[s], e1 = ix.slab_start[s + 1];
-  bool within       = false;
-  for (uint32_t k = e0; k < e1; ++k) {
-    float4 const e = ix.edge32[ix.slab_edges[k]];  // (ax, ay, bx, by)
-    if (e.y == qy || e.w == qy) return kUndecided;
-    bool const y1    = e.y > qy;
-    bool const y0    = e.w > qy;
-    float const rtpx = qx - e.x;
-    float const rise = e.w - e.y;
-    float const run  = e.z - e.x;
-    float const rtp  = qy - e.y;
-    float const cr   = __fmaf_rn(rtpx, rise, -(run * rtp));
-    if (fabsf(cr) <= eb) {
-      float const mn = fminf(e.x, e.z), mx = fmaxf(e.x, e.z);
-      if (!(qx < mn || qx > mx)) return kUndecided;
-      if (y1 != y0) return kUndecided;
-    } else if (y1 != y0) {
-      if ((cr < 0.0f) != y1) within = !within;
-    }
-  }
-  return within ? 1 : 0;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v = fmaxf(v, __shfl_xor_sync(0xFFFFFFFFu, v, off));
+  return v;
+}
+__device__ inline float warp_min(float v)
+{
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v = fminf(v, __shfl_xor_sync(0xFFFFFFFFu, v, off));
+  return v;
 }
 
-template <typename T, bool Filtered>
+// Leaf frames: for every group of consecutive pairs that share a quadrant,
+// one warp rounds the quadrant's first point to the anchor grid and writes
+// u = fl32(p - A_l) for each of its points (indexed by sorted position), the
+// largest |u| and the u-range.  Non-finite points are flagged per leaf.
+struct LeafFrame {
+  double ax, ay;
+  float m;                        // max |u| over finite points
+  float uxmin, uxmax, uymin, uymax;
+  uint32_t nonfinite;
+};
+
 __global__ void __launch_bounds__(256)
-  pip_bits_kernel(uint32_t const* __restrict__ pair_poly, uint32_t const* __restrict__ pair_quad,
-                  size_t npairs, uint32_t const* __restrict__ qlen,
-                  uint32_t const* __restrict__ qoff, uint32_t const* __restrict__ point_indices,
-                  size_t npi, T const* __restrict__ x, T const* __restrict__ y,
-                  PolygonIndexView<T> ix, uint64_t const* __restrict__ word_off,
+  leaf_frame_kernel(uint32_t const* __restrict__ group_start, uint32_t const* __restrict__ ngroups_p,
+                    uint32_t const* __restrict__ pair_quad, uint32_t const* __restrict__ qlen,
+                    uint32_t const* __restrict__ qoff, uint32_t const* __restrict__ point_indices,
+                    size_t npi, double const* __restrict__ x, double const* __restrict__ y,
+                    double const* __restrict__ gridp, float2* __restrict__ u,
+                    LeafFrame* __restrict__ frames)
+{
+  int const lane      = threadIdx.x & 31;
+  size_t const nwarps = (static_cast<size_t>(gridDim.x) * blockDim.x) >> 5;
+  uint32_t const ng   = *ngroups_p;
+  double const g      = *gridp;
+  for (size_t gi = (blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5; gi < ng;
+       gi += nwarps) {
+    uint32_t const quad = pair_quad[group_start[gi]];
+    uint32_t const len  = qlen[quad];
+    uint64_t const off  = qoff[quad];
+    double x0 = 0.0, y0 = 0.0;
+    if (len > 0 && off < npi) {
+      uint32_t const i0 = point_indices[off];
+      x0                = x[i0];
+      y0                = y[i0];
+    }
+    double ax = rint(x0 / g) * g, ay = rint(y0 / g) * g;
+    if (!isfinite(ax)) ax = 0.0;
+    if (!isfinite(ay)) ay = 0.0;
+    float m = 0.0f, xmn = INFINITY, xmx = -INFINITY, ymn = INFINITY, ymx = -INFINITY;
+    bool bad = false;
+    for (uint32_t c = lane; c < len; c += 32) {
+      uint64_t const pos = off + c;
+      if (pos >= npi) break;
+      uint32_t const pi = point_indices[pos];
+      float2 v;
+      v.x    = static_cast<float>(x[pi] - ax);
+      v.y    = static_cast<float>(y[pi] - ay);
+      u[pos] = v;
+      if (isfinite(v.x) && isfinite(v.y)) {
+        m   = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
+        xmn = fminf(xmn, v.x);
+        xmx = fmaxf(xmx, v.x);
+        ymn = fminf(ymn, v.y);
+        ymx = fmaxf(ymx, v.y);
+      } else {
+        bad = true;
+      }
+    }
+    m   = warp_max(m);
+    xmn = warp_min(xmn);
+    xmx = warp_max(xmx);
+    ymn = warp_min(ymn);
+    ymx = warp_max(ymx);
+    bad = __any_sync(0xFFFFFFFFu, bad);
+    if (lane == 0) frames[gi] = LeafFrame{ax, ay, m, xmn, xmx, ymn, ymx, bad ? 1u : 0u};
+  }
+}
+
+// One warp per (polygon, quadrant) pair, lanes over the quadrant's points.
+// Filtered: float32 test in the leaf frame (bounds above), undecided points
+// re-evaluated with pip_exact.  Exact: pip_exact on float64 coordinates.
+template <bool Filtered>
+__global__ void __launch_bounds__(256)
+  pip_pair_kernel(uint32_t const* __restrict__ pair_poly, uint32_t const* __restrict__ pair_quad,
+                  uint32_t const* __restrict__ pair_group, size_t npairs,
+                  uint32_t const* __restrict__ qlen, uint32_t const* __restrict__ qoff,
+                  uint32_t const* __restrict__ point_indices, size_t npi,
+                  double const* __restrict__ x, double const* __restrict__ y,
+                  float2 const* __restrict__ u, LeafFrame const* __restrict__ frames,
+                  PolygonIndexView<double> ix, uint64_t const* __restrict__ word_off,
                   uint32_t* __restrict__ bits, uint32_t* __restrict__ counts,
                   unsigned long long* __restrict__ refined)
 {
+  int const lane      = threadIdx.x & 31;
+  size_t const nwarps = (static_cast<size_t>(gridDim.x) * blockDim.x) >> 5;
+  double const dlim   = Filtered ? *ix.grid * 16777216.0 : 0.0;  // 2^24 grid steps
+  uint32_t nref       = 0;
+  for (size_t k = (blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5; k < npairs;
+       k += nwarps) {
+    uint32_t const poly = pair_poly[k];
+    uint32_t const quad = pair_quad[k];
+    uint32_t const len  = qlen[quad];
+    uint64_t const off  = qoff[quad];
+    uint64_t const wb   = word_off[k];
+    uint32_t const nw   = (len + 31) >> 5;
+    uint32_t cnt        = 0;
+    if (poly >= ix.num_polygons) {
+      for (uint32_t w = lane; w < nw; w += 32) bits[wb + w] = 0u;
+      if (lane == 0) counts[k] = 0;
+      continue;
+    }
+    if constexpr (Filtered) {
+      LeafFrame const lf = frames[pair_group[k]];
+      double const ddx   = ix.anchor_x[poly] - lf.ax;
+      double const ddy   = ix.anchor_y[poly] - lf.ay;
+      bool const exact   = ix.exact_only[poly] || lf.nonfinite || !(fabs(ddx) < dlim) ||
+                         !(fabs(ddy) < dlim);
+      float const dx = static_cast<float>(ddx), dy = static_cast<float>(ddy);
+      float4 const bx = ix.box32[poly];  // polygon box in its own frame
+      float const mp  = ix.max_offset[poly];
+      // whole quadrant outside the polygon's box (beyond the tolerance)
+      if (!exact) {
+        float const qxmin = lf.uxmin - dx, qxmax = lf.uxmax - dx;
+        float const qymin = lf.uymin - dy, qymax = lf.uymax - dy;
+        float const mall  = fmaxf(fmaxf(mp, lf.m), fmaxf(fmaxf(fabsf(qxmin), fabsf(qxmax)),
+                                                        fmaxf(fabsf(qymin), fabsf(qymax))));
+        float const tol   = 4.76837158203125e-07f * mall;
+        if (qxmax < bx.x - tol || qxmin > bx.z + tol || qymax < bx.y - tol ||
+            qymin > bx.w + tol) {
+          for (uint32_t w = lane; w < nw; w += 32) bits[wb + w] = 0u;
+          if (lane == 0) counts[k] = 0;
+          continue;
+        }
+      }
+      float const invh     = static_cast<float>(ix.inv_slab_h[poly]);
+      uint32_t const ns    = ix.num_slabs[poly];
+      uint32_t const slab0 = ix.slab_base[poly];
+      uint32_t const vb = ix.vert_begin[poly], ve = ix.vert_end[poly];
+      for (uint32_t c = 0; c < len; c += 32) {
+        uint64_t const pos = off + c + lane;
+        bool hit           = false;
+        if (c + lane < len && pos < npi) {
+          int r = kUndecided;
+          if (!exact) {
+            float2 const uv = u[pos];
+            float const qx = uv.x - dx, qy = uv.y - dy;
+            float const m   = fmaxf(fmaxf(mp, lf.m), fmaxf(fabsf(qx), fabsf(qy)));
+            float const tol = 4.76837158203125e-07f * m;  // 2^-21 M
+            if (qx < bx.x - tol || qx > bx.z + tol || qy < bx.y - tol || qy > bx.w + tol) {
+              r = 0;
+            } else if (m * invh <= 16384.0f) {
+              r = 0;
+              if (vb < ve) {
+                uint32_t lo = vb, hi = ve;
+                float const key = qx - tol;
+                while (lo < hi) {
+                  uint32_t const mid = (lo + hi) >> 1;
+                  if (ix.vert_x32[mid] < key)
+                    lo = mid + 1;
+                  else
+                    hi = mid;
+                }
+                if (lo < ve && ix.vert_x32[lo] <= qx + tol) r = kUndecided;
+              }
+              if (r == 0) {
+                float const eb = __fmaf_rn(7.62939453125e-06f * m, m, 7.52316384526264e-37f);
+                float const fs = (qy - bx.y) * invh;
+                uint32_t sj    = 0;
+                if (fs > 0.0f) sj = fs >= static_cast<float>(ns) ? ns - 1 : static_cast<uint32_t>(fs);
+                if (sj >= ns) sj = ns - 1;
+                uint32_t const e0 = ix.slab_start[slab0 + sj], e1 = ix.slab_start[slab0 + sj + 1];
+                bool within       = false;
+                for (uint32_t k2 = e0; k2 < e1; ++k2) {
+                  float4 const e  = ix.edge32[ix.slab_edges[k2]];
+                  float const ya = e.y - qy, yb = e.w - qy;
+                  if (fabsf(ya) <= tol || fabsf(yb) <= tol) {
+                    r = kUndecided;
+                    break;
+                  }
+                  bool const y1  = ya > 0.0f;
+                  bool const y0  = yb > 0.0f;
+                  float const cr = __fmaf_rn(qx - e.x, e.w - e.y, -((e.z - e.x) * (qy - e.y)));
+                  if (fabsf(cr) <= eb) {
+                    if (!(qx < fminf(e.x, e.z) - tol || qx > fmaxf(e.x, e.z) + tol) ||
+                        y1 != y0) {
+                      r = kUndecided;
+                      break;
+                    }
+                  } else if (y1 != y0 && ((cr < 0.0f) != y1)) {
+                    within = !within;
+                  }
+                }
+                if (r == 0) r = within ? 1 : 0;
+              }
+            }
+          }
+          if (r == kUndecided) {
+            ++nref;
+            uint32_t const pi = point_indices[pos];
+            hit               = pip_exact<double>(x[pi], y[pi], ix, poly);
+          } else {
+            hit = r == 1;
+          }
+        }
+        unsigned const w = __ballot_sync(0xFFFFFFFFu, hit);
+        if (lane == 0) bits[wb + (c >> 5)] = w;
+        cnt += __popc(w);
+      }
+    } else {
+      for (uint32_t c = 0; c < len; c += 32) {
+        uint64_t const pos = off + c + lane;
+        bool hit           = false;
+        if (c + lane < len && pos < npi) {
+          uint32_t const pi = point_indices[pos];
+          hit               = pip_exact<double>(x[pi], y[pi], ix, poly);
+        }
+        unsigned const w = __ballot_sync(0xFFFFFFFFu, hit);
+        if (lane == 0) bits[wb + (c >> 5)] = w;
+        cnt += __popc(w);
+      }
+    }
+    if (lane == 0) counts[k] = cnt;
+  }
+  if (Filtered && refined) {
+    for (int o = 16; o > 0; o >>= 1) nref += __shfl_xor_sync(0xFFFFFFFFu, nref, o);
+    if (lane == 0 && nref) atomicAdd(refined, static_cast<unsigned long long>(nref));
+  }
+}
+
+// float inputs: the reference's test in float, one warp per pair.
+__global__ void __launch_bounds__(256)
+  pip_pair_kernel_f32(uint32_t const* __restrict__ pair_poly,
+                      uint32_t const* __restrict__ pair_quad, size_t npairs,
+                      uint32_t const* __restrict__ qlen, uint32_t const* __restrict__ qoff,
+                      uint32_t const* __restrict__ point_indices, size_t npi,
+                      float const* __restrict__ x, float const* __restrict__ y,
+                      PolygonIndexView<float> ix, uint64_t const* __restrict__ word_off,
+                      uint32_t* __restrict__ bits, uint32_t* __restrict__ counts)
+{
   int const lane     = threadIdx.x & 31;
   size_t const warps = (static_cast<size_t>(gridDim.x) * blockDim.x) >> 5;
-  uint32_t nref      = 0;
   for (size_t k = (blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5; k < npairs;
        k += warps) {
     uint32_t const poly = pair_poly[k];
@@ -201,28 +411,13 @@ __global__ void __launch_bounds__(256)
       bool hit           = false;
       if (c + lane < len && pos < npi && poly < ix.num_polygons) {
         uint32_t const pi = point_indices[pos];
-        T const px = x[pi], py = y[pi];
-        if constexpr (Filtered) {
-          int const r = pip_filter32(px, py, ix, poly);
-          if (r == kUndecided) {
-            ++nref;
-            hit = pip_exact<T>(px, py, ix, poly);
-          } else {
-            hit = r == 1;
-          }
-        } else {
-          hit = pip_exact<T>(px, py, ix, poly);
-        }
+        hit               = pip_exact<float>(x[pi], y[pi], ix, poly);
       }
       unsigned const w = __ballot_sync(0xFFFFFFFFu, hit);
       if (lane == 0) bits[wb + (c >> 5)] = w;
       cnt += __popc(w);
     }
     if (lane == 0) counts[k] = cnt;
-  }
-  if (Filtered && refined) {
-    for (int off = 16; off > 0; off >>= 1) nref += __shfl_xor_sync(0xFFFFFFFFu, nref, off);
-    if (lane == 0 && nref) atomicAdd(refined, static_cast<unsigned long long>(nref));
   }
 }
 
@@ -284,23 +479,50 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
   CSPT_CUDA_TRY(cudaMemsetAsync(refined.data(), 0, sizeof(unsigned long long), s));
   unsigned const blk = 256;
   unsigned const grd = grid_for(npairs * 32, blk, 152u * 8u * 4u);
-  {
+  if constexpr (std::is_same<T, double>::value) {
+    Buffer<uint32_t> gstart, pgroup;
+    Buffer<float2> u;
+    Buffer<LeafFrame> frames;
+    if (filtered) {
+      // groups of consecutive pairs sharing a quadrant, and each pair's group
+      gstart = Buffer<uint32_t>(alloc, npairs + 1);
+      pgroup = Buffer<uint32_t>(alloc, npairs);
+      uint32_t* gs = gstart.data();
+      uint32_t* pg = pgroup.data();
+      scan_apply<uint32_t>(
+        [pair_quad] __device__(size_t k) {
+          return (k == 0 || pair_quad[k] != pair_quad[k - 1]) ? 1u : 0u;
+        },
+        [gs, pg] __device__(size_t k, uint32_t e, uint32_t f) {
+          if (f) gs[e] = static_cast<uint32_t>(k);
+          pg[k] = e + f - 1u;
+        },
+        npairs, gs + npairs, alloc);
+      u      = Buffer<float2>(alloc, npi);
+      frames = Buffer<LeafFrame>(alloc, npairs);
+      KernelTimer timer("leaf_frames", s);
+      leaf_frame_kernel<<<grd, blk, 0, s>>>(gs, gs + npairs, pair_quad, qlen, qoff, point_indices,
+                                            npi, x, y, index.view().grid, u.data(),
+                                            frames.data());
+      CSPT_CHECK_LAUNCH();
+    }
     KernelTimer timer("pip_bits", s);
-    bool launched = false;
-    if constexpr (std::is_same<T, double>::value) {
-      if (filtered) {
-        pip_bits_kernel<double, true><<<grd, blk, 0, s>>>(
-          pair_poly, pair_quad, npairs, qlen, qoff, point_indices, npi, x, y, index.view(),
-          word_off.data(), bits.data(), counts.data(), refined.data());
-        launched = true;
-      }
-    }
-    if (!launched) {
-      pip_bits_kernel<T, false><<<grd, blk, 0, s>>>(pair_poly, pair_quad, npairs, qlen, qoff,
-                                                     point_indices, npi, x, y, index.view(),
-                                                     word_off.data(), bits.data(),
-                                                     counts.data(), nullptr);
-    }
+    if (filtered)
+      pip_pair_kernel<true><<<grd, blk, 0, s>>>(pair_poly, pair_quad, pgroup.data(), npairs, qlen,
+                                                qoff, point_indices, npi, x, y, u.data(),
+                                                frames.data(), index.view(), word_off.data(),
+                                                bits.data(), counts.data(), refined.data());
+    else
+      pip_pair_kernel<false><<<grd, blk, 0, s>>>(pair_poly, pair_quad, nullptr, npairs, qlen,
+                                                 qoff, point_indices, npi, x, y, nullptr, nullptr,
+                                                 index.view(), word_off.data(), bits.data(),
+                                                 counts.data(), nullptr);
+    CSPT_CHECK_LAUNCH();
+  } else {
+    KernelTimer timer("pip_bits", s);
+    pip_pair_kernel_f32<<<grd, blk, 0, s>>>(pair_poly, pair_quad, npairs, qlen, qoff,
+                                            point_indices, npi, x, y, index.view(),
+                                            word_off.data(), bits.data(), counts.data());
     CSPT_CHECK_LAUNCH();
   }
   Buffer<uint64_t> out_off(alloc, npairs + 1);

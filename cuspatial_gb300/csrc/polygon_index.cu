@@ -100,6 +100,33 @@ __global__ void poly_stats_kernel(uint32_t const* __restrict__ po, uint32_t cons
   }
 }
 
+// The anchor grid: 2^(e-22) where 2^e bounds every finite polygon coordinate.
+template <typename T>
+__global__ void __launch_bounds__(1024)
+  grid_kernel(T const* __restrict__ pminx, T const* __restrict__ pminy,
+              T const* __restrict__ pmaxx, T const* __restrict__ pmaxy, size_t np, T* grid)
+{
+  __shared__ T part[32];
+  T m = 0;
+  for (size_t p = threadIdx.x; p < np; p += blockDim.x) {
+    T const v[4] = {pminx[p], pminy[p], pmaxx[p], pmaxy[p]};
+    for (T a : v)
+      if (isfinite(a)) m = fmax(m, fabs(a));
+  }
+  for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xFFFFFFFFu, m, off));
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = part[threadIdx.x];
+    for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xFFFFFFFFu, m, off));
+    if (threadIdx.x == 0) {
+      int e = 0;
+      frexp(m > T{0} ? m : T{1}, &e);  // m < 2^e
+      *grid = ldexp(T{1}, e - 22);
+    }
+  }
+}
+
 // Per edge: previous vertex, float32 offsets, degenerate/vertical flags and
 // slab range.  fill == false counts entries; fill == true writes them.
 template <typename T, bool Fill>
@@ -113,7 +140,10 @@ __global__ void poly_edges_kernel(uint32_t const* __restrict__ po, uint32_t cons
                                   uint32_t* __restrict__ slab_edges, uint32_t* vert_count,
                                   uint32_t const* __restrict__ vert_begin, T* __restrict__ vert_x,
                                   float* maxoff, uint8_t* exact, uint32_t* __restrict__ prev_out,
-                                  float4* __restrict__ edge32, bool build_float32)
+                                  float4* __restrict__ edge32, bool build_float32,
+                                  T const* __restrict__ pmaxy, T* anchor_x, T* anchor_y,
+                                  T const* __restrict__ pminx, T const* __restrict__ pmaxx,
+                                  T const* __restrict__ grid, float4* __restrict__ box32)
 {
   int const lane     = threadIdx.x & 31;
   size_t const warps = (static_cast<size_t>(gridDim.x) * blockDim.x) >> 5;
@@ -123,7 +153,27 @@ __global__ void poly_edges_kernel(uint32_t const* __restrict__ po, uint32_t cons
     uint32_t const vb = ro[r0], ve = ro[r1];
     uint32_t const ns = nslab[p];
     uint32_t const sb = slab_base[p];
-    T const ymin = pminy[p], ih = invh[p], cx = ax[p], cy = ay[p];
+    T const ymin = pminy[p], ih = invh[p];
+    T cx = ax[p], cy = ay[p];
+    if (!Fill) {
+      // anchors: the box centre rounded to the grid
+      T const g = *grid;
+      if (ve > vb) {
+        cx = rint((pminx[p] + pmaxx[p]) * T{0.5} / g) * g;
+        cy = rint((ymin + pmaxy[p]) * T{0.5} / g) * g;
+        if (!isfinite(cx)) cx = T{0};
+        if (!isfinite(cy)) cy = T{0};
+      }
+      if (lane == 0) {
+        anchor_x[p] = cx;
+        anchor_y[p] = cy;
+        box32[p]    = make_float4(static_cast<float>(pminx[p] - cx), static_cast<float>(ymin - cy),
+                                  static_cast<float>(pmaxx[p] - cx),
+                                  static_cast<float>(pmaxy[p] - cy));
+      }
+    }
+    // a float32 slab lookup is within 1e-3 slab of the float64 one
+    T const slab_margin = ih > T{0} ? T{1} / (ih * T{64}) : T{0};
     float local_max = 0.0f;
     bool tiny_skip  = false;
     for (uint32_t v = vb + lane; v < ve; v += 32) {
@@ -148,7 +198,7 @@ __global__ void poly_edges_kernel(uint32_t const* __restrict__ po, uint32_t cons
       if (skip) continue;
       T const lo = ayv < byv ? ayv : byv;
       T const hi = ayv < byv ? byv : ayv;
-      T const mu = (hi - lo) * T(1.4551915228366852e-11);  // 2^-36 of the edge height
+      T const mu = (hi - lo) * T(1.4551915228366852e-11) + slab_margin;  // 2^-36 of the height
       uint32_t const j0 = slab_of<T>(lo - mu, ymin, ih, ns);
       uint32_t const j1 = slab_of<T>(hi + mu, ymin, ih, ns);
       for (uint32_t j = j0; j <= j1; ++j) {
@@ -232,6 +282,8 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
   vbeg_   = Buffer<uint32_t>(alloc, np + 1);
   vend_   = Buffer<uint32_t>(alloc, np);
   exact_  = Buffer<uint8_t>(alloc, np);
+  grid_   = Buffer<T>(alloc, 1);
+  box32_  = Buffer<float4>(alloc, np);
   prev_   = Buffer<uint32_t>(alloc, nv);
   if (build_float32) edge32_ = Buffer<float4>(alloc, nv);
 
@@ -244,6 +296,9 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
                                              vend_.data(), maxoff_.data(), exact_.data());
     CSPT_CHECK_LAUNCH();
   }
+  grid_kernel<T><<<1, 1024, 0, s>>>(pminx_.data(), pminy_.data(), pmaxx_.data(), pmaxy_.data(),
+                                    np, grid_.data());
+  CSPT_CHECK_LAUNCH();
   // slab bases
   Buffer<uint32_t> total(alloc, 1);
   exclusive_scan<uint32_t>(nslab_.data(), slab_base_.data(), np, total.data(), alloc);
@@ -254,7 +309,8 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
     poly_edges_kernel<T, false><<<grd, blk, 0, s>>>(
       po, ro, vx, vy, np, pminy_.data(), ax_.data(), ay_.data(), invh_.data(), nslab_.data(),
       slab_base_.data(), slab_count.data(), nullptr, nullptr, vend_.data(), nullptr, nullptr,
-      maxoff_.data(), exact_.data(), prev_.data(), edge32_.data(), build_float32);
+      maxoff_.data(), exact_.data(), prev_.data(), edge32_.data(), build_float32, pmaxy_.data(),
+      ax_.data(), ay_.data(), pminx_.data(), pmaxx_.data(), grid_.data(), box32_.data());
     CSPT_CHECK_LAUNCH();
   }
   slab_start_ = Buffer<uint32_t>(alloc, nslabs_total + 1);
@@ -273,7 +329,8 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
       po, ro, vx, vy, np, pminy_.data(), ax_.data(), ay_.data(), invh_.data(), nslab_.data(),
       slab_base_.data(), slab_count.data(), slab_start_.data(), slab_edges_.data(),
       vend_.data(), vbeg_.data(), vert_x_.data(), maxoff_.data(), exact_.data(), prev_.data(),
-      edge32_.data(), build_float32);
+      edge32_.data(), build_float32, pmaxy_.data(), ax_.data(), ay_.data(), pminx_.data(),
+      pmaxx_.data(), grid_.data(), box32_.data());
     CSPT_CHECK_LAUNCH();
     // vend = vbeg + count
     add_begin_kernel<<<grid_for(np, 256, 152u * 16u), 256, 0, s>>>(vbeg_.data(), vend_.data(),
@@ -296,8 +353,10 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
                            pmaxy_.data(),
                            ax_.data(),
                            ay_.data(),
+                           grid_.data(),
                            invh_.data(),
                            maxoff_.data(),
+                           box32_.data(),
                            nslab_.data(),
                            slab_base_.data(),
                            exact_.data(),

@@ -29,6 +29,12 @@
 //   5. An exactly vertical edge reports "on edge" for any py whenever
 //      px == its x (x-range check only, is_point_in_polygon.cuh:75-83); that
 //      case is caught by a lookup in the sorted vertical-x list.
+//   6. Slabs are also widened by 1/64 of a slab so that a float32 evaluation
+//      of the slab index (error below 1e-3 slab) still finds every edge.
+//
+// Anchors lie on a power-of-two grid (2^(e-22) for coordinates below 2^e), so
+// the offset between a polygon anchor and a leaf anchor on the same grid is
+// exact in float64 and, when below 2^24 grid steps, in float32.
 #pragma once
 
 #include "common.cuh"
@@ -48,10 +54,12 @@ struct PolygonIndexView {
   T const* pminy;
   T const* pmaxx;
   T const* pmaxy;
-  T const* anchor_x;
+  T const* anchor_x;          // on the grid
   T const* anchor_y;
+  T const* grid;              // device scalar: the anchor grid step
   T const* inv_slab_h;       // slabs per unit of y
   float const* max_offset;   // largest |float32 offset| over the polygon's vertices
+  float4 const* box32;       // vertex box as float32 offsets from the anchor
   uint32_t const* num_slabs;
   uint32_t const* slab_base;  // first slab of the polygon in slab_start
   uint8_t const* exact_only;  // 1: walk the reference loop, no index
@@ -76,11 +84,11 @@ class PolygonIndex {
   PolygonIndexView<T> view() const { return v_; }
 
  private:
-  Buffer<T> pminx_, pminy_, pmaxx_, pmaxy_, ax_, ay_, invh_, vert_x_;
+  Buffer<T> pminx_, pminy_, pmaxx_, pmaxy_, ax_, ay_, invh_, vert_x_, grid_;
   Buffer<float> maxoff_, vert_x32_;
   Buffer<uint32_t> nslab_, slab_base_, vbeg_, vend_, slab_start_, slab_edges_, prev_;
   Buffer<uint8_t> exact_;
-  Buffer<float4> edge32_;
+  Buffer<float4> edge32_, box32_;
   PolygonIndexView<T> v_{};
 };
 

@@ -349,3 +349,35 @@ def test_repeatable_output():
     b = _run_pipeline(w, np.float64, "filtered")[-1]
     assert torch.equal(a["polygon_index"], b["polygon_index"])
     assert torch.equal(a["point_index"], b["point_index"])
+
+
+@pytest.mark.parametrize("method", METHODS)
+def test_tiny_polygons_in_large_leaves(method):
+    # sparse points -> leaves much larger than the polygons; the float32
+    # filter must fall back to the exact test where its slab index is unsafe
+    rng = np.random.default_rng(11)
+    centers = rng.uniform(100, 9900, (200, 2))
+    tiny = [1e-3 if i % 2 else 0.5 for i in range(200)]
+    P = D.star_polygons(rng, centers, rng.integers(8, 40, 200),
+                        lambda g, pid: np.asarray(tiny)[pid] * g.uniform(0.5, 1.0, len(pid)),
+                        hole_fraction=0.2)
+    x = rng.uniform(0, 10000, 20000)
+    y = rng.uniform(0, 10000, 20000)
+    # points inside and on the tiny polygons
+    k = rng.integers(0, len(P.x), 4000)
+    x = np.concatenate([x, P.x[k], centers[:, 0]])
+    y = np.concatenate([y, P.y[k], centers[:, 1]])
+    w = D.Workload("tiny", x, y, 0.0, 10000.0, 0.0, 10000.0, 10000.0 / 4096, 12, 64, polygons=P)
+    _check_against_oracle(w, np.float64, method)
+
+
+@pytest.mark.parametrize("method", METHODS)
+def test_infinite_points(method):
+    # +-inf coordinates take the out-of-box key and go through the exact test
+    w = D.precision_at_scale(n_points=50_000, n_polygons=60, extent=300.0, max_vertices=64)
+    x, y = w.x.copy(), w.y.copy()
+    x[::997] = np.inf
+    y[5::991] = -np.inf
+    x[7::983] = -np.inf
+    w.x, w.y = x, y
+    _check_against_oracle(w, np.float64, method)
