@@ -286,7 +286,8 @@ def run_ours(args, dist):
     step_ms = [a.elapsed_time(b) for a, b in times]
     total_ms = dist.max(g0.elapsed_time(g1))
     kern = {}
-    for name in ("pip_bits", "pip_expand", "join_count", "join_write"):
+    for name in ("pip_bits", "pip_expand", "join_count", "join_write", "leaf_frames",
+                 "polygon_index"):
         ms, cnt = ctypes.c_double(), ctypes.c_uint64()
         lib.cspt_profile_read(name.encode(), ctypes.byref(ms), ctypes.byref(cnt))
         kern[name] = (ms.value, int(cnt.value))

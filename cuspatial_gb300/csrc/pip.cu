@@ -99,6 +99,25 @@ __device__ inline uint32_t point_slab(T py, PolygonIndexView<T> const& ix, uint3
   return j < ns ? j : ns - 1;
 }
 
+// One effective edge (b -> a) of the reference's ring walk
+// (is_point_in_polygon.cuh:61-90), in the input precision: 2 when the point
+// is on the edge, 1 when the edge toggles the crossing parity, 0 otherwise.
+template <typename T>
+__device__ inline int exact_edge(T px, T py, T ax, T ay, T bx, T by)
+{
+  T const run = bx - ax, rise = by - ay;
+  T const rtp = py - ay, rtpx = px - ax;
+  if (float_equal(run * rtp, rtpx * rise)) {
+    T const mn = ax < bx ? ax : bx;
+    T const mx = ax < bx ? bx : ax;
+    if (mn <= px && px <= mx) return 2;
+  }
+  bool const y1 = ay > py;
+  bool const y0 = by > py;
+  if (y1 != y0 && ((rtpx * rise < run * rtp) != y1)) return 1;
+  return 0;
+}
+
 // The reference's test restricted to the edges of the point's slab.
 template <typename T>
 __device__ bool pip_exact(T px, T py, PolygonIndexView<T> const& ix, uint32_t poly)
@@ -112,21 +131,9 @@ __device__ bool pip_exact(T px, T py, PolygonIndexView<T> const& ix, uint32_t po
   for (uint32_t k = e0; k < e1; ++k) {
     uint32_t const v  = ix.slab_edges[k];
     uint32_t const pv = ix.prev_vertex[v];
-    T const ax = ix.vx[v], ay = ix.vy[v], bx = ix.vx[pv], by = ix.vy[pv];
-    T const run = bx - ax, rise = by - ay;
-    T const rtp = py - ay, rtpx = px - ax;
-    if (float_equal(run * rtp, rtpx * rise)) {
-      T const mn = ax < bx ? ax : bx;
-      T const mx = ax < bx ? bx : ax;
-      if (mn <= px && px <= mx) return false;
-    }
-    bool const y1 = ay > py;
-    bool const y0 = by > py;
-    if (y1 != y0) {
-      T const lhs = rtpx * rise;
-      T const rhs = run * rtp;
-      if ((lhs < rhs) != y1) within = !within;
-    }
+    int const r       = exact_edge<T>(px, py, ix.vx[v], ix.vy[v], ix.vx[pv], ix.vy[pv]);
+    if (r == 2) return false;
+    if (r == 1) within = !within;
   }
   return within;
 }
@@ -174,6 +181,7 @@ __device__ inline float warp_min(float v)
 // largest |u| and the u-range.  Non-finite points are flagged per leaf.
 struct LeafFrame {
   double ax, ay;
+  long long ix, iy;               // anchor in grid steps
   float m;                        // max |u| over finite points
   float uxmin, uxmax, uymin, uymax;
   uint32_t nonfinite;
@@ -202,9 +210,10 @@ __global__ void __launch_bounds__(256)
       x0                = x[i0];
       y0                = y[i0];
     }
-    double ax = rint(x0 / g) * g, ay = rint(y0 / g) * g;
-    if (!isfinite(ax)) ax = 0.0;
-    if (!isfinite(ay)) ay = 0.0;
+    double rx = rint(x0 / g), ry = rint(y0 / g);
+    if (!(fabs(rx) < 4.0e18)) rx = 0.0;  // also NaN
+    if (!(fabs(ry) < 4.0e18)) ry = 0.0;
+    double const ax = rx * g, ay = ry * g;
     float m = 0.0f, xmn = INFINITY, xmx = -INFINITY, ymn = INFINITY, ymx = -INFINITY;
     bool bad = false;
     for (uint32_t c = lane; c < len; c += 32) {
@@ -231,7 +240,9 @@ __global__ void __launch_bounds__(256)
     ymn = warp_min(ymn);
     ymx = warp_max(ymx);
     bad = __any_sync(0xFFFFFFFFu, bad);
-    if (lane == 0) frames[gi] = LeafFrame{ax, ay, m, xmn, xmx, ymn, ymx, bad ? 1u : 0u};
+    if (lane == 0)
+      frames[gi] = LeafFrame{ax,  ay,  static_cast<long long>(rx), static_cast<long long>(ry), m,
+                             xmn, xmx, ymn, ymx, bad ? 1u : 0u};
   }
 }
 
@@ -252,7 +263,8 @@ __global__ void __launch_bounds__(256)
 {
   int const lane      = threadIdx.x & 31;
   size_t const nwarps = (static_cast<size_t>(gridDim.x) * blockDim.x) >> 5;
-  double const dlim   = Filtered ? *ix.grid * 16777216.0 : 0.0;  // 2^24 grid steps
+  float const gf      = Filtered ? static_cast<float>(*ix.grid) : 0.0f;
+  bool const gok      = gf >= 1.17549435e-38f && gf < 1.0e30f;  // normal float grid step
   uint32_t nref       = 0;
   for (size_t k = (blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5; k < npairs;
        k += nwarps) {
@@ -270,11 +282,14 @@ __global__ void __launch_bounds__(256)
     }
     if constexpr (Filtered) {
       LeafFrame const lf = frames[pair_group[k]];
-      double const ddx   = ix.anchor_x[poly] - lf.ax;
-      double const ddy   = ix.anchor_y[poly] - lf.ay;
-      bool const exact   = ix.exact_only[poly] || lf.nonfinite || !(fabs(ddx) < dlim) ||
-                         !(fabs(ddy) < dlim);
-      float const dx = static_cast<float>(ddx), dy = static_cast<float>(ddy);
+      // anchor offset in grid steps: exact in float32 below 2^24 steps
+      long long const dix = ix.anchor_ix[poly] - lf.ix;
+      long long const diy = ix.anchor_iy[poly] - lf.iy;
+      bool const exact    = ix.exact_only[poly] || lf.nonfinite || !gok ||
+                         dix <= -16777216LL || dix >= 16777216LL || diy <= -16777216LL ||
+                         diy >= 16777216LL;
+      float const dx = exact ? 0.0f : static_cast<float>(static_cast<int>(dix)) * gf;
+      float const dy = exact ? 0.0f : static_cast<float>(static_cast<int>(diy)) * gf;
       float4 const bx = ix.box32[poly];  // polygon box in its own frame
       float const mp  = ix.max_offset[poly];
       // whole quadrant outside the polygon's box (beyond the tolerance)
@@ -291,7 +306,7 @@ __global__ void __launch_bounds__(256)
           continue;
         }
       }
-      float const invh     = static_cast<float>(ix.inv_slab_h[poly]);
+      float const invh     = ix.inv_slab_h32[poly];
       uint32_t const ns    = ix.num_slabs[poly];
       uint32_t const slab0 = ix.slab_base[poly];
       uint32_t const vb = ix.vert_begin[poly], ve = ix.vert_end[poly];
@@ -299,7 +314,10 @@ __global__ void __launch_bounds__(256)
         uint64_t const pos = off + c + lane;
         bool hit           = false;
         if (c + lane < len && pos < npi) {
-          int r = kUndecided;
+          // r: 0/1 decided, kUndecided: run the whole exact test
+          int r       = kUndecided;
+          bool have64 = false;
+          double px64 = 0.0, py64 = 0.0;
           if (!exact) {
             float2 const uv = u[pos];
             float const qx = uv.x - dx, qy = uv.y - dy;
@@ -308,8 +326,9 @@ __global__ void __launch_bounds__(256)
             if (qx < bx.x - tol || qx > bx.z + tol || qy < bx.y - tol || qy > bx.w + tol) {
               r = 0;
             } else if (m * invh <= 16384.0f) {
-              r = 0;
+              r = -1;  // in progress
               if (vb < ve) {
+                // a vertical edge within tol: decide the px == x quirk exactly
                 uint32_t lo = vb, hi = ve;
                 float const key = qx - tol;
                 while (lo < hi) {
@@ -319,9 +338,15 @@ __global__ void __launch_bounds__(256)
                   else
                     hi = mid;
                 }
-                if (lo < ve && ix.vert_x32[lo] <= qx + tol) r = kUndecided;
+                if (lo < ve && ix.vert_x32[lo] <= qx + tol) {
+                  uint32_t const pi = point_indices[pos];
+                  px64              = x[pi];
+                  py64              = y[pi];
+                  have64            = true;
+                  if (sorted_has<double>(ix.vert_x, vb, ve, px64)) r = 0;
+                }
               }
-              if (r == 0) {
+              if (r == -1) {
                 float const eb = __fmaf_rn(7.62939453125e-06f * m, m, 7.52316384526264e-37f);
                 float const fs = (qy - bx.y) * invh;
                 uint32_t sj    = 0;
@@ -330,33 +355,49 @@ __global__ void __launch_bounds__(256)
                 uint32_t const e0 = ix.slab_start[slab0 + sj], e1 = ix.slab_start[slab0 + sj + 1];
                 bool within       = false;
                 for (uint32_t k2 = e0; k2 < e1; ++k2) {
-                  float4 const e  = ix.edge32[ix.slab_edges[k2]];
+                  uint32_t const v = ix.slab_edges[k2];
+                  float4 const e   = ix.edge32[v];  // (ax, ay, bx, by)
                   float const ya = e.y - qy, yb = e.w - qy;
-                  if (fabsf(ya) <= tol || fabsf(yb) <= tol) {
-                    r = kUndecided;
-                    break;
-                  }
                   bool const y1  = ya > 0.0f;
                   bool const y0  = yb > 0.0f;
                   float const cr = __fmaf_rn(qx - e.x, e.w - e.y, -((e.z - e.x) * (qy - e.y)));
-                  if (fabsf(cr) <= eb) {
-                    if (!(qx < fminf(e.x, e.z) - tol || qx > fmaxf(e.x, e.z) + tol) ||
-                        y1 != y0) {
-                      r = kUndecided;
-                      break;
-                    }
-                  } else if (y1 != y0 && ((cr < 0.0f) != y1)) {
-                    within = !within;
+                  bool const undecided =
+                    fabsf(ya) <= tol || fabsf(yb) <= tol ||
+                    (fabsf(cr) <= eb &&
+                     (y1 != y0 || !(qx < fminf(e.x, e.z) - tol || qx > fmaxf(e.x, e.z) + tol)));
+                  if (!undecided) {
+                    if (y1 != y0 && ((cr < 0.0f) != y1)) within = !within;
+                    continue;
                   }
+                  // this edge only, with the reference's float64 expression
+                  ++nref;
+                  if (!have64) {
+                    uint32_t const pi = point_indices[pos];
+                    px64              = x[pi];
+                    py64              = y[pi];
+                    have64            = true;
+                  }
+                  uint32_t const pv = ix.prev_vertex[v];
+                  int const ee =
+                    exact_edge<double>(px64, py64, ix.vx[v], ix.vy[v], ix.vx[pv], ix.vy[pv]);
+                  if (ee == 2) {
+                    r = 0;  // on an edge: outside
+                    break;
+                  }
+                  if (ee == 1) within = !within;
                 }
-                if (r == 0) r = within ? 1 : 0;
+                if (r == -1) r = within ? 1 : 0;
               }
             }
           }
           if (r == kUndecided) {
             ++nref;
-            uint32_t const pi = point_indices[pos];
-            hit               = pip_exact<double>(x[pi], y[pi], ix, poly);
+            if (!have64) {
+              uint32_t const pi = point_indices[pos];
+              px64              = x[pi];
+              py64              = y[pi];
+            }
+            hit = pip_exact<double>(px64, py64, ix, poly);
           } else {
             hit = r == 1;
           }

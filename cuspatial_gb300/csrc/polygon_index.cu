@@ -143,7 +143,9 @@ __global__ void poly_edges_kernel(uint32_t const* __restrict__ po, uint32_t cons
                                   float4* __restrict__ edge32, bool build_float32,
                                   T const* __restrict__ pmaxy, T* anchor_x, T* anchor_y,
                                   T const* __restrict__ pminx, T const* __restrict__ pmaxx,
-                                  T const* __restrict__ grid, float4* __restrict__ box32)
+                                  T const* __restrict__ grid, float4* __restrict__ box32,
+                                  long long* __restrict__ aix, long long* __restrict__ aiy,
+                                  float* __restrict__ invh32)
 {
   int const lane     = threadIdx.x & 31;
   size_t const warps = (static_cast<size_t>(gridDim.x) * blockDim.x) >> 5;
@@ -167,6 +169,9 @@ __global__ void poly_edges_kernel(uint32_t const* __restrict__ po, uint32_t cons
       if (lane == 0) {
         anchor_x[p] = cx;
         anchor_y[p] = cy;
+        aix[p]      = llrint(cx / g);
+        aiy[p]      = llrint(cy / g);
+        invh32[p]   = static_cast<float>(ih);
         box32[p]    = make_float4(static_cast<float>(pminx[p] - cx), static_cast<float>(ymin - cy),
                                   static_cast<float>(pmaxx[p] - cx),
                                   static_cast<float>(pmaxy[p] - cy));
@@ -268,6 +273,7 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
 {
   (void)nro;
   cudaStream_t const s = alloc.stream();
+  KernelTimer timer("polygon_index", s);
   size_t const np      = npo > 0 ? npo - 1 : 0;
   pminx_  = Buffer<T>(alloc, np);
   pminy_  = Buffer<T>(alloc, np);
@@ -284,6 +290,9 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
   exact_  = Buffer<uint8_t>(alloc, np);
   grid_   = Buffer<T>(alloc, 1);
   box32_  = Buffer<float4>(alloc, np);
+  aix_    = Buffer<long long>(alloc, np);
+  aiy_    = Buffer<long long>(alloc, np);
+  invh32_ = Buffer<float>(alloc, np);
   prev_   = Buffer<uint32_t>(alloc, nv);
   if (build_float32) edge32_ = Buffer<float4>(alloc, nv);
 
@@ -310,7 +319,8 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
       po, ro, vx, vy, np, pminy_.data(), ax_.data(), ay_.data(), invh_.data(), nslab_.data(),
       slab_base_.data(), slab_count.data(), nullptr, nullptr, vend_.data(), nullptr, nullptr,
       maxoff_.data(), exact_.data(), prev_.data(), edge32_.data(), build_float32, pmaxy_.data(),
-      ax_.data(), ay_.data(), pminx_.data(), pmaxx_.data(), grid_.data(), box32_.data());
+      ax_.data(), ay_.data(), pminx_.data(), pmaxx_.data(), grid_.data(), box32_.data(),
+      aix_.data(), aiy_.data(), invh32_.data());
     CSPT_CHECK_LAUNCH();
   }
   slab_start_ = Buffer<uint32_t>(alloc, nslabs_total + 1);
@@ -330,7 +340,7 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
       slab_base_.data(), slab_count.data(), slab_start_.data(), slab_edges_.data(),
       vend_.data(), vbeg_.data(), vert_x_.data(), maxoff_.data(), exact_.data(), prev_.data(),
       edge32_.data(), build_float32, pmaxy_.data(), ax_.data(), ay_.data(), pminx_.data(),
-      pmaxx_.data(), grid_.data(), box32_.data());
+      pmaxx_.data(), grid_.data(), box32_.data(), aix_.data(), aiy_.data(), invh32_.data());
     CSPT_CHECK_LAUNCH();
     // vend = vbeg + count
     add_begin_kernel<<<grid_for(np, 256, 152u * 16u), 256, 0, s>>>(vbeg_.data(), vend_.data(),
@@ -354,6 +364,9 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
                            ax_.data(),
                            ay_.data(),
                            grid_.data(),
+                           aix_.data(),
+                           aiy_.data(),
+                           invh32_.data(),
                            invh_.data(),
                            maxoff_.data(),
                            box32_.data(),

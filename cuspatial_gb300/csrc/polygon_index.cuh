@@ -57,6 +57,9 @@ struct PolygonIndexView {
   T const* anchor_x;          // on the grid
   T const* anchor_y;
   T const* grid;              // device scalar: the anchor grid step
+  long long const* anchor_ix;  // anchors in grid steps
+  long long const* anchor_iy;
+  float const* inv_slab_h32;   // inv_slab_h rounded to float
   T const* inv_slab_h;       // slabs per unit of y
   float const* max_offset;   // largest |float32 offset| over the polygon's vertices
   float4 const* box32;       // vertex box as float32 offsets from the anchor
@@ -85,7 +88,8 @@ class PolygonIndex {
 
  private:
   Buffer<T> pminx_, pminy_, pmaxx_, pmaxy_, ax_, ay_, invh_, vert_x_, grid_;
-  Buffer<float> maxoff_, vert_x32_;
+  Buffer<float> maxoff_, vert_x32_, invh32_;
+  Buffer<long long> aix_, aiy_;
   Buffer<uint32_t> nslab_, slab_base_, vbeg_, vend_, slab_start_, slab_edges_, prev_;
   Buffer<uint8_t> exact_;
   Buffer<float4> edge32_, box32_;
