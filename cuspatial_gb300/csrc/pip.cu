@@ -131,9 +131,21 @@ __device__ bool pip_exact(T px, T py, PolygonIndexView<T> const& ix, uint32_t po
   for (uint32_t k = e0; k < e1; ++k) {
     uint32_t const v  = ix.slab_edges[k];
     uint32_t const pv = ix.prev_vertex[v];
-    int const r       = exact_edge<T>(px, py, ix.vx[v], ix.vy[v], ix.vx[pv], ix.vy[pv]);
-    if (r == 2) return false;
-    if (r == 1) within = !within;
+    T const ax = ix.vx[v], ay = ix.vy[v], bx = ix.vx[pv], by = ix.vy[pv];
+    T const run = bx - ax, rise = by - ay;
+    T const rtp = py - ay, rtpx = px - ax;
+    if (float_equal(run * rtp, rtpx * rise)) {
+      T const mn = ax < bx ? ax : bx;
+      T const mx = ax < bx ? bx : ax;
+      if (mn <= px && px <= mx) return false;
+    }
+    bool const y1 = ay > py;
+    bool const y0 = by > py;
+    if (y1 != y0) {
+      T const lhs = rtpx * rise;
+      T const rhs = run * rtp;
+      if ((lhs < rhs) != y1) within = !within;
+    }
   }
   return within;
 }
@@ -216,22 +228,39 @@ __global__ void __launch_bounds__(256)
     double const ax = rx * g, ay = ry * g;
     float m = 0.0f, xmn = INFINITY, xmx = -INFINITY, ymn = INFINITY, ymx = -INFINITY;
     bool bad = false;
-    for (uint32_t c = lane; c < len; c += 32) {
-      uint64_t const pos = off + c;
-      if (pos >= npi) break;
-      uint32_t const pi = point_indices[pos];
-      float2 v;
-      v.x    = static_cast<float>(x[pi] - ax);
-      v.y    = static_cast<float>(y[pi] - ay);
-      u[pos] = v;
-      if (isfinite(v.x) && isfinite(v.y)) {
-        m   = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
-        xmn = fminf(xmn, v.x);
-        xmx = fmaxf(xmx, v.x);
-        ymn = fminf(ymn, v.y);
-        ymx = fmaxf(ymx, v.y);
-      } else {
-        bad = true;
+    // four independent gathers per lane per round
+    for (uint32_t c0 = 0; c0 < len; c0 += 128) {
+      uint32_t pi[4];
+      bool ok[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        uint32_t const c   = c0 + t * 32 + lane;
+        uint64_t const pos = off + c;
+        ok[t]              = c < len && pos < npi;
+        pi[t]              = ok[t] ? point_indices[pos] : 0u;
+      }
+      double px[4], py[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        px[t] = ok[t] ? x[pi[t]] : 0.0;
+        py[t] = ok[t] ? y[pi[t]] : 0.0;
+      }
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        if (!ok[t]) continue;
+        float2 v;
+        v.x                           = static_cast<float>(px[t] - ax);
+        v.y                           = static_cast<float>(py[t] - ay);
+        u[off + c0 + t * 32 + lane]   = v;
+        if (isfinite(v.x) && isfinite(v.y)) {
+          m   = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
+          xmn = fminf(xmn, v.x);
+          xmx = fmaxf(xmx, v.x);
+          ymn = fminf(ymn, v.y);
+          ymx = fmaxf(ymx, v.y);
+        } else {
+          bad = true;
+        }
       }
     }
     m   = warp_max(m);
@@ -355,8 +384,7 @@ __global__ void __launch_bounds__(256)
                 uint32_t const e0 = ix.slab_start[slab0 + sj], e1 = ix.slab_start[slab0 + sj + 1];
                 bool within       = false;
                 for (uint32_t k2 = e0; k2 < e1; ++k2) {
-                  uint32_t const v = ix.slab_edges[k2];
-                  float4 const e   = ix.edge32[v];  // (ax, ay, bx, by)
+                  float4 const e = ix.slab_e32[k2];  // (ax, ay, bx, by)
                   float const ya = e.y - qy, yb = e.w - qy;
                   bool const y1  = ya > 0.0f;
                   bool const y0  = yb > 0.0f;
@@ -377,6 +405,7 @@ __global__ void __launch_bounds__(256)
                     py64              = y[pi];
                     have64            = true;
                   }
+                  uint32_t const v  = ix.slab_edges[k2];
                   uint32_t const pv = ix.prev_vertex[v];
                   int const ee =
                     exact_edge<double>(px64, py64, ix.vx[v], ix.vy[v], ix.vx[pv], ix.vy[pv]);

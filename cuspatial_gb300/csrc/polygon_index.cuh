@@ -54,18 +54,18 @@ struct PolygonIndexView {
   T const* pminy;
   T const* pmaxx;
   T const* pmaxy;
-  T const* anchor_x;          // on the grid
+  T const* anchor_x;           // box centre rounded to the grid
   T const* anchor_y;
-  T const* grid;              // device scalar: the anchor grid step
+  T const* grid;               // device scalar: the anchor grid step
   long long const* anchor_ix;  // anchors in grid steps
   long long const* anchor_iy;
   float const* inv_slab_h32;   // inv_slab_h rounded to float
-  T const* inv_slab_h;       // slabs per unit of y
-  float const* max_offset;   // largest |float32 offset| over the polygon's vertices
-  float4 const* box32;       // vertex box as float32 offsets from the anchor
+  T const* inv_slab_h;         // slabs per unit of y
+  float const* max_offset;     // largest |float32 offset| over the polygon's vertices
+  float4 const* box32;         // vertex box as float32 offsets from the anchor
   uint32_t const* num_slabs;
-  uint32_t const* slab_base;  // first slab of the polygon in slab_start
-  uint8_t const* exact_only;  // 1: walk the reference loop, no index
+  uint32_t const* slab_base;   // first slab of the polygon in slab_start
+  uint8_t const* exact_only;   // 1: walk the reference loop, no index
   uint32_t const* vert_begin;  // sorted vertical-edge x values, per polygon range
   uint32_t const* vert_end;
   T const* vert_x;
@@ -73,9 +73,10 @@ struct PolygonIndexView {
   // per slab: entries [slab_start[s], slab_start[s+1])
   uint32_t const* slab_start;
   uint32_t const* slab_edges;  // vertex index of the edge's end point
+  float4 const* slab_e32;      // the entry's edge (ax, ay, bx, by) as float32 offsets
   // per vertex
   uint32_t const* prev_vertex;
-  float4 const* edge32;  // (ax, ay, bx, by) offsets from the anchor
+  float4 const* edge32;        // (ax, ay, bx, by) offsets from the anchor
 };
 
 template <typename T>
@@ -92,7 +93,7 @@ class PolygonIndex {
   Buffer<long long> aix_, aiy_;
   Buffer<uint32_t> nslab_, slab_base_, vbeg_, vend_, slab_start_, slab_edges_, prev_;
   Buffer<uint8_t> exact_;
-  Buffer<float4> edge32_, box32_;
+  Buffer<float4> edge32_, box32_, slab_e32_;
   PolygonIndexView<T> v_{};
 };
 
