@@ -381,3 +381,47 @@ def test_infinite_points(method):
     x[7::983] = -np.inf
     w.x, w.y = x, y
     _check_against_oracle(w, np.float64, method)
+
+
+@pytest.mark.parametrize("method", METHODS)
+def test_nearest_linestring_adversarial(method):
+    # points on vertices and on segments (distance exactly 0 loses to any
+    # non-zero candidate), symmetric ties (smaller id wins), zero-length
+    # segments and single-vertex linestrings
+    rng = np.random.default_rng(5)
+    lx, ly, offs = [], [], [0]
+    for i in range(40):
+        y0 = 2.0 * i
+        xs = [0.0, 3.0, 3.0, 6.0, 9.0]          # repeated vertex: zero-length segment
+        ys = [y0, y0, y0, y0 + 1.0, y0]
+        if i % 7 == 3:
+            xs, ys = [4.0], [y0]               # a single vertex: no segment
+        lx += xs
+        ly += ys
+        offs.append(len(lx))
+    lx, ly = np.array(lx), np.array(ly)
+    px = list(rng.uniform(-2, 11, 4000))
+    py = list(rng.uniform(-2, 80, 4000))
+    px += list(lx)                              # on vertices
+    py += list(ly)
+    px += [1.5] * 40                            # on the first segment of every line
+    py += [2.0 * i for i in range(40)]
+    px += [1.5] * 39                            # exactly between two lines: tie
+    py += [2.0 * i + 1.0 for i in range(39)]
+    px, py = np.array(px), np.array(py)
+    w = D.Workload("lines", px, py, -5.0, 95.0, -5.0, 95.0, 100.0 / 64, 6, 16)
+    pts = cs.GeoSeries.from_points(px, py)
+    pi, t = cs.quadtree_on_points(pts, w.x_min, w.x_max, w.y_min, w.y_max, w.scale, 6, 16)
+    xy = _xy(lx, ly, np.float64)
+    lines = cs.GeoSeries.from_linestrings_xy(xy, np.array(offs), np.arange(len(offs)))
+    bb = cs.linestring_bounding_boxes(lines, 1.5)
+    j = cs.join_quadtree_and_bounding_boxes(t, bb, w.x_min, w.x_max, w.y_min, w.y_max, w.scale, 6)
+    r = cs.quadtree_point_to_nearest_linestring(j, t, pi, pts, lines, method=method)
+    opi, ot = O.quadtree_on_points(px, py, w.x_min, w.x_max, w.y_min, w.y_max, w.scale, 6, 16)
+    obb = O.linestring_bounding_boxes(np.array(offs), lx, ly, 1.5)
+    oj = O.join_quadtree_and_bounding_boxes(ot, obb, w.x_min, w.x_max, w.y_min, w.y_max,
+                                            w.scale, 6)
+    orr = O.quadtree_point_to_nearest_linestring(oj, ot, opi, px, py, np.array(offs), lx, ly)
+    np.testing.assert_array_equal(u32(r["point_index"]), orr["point_index"])
+    np.testing.assert_array_equal(u32(r["linestring_index"]), orr["linestring_index"])
+    np.testing.assert_array_equal(to_np(r["distance"]), orr["distance"])
