@@ -36,6 +36,21 @@ class CsptQuadtree(ctypes.Structure):
                 ("offset", _vp), ("num_nodes", _sz)]
 
 
+class CsptInstanceParams(ctypes.Structure):
+    _fields_ = [("x_min", ctypes.c_double), ("x_max", ctypes.c_double),
+                ("y_min", ctypes.c_double), ("y_max", ctypes.c_double),
+                ("scale", ctypes.c_double), ("max_depth", ctypes.c_int32),
+                ("max_size", ctypes.c_int32)]
+
+
+class CsptBatchedPipInfo(ctypes.Structure):
+    _fields_ = [("num_instances", _sz), ("num_points", _sz), ("num_polygons", _sz),
+                ("num_nodes", _sz), ("num_pairs", _sz), ("num_rows", _sz),
+                ("kernels_per_run", ctypes.c_uint64), ("polygon_index", _vp),
+                ("point_index", _vp), ("row_offsets", _vp), ("point_indices", _vp),
+                ("tree", CsptQuadtree), ("node_offsets", _vp)]
+
+
 class CuspatialError(RuntimeError):
     """Raised for CUDA, allocation and timeout failures reported by the library."""
 
@@ -72,6 +87,19 @@ def _declare(lib):
         _vp, _vp, _sz, ctypes.POINTER(CsptQuadtree), _vp, _sz, _vp, _vp, _sz, _vp, _sz, _vp, _vp,
         _sz, ctypes.c_int, ctypes.c_int, ctypes.POINTER(CsptAllocator), _vp, _vp, _vp, _vp,
         ctypes.POINTER(_sz)]
+    _u64p = ctypes.POINTER(ctypes.c_uint64)
+    lib.cspt_batched_pip_plan.argtypes = [
+        _sz, _u64p, _vp, _vp, _u64p, _vp, _sz, _vp, _sz, _vp, _vp, _sz,
+        ctypes.POINTER(CsptInstanceParams), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+        ctypes.POINTER(CsptAllocator), _vp, ctypes.POINTER(_vp)]
+    lib.cspt_batched_pip_run.argtypes = [_vp, ctypes.c_int, _vp]
+    lib.cspt_batched_pip_get_info.argtypes = [_vp, ctypes.POINTER(CsptBatchedPipInfo)]
+    lib.cspt_batched_pip_refined_count.argtypes = [_vp, _vp, _u64p]
+    lib.cspt_batched_pip_free.argtypes = [_vp]
+    lib.cspt_batched_pip_free.restype = None
+    for name in ("cspt_batched_pip_plan", "cspt_batched_pip_run", "cspt_batched_pip_get_info",
+                 "cspt_batched_pip_refined_count"):
+        getattr(lib, name).restype = ctypes.c_int
     for name in ("cspt_quadtree_on_points", "cspt_polygon_bounding_boxes",
                  "cspt_linestring_bounding_boxes", "cspt_join_quadtree_and_bounding_boxes",
                  "cspt_quadtree_point_in_polygon", "cspt_quadtree_point_to_nearest_linestring"):

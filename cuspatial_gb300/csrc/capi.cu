@@ -101,6 +101,8 @@ void resolve_pending()
 }  // namespace
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+void uncount_launches(uint64_t n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
 
 KernelTimer::KernelTimer(char const* name, cudaStream_t stream) : name_(name), stream_(stream)
 {

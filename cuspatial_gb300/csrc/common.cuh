@@ -48,8 +48,11 @@ void clear_last_error();
   } while (0)
 
 // Every kernel launch site is followed by CSPT_CHECK_LAUNCH(), which also
-// counts the launch (cspt_launch_count()).
+// counts the launch (cspt_launch_count()).  Launches recorded into a CUDA
+// graph are taken back after the capture and counted per replay instead.
 void count_launch();
+void count_launches(uint64_t n);
+void uncount_launches(uint64_t n);
 #define CSPT_CHECK_LAUNCH()                     \
   do {                                          \
     ::cspt::count_launch();                     \

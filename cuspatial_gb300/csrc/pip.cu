@@ -396,7 +396,8 @@ __global__ void __launch_bounds__(256)
                     size_t npairs, uint32_t const* __restrict__ qlen,
                     uint32_t const* __restrict__ qoff, uint64_t const* __restrict__ word_off,
                     uint32_t const* __restrict__ bits, uint64_t const* __restrict__ out_off,
-                    uint32_t* __restrict__ out_poly, uint32_t* __restrict__ out_point)
+                    uint32_t* __restrict__ out_poly, uint32_t* __restrict__ out_point,
+                    uint64_t cap)
 {
   int const lane     = threadIdx.x & 31;
   unsigned const lt  = (1u << lane) - 1u;
@@ -413,8 +414,10 @@ __global__ void __launch_bounds__(256)
       if (w == 0) continue;
       if (w & (1u << lane)) {
         uint64_t const d = o + __popc(w & lt);
-        out_poly[d]      = poly;
-        out_point[d]     = off + c + lane;
+        if (d < cap) {
+          out_poly[d]  = poly;
+          out_point[d] = off + c + lane;
+        }
       }
       o += __popc(w);
     }
@@ -510,7 +513,7 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
     KernelTimer timer("pip_expand", s);
     pip_expand_kernel<<<grd, blk, 0, s>>>(pair_poly, pair_quad, npairs, qlen, qoff,
                                           word_off.data(), bits.data(), out_off.data(),
-                                          op.data(), oq.data());
+                                          op.data(), oq.data(), m);
     CSPT_CHECK_LAUNCH();
   }
   *out_poly  = op.release();
@@ -518,6 +521,154 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
 }
 
 }  // namespace
+
+// ---------------------------------------------------------------------------
+// PipExec: a point-in-polygon evaluation over fixed pairs, tree and polygon
+// index (float64).  The constructor plans and allocates (and synchronises);
+// execute() only launches kernels into those buffers — no allocation, no
+// host synchronisation — so it can be captured into a CUDA graph and
+// replayed.  Outputs beyond the capacity are dropped and *overflow() tells.
+// block_threads (a multiple of 32, at most 256) is the block size of the
+// per-pair kernels; grids hold at most 256 warps per SM and stride beyond.
+// ---------------------------------------------------------------------------
+struct GroupOf {
+  uint32_t const* pair_quad;
+  __device__ uint32_t operator()(size_t k) const
+  {
+    return (k == 0 || pair_quad[k] != pair_quad[k - 1]) ? 1u : 0u;
+  }
+};
+struct StoreGroups {
+  uint32_t* gs;
+  uint32_t* pg;
+  __device__ void operator()(size_t k, uint32_t e, uint32_t f) const
+  {
+    if (f) gs[e] = static_cast<uint32_t>(k);
+    pg[k] = e + f - 1u;
+  }
+};
+struct WordsOf {
+  uint32_t const* pair_quad;
+  uint32_t const* qlen;
+  __device__ uint64_t operator()(size_t k) const
+  {
+    return static_cast<uint64_t>((qlen[pair_quad[k]] + 31u) >> 5);
+  }
+};
+struct CountsOf {
+  uint32_t const* c;
+  __device__ uint64_t operator()(size_t k) const { return c[k]; }
+};
+struct Store64 {
+  uint64_t* p;
+  __device__ void operator()(size_t k, uint64_t e, uint64_t) const { p[k] = e; }
+};
+
+__global__ void overflow_kernel(uint64_t const* total, uint64_t cap, int* flag)
+{
+  *flag = *total > cap ? 1 : 0;
+}
+
+class PipExec::Impl {
+ public:
+  Impl(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs, uint32_t const* qlen,
+       uint32_t const* qoff, uint32_t const* point_indices, size_t npi, double const* x,
+       double const* y, PolygonIndexView<double> ix, bool filtered, unsigned block,
+       Allocator const& alloc)
+    : pp_(pair_poly), pq_(pair_quad), np_(npairs), qlen_(qlen), qoff_(qoff),
+      pi_(point_indices), npi_(npi), x_(x), y_(y), ix_(ix), filtered_(filtered), blk_(block)
+  {
+    cudaStream_t const s = alloc.stream();
+    size_t const parts   = (npairs + kScanTile - 1) / kScanTile + 1;
+    word_off_ = Buffer<uint64_t>(alloc, npairs + 1);
+    out_off_  = Buffer<uint64_t>(alloc, npairs + 1);
+    partials_ = Buffer<uint64_t>(alloc, parts);
+    gpart_    = Buffer<uint32_t>(alloc, parts);
+    counts_   = Buffer<uint32_t>(alloc, npairs);
+    gstart_   = Buffer<uint32_t>(alloc, npairs + 1);
+    pgroup_   = Buffer<uint32_t>(alloc, npairs);
+    frames_   = Buffer<LeafFrame>(alloc, npairs);
+    u_        = Buffer<float2>(alloc, filtered ? npi : 0);
+    refined_  = Buffer<unsigned long long>(alloc, 1);
+    flag_     = Buffer<int>(alloc, 1);
+    scan_apply_prealloc<uint64_t>(WordsOf{pair_quad, qlen}, Store64{word_off_.data()}, npairs,
+                                  word_off_.data() + npairs, partials_.data(), s);
+    nwords_ = read_back(word_off_.data() + npairs, s);
+    bits_   = Buffer<uint32_t>(alloc, nwords_);
+    scan_apply_prealloc<uint32_t>(GroupOf{pair_quad}, StoreGroups{gstart_.data(), pgroup_.data()},
+                                  npairs, gstart_.data() + npairs, gpart_.data(), s);
+  }
+
+  // launches the evaluation; outputs go to op/oq up to cap entries
+  void execute(cudaStream_t s, uint32_t* op, uint32_t* oq, uint64_t cap)
+  {
+    unsigned const blk = blk_;
+    unsigned const grd = grid_for(np_ * 32, blk, 152u * 8u * 1024u / blk);
+    CSPT_CUDA_TRY(cudaMemsetAsync(refined_.data(), 0, sizeof(unsigned long long), s));
+    if (filtered_) {
+      leaf_frame_kernel<<<grd, blk, 0, s>>>(gstart_.data(), gstart_.data() + np_, pq_, qlen_,
+                                            qoff_, pi_, npi_, x_, y_, ix_.grid, u_.data(),
+                                            frames_.data());
+      CSPT_CHECK_LAUNCH();
+      pip_pair_kernel<true><<<grd, blk, 0, s>>>(pp_, pq_, pgroup_.data(), np_, qlen_, qoff_, pi_,
+                                                npi_, x_, y_, u_.data(), frames_.data(), ix_,
+                                                word_off_.data(), bits_.data(), counts_.data(),
+                                                refined_.data());
+    } else {
+      pip_pair_kernel<false><<<grd, blk, 0, s>>>(pp_, pq_, nullptr, np_, qlen_, qoff_, pi_, npi_,
+                                                 x_, y_, nullptr, nullptr, ix_, word_off_.data(),
+                                                 bits_.data(), counts_.data(), nullptr);
+    }
+    CSPT_CHECK_LAUNCH();
+    scan_apply_prealloc<uint64_t>(CountsOf{counts_.data()}, Store64{out_off_.data()}, np_,
+                                  out_off_.data() + np_, partials_.data(), s);
+    pip_expand_kernel<<<grd, blk, 0, s>>>(pp_, pq_, np_, qlen_, qoff_, word_off_.data(),
+                                          bits_.data(), out_off_.data(), op, oq, cap);
+    CSPT_CHECK_LAUNCH();
+    overflow_kernel<<<1, 1, 0, s>>>(out_off_.data() + np_, cap, flag_.data());
+    CSPT_CHECK_LAUNCH();
+  }
+
+  uint64_t const* total() const { return out_off_.data() + np_; }
+  uint64_t const* pair_out_offsets() const { return out_off_.data(); }
+  int const* overflow() const { return flag_.data(); }
+  unsigned long long const* refined() const { return refined_.data(); }
+
+ private:
+  uint32_t const *pp_, *pq_;
+  size_t np_;
+  uint32_t const *qlen_, *qoff_, *pi_;
+  size_t npi_;
+  double const *x_, *y_;
+  PolygonIndexView<double> ix_;
+  bool filtered_;
+  unsigned blk_;
+  size_t nwords_ = 0;
+  Buffer<uint64_t> word_off_, out_off_, partials_;
+  Buffer<uint32_t> gpart_, counts_, gstart_, pgroup_, bits_;
+  Buffer<LeafFrame> frames_;
+  Buffer<float2> u_;
+  Buffer<unsigned long long> refined_;
+  Buffer<int> flag_;
+};
+
+PipExec::PipExec(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
+                 uint32_t const* qlen, uint32_t const* qoff, uint32_t const* point_indices,
+                 size_t npi, double const* x, double const* y, PolygonIndexView<double> const& ix,
+                 bool filtered, unsigned block_threads, Allocator const& alloc)
+  : impl_(new Impl(pair_poly, pair_quad, npairs, qlen, qoff, point_indices, npi, x, y, ix,
+                   filtered, block_threads, alloc))
+{
+}
+PipExec::~PipExec() { delete impl_; }
+void PipExec::execute(cudaStream_t s, uint32_t* op, uint32_t* oq, uint64_t cap)
+{
+  impl_->execute(s, op, oq, cap);
+}
+uint64_t const* PipExec::total() const { return impl_->total(); }
+uint64_t const* PipExec::pair_out_offsets() const { return impl_->pair_out_offsets(); }
+int const* PipExec::overflow() const { return impl_->overflow(); }
+unsigned long long const* PipExec::refined() const { return impl_->refined(); }
 
 void quadtree_point_in_polygon(uint32_t const* pair_poly, uint32_t const* pair_quad,
                                size_t npairs, cspt_quadtree const* tree,

@@ -97,4 +97,25 @@ class PolygonIndex {
   PolygonIndexView<T> v_{};
 };
 
+// A planned float64 point-in-polygon evaluation (defined in pip.cu).
+class PipExec {
+ public:
+  PipExec(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
+          uint32_t const* qlen, uint32_t const* qoff, uint32_t const* point_indices, size_t npi,
+          double const* x, double const* y, PolygonIndexView<double> const& ix, bool filtered,
+          unsigned block_threads, Allocator const& alloc);
+  ~PipExec();
+  PipExec(PipExec const&)            = delete;
+  PipExec& operator=(PipExec const&) = delete;
+  void execute(cudaStream_t s, uint32_t* out_poly, uint32_t* out_point, uint64_t cap);
+  uint64_t const* total() const;             // device: number of output pairs
+  uint64_t const* pair_out_offsets() const;  // device: first output of each pair
+  int const* overflow() const;               // device: 1 when total > cap
+  unsigned long long const* refined() const;
+
+ private:
+  class Impl;
+  Impl* impl_;
+};
+
 }  // namespace cspt

@@ -11,6 +11,11 @@ machine.  All sizes can be scaled down (same distributions) for tests.
                        of an edge; 100,000 star polygons (8-512 vertices,
                        radius U[2,60] per polygon with per-vertex factor
                        U[0.5,1]), 10% with a reversed hole at 0.4 scale.
+  batched_instances    4096 independent instances: points per instance
+                       log-uniform in [1e3, 1e6], uniform in a box of side
+                       U[100, 10000] at a random origin; polygons per
+                       instance log-uniform in [1, 2000], star-shaped with
+                       4-256 vertices and radius 0.5%-5% of the box side.
   nearest_linestring   50,000,000 uniform points in [0,10000)^2, 200,000
                        random-walk linestrings (2-256 segments, step U[1,20],
                        heading change N(0, 0.3 rad)).
@@ -87,29 +92,34 @@ def star_polygons(rng, centers, nverts, radius_fn, hole_fraction=0.0, hole_scale
     vx = np.repeat(centers[:, 0], nverts) + r * np.cos(ang)
     vy = np.repeat(centers[:, 1], nverts) + r * np.sin(ang)
     has_hole = rng.random(p) < hole_fraction
-    # assemble rings: outer (closed), optional hole (reversed, closed)
-    xs, ys, ring_len, rings_per_poly = [], [], [], np.where(has_hole, 2, 1)
+    # rings: outer closed by repeating its first vertex, then (optionally) the
+    # hole: the closed outer ring scaled about the centre and reversed
+    ring_len = nverts + 1
+    rings_per_poly = np.where(has_hole, 2, 1)
+    poly_len = ring_len * rings_per_poly
+    pstart = np.concatenate([[0], np.cumsum(poly_len)])
     vstart = np.concatenate([[0], np.cumsum(nverts)])
-    ring_sizes = []
-    out_x = []
-    out_y = []
-    for i in range(p):
-        a, b = vstart[i], vstart[i + 1]
-        ox = np.append(vx[a:b], vx[a])
-        oy = np.append(vy[a:b], vy[a])
-        out_x.append(ox)
-        out_y.append(oy)
-        ring_sizes.append(len(ox))
-        if has_hole[i]:
-            cx, cy = centers[i]
-            hx = (cx + hole_scale * (ox - cx))[::-1]
-            hy = (cy + hole_scale * (oy - cy))[::-1]
-            out_x.append(hx)
-            out_y.append(hy)
-            ring_sizes.append(len(hx))
-    del xs, ys, ring_len
-    x = np.concatenate(out_x)
-    y = np.concatenate(out_y)
+    total = int(pstart[-1])
+    x = np.empty(total)
+    y = np.empty(total)
+    # outer ring: position pstart + j (j < k) takes vertex j, j = k closes
+    pos = np.repeat(pstart[:-1], nverts) + local
+    x[pos] = vx
+    y[pos] = vy
+    x[pstart[:-1] + nverts] = vx[vstart[:-1]]
+    y[pstart[:-1] + nverts] = vy[vstart[:-1]]
+    hp = np.nonzero(has_hole)[0]
+    if len(hp):
+        hk = ring_len[hp]
+        hpos = np.repeat(pstart[hp] + hk, hk) + (np.arange(hk.sum()) -
+                                                  np.repeat(np.cumsum(hk) - hk, hk))
+        j = hpos - np.repeat(pstart[hp] + hk, hk)          # 0..k within the hole
+        src = np.repeat(pstart[hp], hk) + (np.repeat(hk, hk) - 1 - j)  # reversed outer
+        cx = np.repeat(centers[hp, 0], hk)
+        cy = np.repeat(centers[hp, 1], hk)
+        x[hpos] = cx + hole_scale * (x[src] - cx)
+        y[hpos] = cy + hole_scale * (y[src] - cy)
+    ring_sizes = np.repeat(ring_len, rings_per_poly)
     ring_offset = np.concatenate([[0], np.cumsum(ring_sizes)]).astype(np.int32)
     part_offset = np.concatenate([[0], np.cumsum(rings_per_poly)]).astype(np.int32)
     geometry_offset = np.arange(p + 1, dtype=np.int32)
@@ -215,3 +225,53 @@ def nearest_linestring(n_points=50_000_000, n_linestrings=200_000, extent=10000.
     ls = Linestrings(lx, ly, voff.astype(np.int32), np.arange(n_linestrings + 1, dtype=np.int32))
     return Workload("nearest_linestring", x, y, 0.0, extent, 0.0, extent, extent / 16384, 14,
                     256, linestrings=ls, expansion_radius=25.0)
+
+
+@dataclass
+class BatchedWorkload:
+    """Concatenated instances: instance i owns points
+    [point_offsets[i], point_offsets[i+1]) and polygons
+    [polygon_offsets[i], polygon_offsets[i+1]) of `polygons` (global ring and
+    vertex offsets); box[i] = (x_min, x_max, y_min, y_max)."""
+    x: np.ndarray
+    y: np.ndarray
+    point_offsets: np.ndarray
+    polygons: Polygons
+    polygon_offsets: np.ndarray
+    boxes: np.ndarray
+
+    @property
+    def num_instances(self):
+        return len(self.point_offsets) - 1
+
+
+def _log_uniform_int(rng, lo, hi, n):
+    return np.floor(np.exp(rng.uniform(math.log(lo), math.log(hi), n))).astype(np.int64)
+
+
+def batched_instances(n_instances=4096, points_range=(1e3, 1e6), polygons_range=(1, 2000),
+                      side_range=(100.0, 10000.0), vertices_range=(4, 256), seed_offset=0):
+    rng = np.random.Generator(np.random.PCG64(SEED + 2 + seed_offset))
+    npts = _log_uniform_int(rng, points_range[0], points_range[1], n_instances)
+    npoly = _log_uniform_int(rng, polygons_range[0], polygons_range[1], n_instances)
+    side = rng.uniform(side_range[0], side_range[1], n_instances)
+    origin = rng.uniform(-50000.0, 50000.0, (n_instances, 2))
+    boxes = np.stack([origin[:, 0], origin[:, 0] + side, origin[:, 1], origin[:, 1] + side], 1)
+    point_offsets = np.concatenate([[0], np.cumsum(npts)]).astype(np.uint64)
+    total = int(point_offsets[-1])
+    x = np.empty(total)
+    y = np.empty(total)
+    for i in range(n_instances):
+        a, b = int(point_offsets[i]), int(point_offsets[i + 1])
+        u = rng.random((2, b - a))
+        np.minimum(origin[i, 0] + side[i] * u[0], np.nextafter(boxes[i, 1], -np.inf), out=x[a:b])
+        np.minimum(origin[i, 1] + side[i] * u[1], np.nextafter(boxes[i, 3], -np.inf), out=y[a:b])
+    pinst = np.repeat(np.arange(n_instances), npoly)
+    u = rng.uniform(0.05, 0.95, (len(pinst), 2))
+    centers = origin[pinst] + u * side[pinst, None]
+    k = rng.integers(vertices_range[0], vertices_range[1] + 1, len(pinst))
+    prad = side[pinst] * rng.uniform(0.005, 0.05, len(pinst))
+    polys = star_polygons(rng, centers, k,
+                          lambda g, pid: prad[pid] * g.uniform(0.5, 1.0, len(pid)))
+    polygon_offsets = np.concatenate([[0], np.cumsum(npoly)]).astype(np.uint64)
+    return BatchedWorkload(x, y, point_offsets, polys, polygon_offsets, boxes)

@@ -211,6 +211,85 @@ cspt_status cspt_quadtree_point_to_nearest_linestring(
   uint32_t* out_point_index, uint32_t* out_linestring_index, void* out_distance,
   size_t* out_num_rows);
 
+/* ------------------------------------------------------------------------
+ * Batched point-in-polygon join (no counterpart in the reference, which
+ * joins one point set with one polygon set per call).
+ *
+ * Many independent instances, each with its own points, polygons and
+ * quadtree parameters, are planned together: one tree build over all
+ * points, one box join over all polygons, one polygon index.  Running the
+ * plan evaluates every instance's candidate pairs in the same kernels and
+ * writes, per instance, exactly the rows that
+ *   cspt_quadtree_on_points -> cspt_polygon_bounding_boxes (radius 0) ->
+ *   cspt_join_quadtree_and_bounding_boxes -> cspt_quadtree_point_in_polygon
+ * return for that instance alone with its parameters.
+ *
+ * Inputs (device, float64): x/y of all points, instance i owning points
+ * [point_offsets[i], point_offsets[i+1]); a polygon column whose
+ * poly_offsets index ring_offsets and whose ring_offsets index poly_x/poly_y
+ * (global offsets), instance i owning polygons
+ * [polygon_offsets[i], polygon_offsets[i+1]).  point_offsets,
+ * polygon_offsets (num_instances + 1 entries each, starting at 0) and params
+ * are HOST arrays.  Every polygon must have at least one vertex.  Inputs are
+ * borrowed for the plan's lifetime.
+ * ------------------------------------------------------------------------ */
+typedef struct cspt_instance_params {
+  double x_min, x_max, y_min, y_max; /* quadtree area: x_min < x_max, y_min < y_max */
+  double scale;                      /* raised to max(dx, dy) / ((1 << max_depth) + 2) */
+  int32_t max_depth;                 /* 1..15 */
+  int32_t max_size;                  /* raised to 1 */
+} cspt_instance_params;
+
+typedef struct cspt_batched_pip cspt_batched_pip;
+
+/* Results of a plan (device pointers owned by the plan).  Rows of instance i
+ * are [row_offsets[i], row_offsets[i+1]); polygon_index is local to the
+ * instance's polygons and point_index is a position in the instance's
+ * point_indices.  point_indices holds instance i's sorted point order at
+ * [point_offsets[i], point_offsets[i+1]) with instance-local values; tree
+ * holds instance i's nodes at [node_offsets[i], node_offsets[i+1]) with
+ * instance-local child and point offsets.  Rows are valid once a run has
+ * completed. */
+typedef struct cspt_batched_pip_info {
+  size_t num_instances, num_points, num_polygons, num_nodes, num_pairs, num_rows;
+  uint64_t kernels_per_run; /* kernel launches one graph replay makes (0 before capture) */
+  const uint32_t* polygon_index;
+  const uint32_t* point_index;
+  const uint64_t* row_offsets;
+  const uint32_t* point_indices;
+  cspt_quadtree tree;
+  const uint64_t* node_offsets;
+} cspt_batched_pip_info;
+
+/* Builds the trees, joins the boxes, builds the polygon index and sizes the
+ * outputs by one evaluation; synchronises `stream`.  method selects plain
+ * float64 or float32-filtered evaluation (same rows).  block_threads (a
+ * multiple of 32 up to 256; 256 is a good default) is the block size of the
+ * per-pair kernels.  Device memory comes from mr on `stream`, which must stay
+ * valid until cspt_batched_pip_free. */
+cspt_status cspt_batched_pip_plan(
+  size_t num_instances, const uint64_t* point_offsets, const void* x, const void* y,
+  const uint64_t* polygon_offsets, const uint32_t* poly_offsets, size_t num_poly_offsets,
+  const uint32_t* ring_offsets, size_t num_ring_offsets, const void* poly_x, const void* poly_y,
+  size_t num_poly_vertices, const cspt_instance_params* params, cspt_dtype dtype,
+  cspt_method method, int block_threads, const cspt_allocator* mr, void* stream,
+  cspt_batched_pip** out_plan);
+
+/* Evaluates all instances on `stream` (asynchronous; allocates nothing).
+ * With use_graph != 0 the evaluation is recorded into a CUDA graph on the
+ * first such call and replayed as one graph launch afterwards. */
+cspt_status cspt_batched_pip_run(cspt_batched_pip* plan, int use_graph, void* stream);
+
+cspt_status cspt_batched_pip_get_info(const cspt_batched_pip* plan, cspt_batched_pip_info* out);
+
+/* Candidates re-evaluated in float64 by the last run (filtered method);
+ * synchronises `stream`. */
+cspt_status cspt_batched_pip_refined_count(const cspt_batched_pip* plan, void* stream,
+                                           uint64_t* out);
+
+/* Frees the plan; runs issued on it must have completed. */
+void cspt_batched_pip_free(cspt_batched_pip* plan);
+
 #ifdef __cplusplus
 }
 #endif
