@@ -46,9 +46,14 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="target CPU time of the oracle baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", choices=["precision", "batched"], default="precision",
+    ap.add_argument("--workload", choices=["precision", "batched", "serving"],
+                    default="precision",
                     help="precision: the 100M-point join (default line); batched: 4096 "
-                         "independent instances through the batched plan")
+                         "independent instances through the batched plan; serving: Poisson "
+                         "requests against a resident 250k-polygon set")
+    ap.add_argument("--requests", type=int, default=4000)
+    ap.add_argument("--rate", type=float, default=2000.0)
+    ap.add_argument("--streams", type=int, default=4)
     ap.add_argument("--instances", type=int, default=4096)
     ap.add_argument("--single-sample", type=int, default=64,
                     help="instances timed through the single-instance calls (batched)")
@@ -681,6 +686,80 @@ def run_batched(args, dist):
         print(json.dumps(line), flush=True)
 
 
+def run_serving(args, dist):
+    """A resident set of 250,000 star polygons over [0,20000)^2 and a Poisson
+    stream of requests (log-uniform [1, 1e5] points, half uniform, half one
+    Gaussian cluster); admission by a 40 GB device-memory budget."""
+    import torch
+
+    import cuspatial_gb300 as cs
+    from cuspatial_gb300 import _lib, datasets
+    from cuspatial_gb300.serving import PolygonSet, Server, request_params, run_poisson
+
+    torch.cuda.set_device(dist.local)
+    dist.init("nccl")
+    lib = _lib.load()
+    lib.cspt_launch_count.restype = ctypes.c_uint64
+    t0 = time.time()
+    P = datasets.serving_polygons()
+    reqs = datasets.serving_requests(args.requests)
+    warm = datasets.serving_requests(200, seed_offset=1)
+    gen_s = time.time() - t0
+    gp = cs.GeoSeries.from_polygons_xy(polygons_xy(P), P.ring_offset, P.part_offset,
+                                       P.geometry_offset)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    pset = PolygonSet(gp)
+    torch.cuda.synchronize()
+    set_ms = (time.perf_counter() - t) * 1e3
+    params = [request_params(r.x, r.y) for r in reqs]
+    wparams = [request_params(r.x, r.y) for r in warm]
+    budget = 40 << 30
+    out = {}
+    for method in (["filtered", "exact"] if args.method == "filtered" else [args.method]):
+        with Server(pset, memory_budget_bytes=budget, num_streams=args.streams,
+                    method=method) as srv:
+            run_poisson(srv, warm, rate=0, params=wparams, seed=1)
+            clocks = ClockSampler(dist.local)
+            clocks.start()
+            l0 = lib.cspt_launch_count()
+            live = run_poisson(srv, reqs, rate=args.rate, params=params, seed=2)
+            l1 = lib.cspt_launch_count()
+            sat = run_poisson(srv, reqs, rate=0, params=params, seed=3)
+            clock_info = clocks.stop()
+            st = srv.stats()
+        out[method] = {"live": live, "saturated": sat, "stats": st, "clocks": clock_info,
+                       "launches_live": int(l1 - l0)}
+    f = out[args.method]
+    value = f["saturated"]["points_per_s"] * args.gpus
+    line = {
+        "metric": METRIC, "workload": "serving", "value": value, "unit": "points/s",
+        "n_gpus": args.gpus, "steps": args.requests, "warmup": len(warm),
+        "ms_per_step": f["saturated"]["span_s"] * 1e3 / args.requests,
+        "p50_ms": f["live"]["p50_ms"], "p99_ms": f["live"]["p99_ms"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded numpy PCG64; shapes of the serving config)",
+        "config": {"workload": "serving: 250,000 resident star polygons (8-256 vertices, "
+                               "radius U[1,30]) on a jittered 500x500 grid over [0,20000)^2; "
+                               "%d Poisson requests at %.0f req/s, log-uniform [1,1e5] points"
+                               % (args.requests, args.rate),
+                   "polygons": P.num_polygons, "vertices": len(P.x),
+                   "requests": args.requests, "points": f["live"]["points"],
+                   "memory_budget_bytes": budget, "streams": args.streams,
+                   "method": args.method,
+                   "step": "one request (value: points/s with all requests queued at once; "
+                           "p50/p99: latency at the offered Poisson rate)"},
+        "polygon_set_ms": set_ms,
+        "live": f["live"], "saturated": f["saturated"], "server_stats": f["stats"],
+        "plain_fp64": ({"live": out["exact"]["live"], "saturated": out["exact"]["saturated"]}
+                       if "exact" in out and args.method != "exact" else None),
+        "gpu_launches": f["launches_live"], "clocks": f["clocks"], "generation_s": gen_s,
+    }
+    pset.close()
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     dist = Dist()
@@ -688,6 +767,8 @@ def main():
         run_reference(args, dist)
     elif args.workload == "batched":
         run_batched(args, dist)
+    elif args.workload == "serving":
+        run_serving(args, dist)
     else:
         run_ours(args, dist)
 

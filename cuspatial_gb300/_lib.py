@@ -51,6 +51,28 @@ class CsptBatchedPipInfo(ctypes.Structure):
                 ("tree", CsptQuadtree), ("node_offsets", _vp)]
 
 
+class CsptServerOptions(ctypes.Structure):
+    _fields_ = [("memory_budget_bytes", _sz), ("num_streams", ctypes.c_int),
+                ("max_batch_points", _sz), ("max_batch_requests", _sz),
+                ("method", ctypes.c_int), ("block_threads", ctypes.c_int)]
+
+
+class CsptServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
+                ("failed", ctypes.c_uint64), ("batches", ctypes.c_uint64),
+                ("split_batches", ctypes.c_uint64), ("queued", ctypes.c_uint64),
+                ("reserved_bytes", _sz), ("peak_device_bytes", _sz),
+                ("memory_budget_bytes", _sz), ("max_batch_requests_seen", ctypes.c_uint64)]
+
+
+class CsptRequestResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("error", ctypes.c_char_p),
+                ("polygon_index", _vp), ("point_index", _vp), ("num_rows", _sz),
+                ("point_indices", _vp), ("num_points", _sz), ("submit_s", ctypes.c_double),
+                ("admit_s", ctypes.c_double), ("done_s", ctypes.c_double),
+                ("batch", ctypes.c_uint64), ("batch_requests", ctypes.c_uint32)]
+
+
 class CuspatialError(RuntimeError):
     """Raised for CUDA, allocation and timeout failures reported by the library."""
 
@@ -97,6 +119,28 @@ def _declare(lib):
     lib.cspt_batched_pip_refined_count.argtypes = [_vp, _vp, _u64p]
     lib.cspt_batched_pip_free.argtypes = [_vp]
     lib.cspt_batched_pip_free.restype = None
+    lib.cspt_polygon_set_create.argtypes = [_vp, _sz, _vp, _sz, _vp, _vp, _sz, ctypes.c_int,
+                                            ctypes.POINTER(CsptAllocator), _vp,
+                                            ctypes.POINTER(_vp)]
+    lib.cspt_polygon_set_free.argtypes = [_vp]
+    lib.cspt_polygon_set_free.restype = None
+    lib.cspt_server_create.argtypes = [_vp, ctypes.POINTER(CsptServerOptions),
+                                       ctypes.POINTER(_vp)]
+    lib.cspt_server_submit.argtypes = [_vp, ctypes.c_uint64, _vp, _vp, _sz,
+                                       ctypes.POINTER(CsptInstanceParams)]
+    lib.cspt_server_poll.argtypes = [_vp, ctypes.POINTER(ctypes.c_uint64), _sz, ctypes.c_double]
+    lib.cspt_server_poll.restype = _sz
+    lib.cspt_server_result.argtypes = [_vp, ctypes.c_uint64, ctypes.POINTER(CsptRequestResult)]
+    lib.cspt_server_release.argtypes = [_vp, ctypes.c_uint64]
+    lib.cspt_server_release.restype = None
+    lib.cspt_server_now.argtypes = [_vp]
+    lib.cspt_server_now.restype = ctypes.c_double
+    lib.cspt_server_get_stats.argtypes = [_vp, ctypes.POINTER(CsptServerStats)]
+    lib.cspt_server_free.argtypes = [_vp]
+    lib.cspt_server_free.restype = None
+    for name in ("cspt_polygon_set_create", "cspt_server_create", "cspt_server_submit",
+                 "cspt_server_result", "cspt_server_get_stats"):
+        getattr(lib, name).restype = ctypes.c_int
     for name in ("cspt_batched_pip_plan", "cspt_batched_pip_run", "cspt_batched_pip_get_info",
                  "cspt_batched_pip_refined_count"):
         getattr(lib, name).restype = ctypes.c_int

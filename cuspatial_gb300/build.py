@@ -70,7 +70,7 @@ def build(verbose=False, ptxas_info=False, force=False):
                 print("==", os.path.basename(obj), file=sys.stderr)
                 print(err, file=sys.stderr)
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *[o for o, _ in results], "-lcudart"]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *[o for o, _ in results], "-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))

@@ -1,0 +1,614 @@
+// A forest of point quadtrees, one per instance, built in one pass.
+//
+// Instance i owns points [pt_begin_i, pt_end_i) of concatenated x/y columns
+// and has its own quadtree_on_points parameters.  The forest holds the
+// concatenation of the per-instance results:
+//   * point_indices: instance i's sorted point order at [pt_begin_i,
+//     pt_end_i), values local to the instance (pidx) and global (sidx);
+//   * quadtree: instance i's nodes at [node_offsets_i, node_offsets_{i+1}),
+//     child and point offsets local to the instance, plus goff = the leaf's
+//     first position in the global sorted order.
+// Each instance's part equals what quadtree_on_points returns for it alone
+// (cpp/include/cuspatial/detail/point_quadtree.cuh:237-272).
+//
+// Points are sorted once by the composite key (instance << kb) | morton key,
+// which keeps instances contiguous and each instance's points in its own
+// stable Morton order.  The single-tree construction (quadtree.cu) carries
+// over level by level with three changes: a sorted position starts a node at
+// every level when it is the first point of its instance, a level-l node
+// exists only for instances with max_depth > l, and node ends are clipped to
+// the instance's last point.  Kept nodes are then laid out instance-major,
+// level-major within the instance.
+#pragma once
+
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+#include "join_kernel.cuh"
+#include "radix_sort.cuh"
+#include "scan.cuh"
+
+namespace cspt {
+namespace {
+
+constexpr int kLevels       = 16;
+constexpr uint8_t kNoStart  = 0xFF;
+constexpr unsigned kBlk     = 256;
+constexpr unsigned kGridCap = 152u * 16u;
+
+struct Inst {
+  double minx, miny, maxx, maxy, scale;
+  uint32_t d, max_size;
+  uint32_t pt_begin, pt_end;
+  uint32_t poly_begin, poly_end;
+  uint32_t node_base, nq, L0;
+};
+
+// the instance whose [begin, next begin) holds v; begins has ni + 1 sorted
+// entries and begins[0] <= v < begins[ni]
+__device__ inline uint32_t find_instance(uint32_t const* __restrict__ begins, uint32_t ni,
+                                         uint32_t v)
+{
+  uint32_t lo = 0, hi = ni;
+  while (hi - lo > 1) {
+    uint32_t const mid = (lo + hi) >> 1;
+    if (begins[mid] <= v)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+#define CSPT_GRID_STRIDE(i, n)                                                           \
+  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < (n); \
+       i += static_cast<size_t>(gridDim.x) * blockDim.x)
+
+// phase_1.cuh:73-85 per instance, tagged with the instance
+__global__ void keys_kernel(double const* __restrict__ x, double const* __restrict__ y, size_t n,
+                            uint32_t const* __restrict__ pt_begin, uint32_t ni,
+                            Inst const* __restrict__ inst, int kb, uint64_t* __restrict__ keys)
+{
+  CSPT_GRID_STRIDE(i, n)
+  {
+    uint32_t const k = find_instance(pt_begin, ni, static_cast<uint32_t>(i));
+    Inst const& I    = inst[k];
+    double const px = x[i], py = y[i];
+    uint32_t key;
+    if (px < I.minx || px > I.maxx || py < I.miny || py > I.maxy) {
+      key = (1u << (2 * I.d)) - 1u;
+    } else {
+      uint16_t const cx = static_cast<uint16_t>((px - I.minx) / I.scale);
+      uint16_t const cy = static_cast<uint16_t>((py - I.miny) / I.scale);
+      key               = (spread16(cy) << 1) | spread16(cx);
+    }
+    keys[i] = (static_cast<uint64_t>(k) << kb) | key;
+  }
+}
+
+__global__ void start_level_kernel(uint64_t const* __restrict__ sk, size_t n, int kb,
+                                   Inst const* __restrict__ inst, uint8_t* __restrict__ lvl,
+                                   uint8_t* __restrict__ lim)
+{
+  uint64_t const mask = (uint64_t{1} << kb) - 1u;
+  CSPT_GRID_STRIDE(i, n)
+  {
+    uint64_t const c = sk[i];
+    uint32_t const k = static_cast<uint32_t>(c >> kb);
+    int const d      = static_cast<int>(inst[k].d);
+    uint8_t l        = 0;
+    if (i > 0 && (sk[i - 1] >> kb) == k) {
+      uint32_t const diff = static_cast<uint32_t>((c ^ sk[i - 1]) & mask);
+      if (diff == 0) {
+        l = kNoStart;
+      } else {
+        int const lv = d - 1 - (31 - __clz(diff)) / 2;
+        l            = static_cast<uint8_t>(lv < 0 ? 0 : lv);
+      }
+    }
+    lvl[i] = l;
+    lim[i] = static_cast<uint8_t>(d);
+  }
+}
+
+struct StartFlag {
+  uint8_t const* lvl;
+  uint8_t const* lim;
+  int l;
+  __device__ uint32_t operator()(size_t i) const
+  {
+    return (static_cast<int>(lvl[i]) <= l && l < static_cast<int>(lim[i])) ? 1u : 0u;
+  }
+};
+struct RankStore {
+  uint32_t* rank;
+  uint32_t* starts;
+  __device__ void operator()(size_t i, uint32_t e, uint32_t f) const
+  {
+    rank[i] = e;
+    if (f) starts[e] = static_cast<uint32_t>(i);
+  }
+};
+
+__device__ inline uint32_t node_end(uint32_t const* starts, size_t nl, size_t k, uint32_t iend)
+{
+  uint32_t const e = (k + 1 < nl) ? starts[k + 1] : iend;
+  return e < iend ? e : iend;
+}
+
+// point counts and instances of one level's nodes
+__global__ void count_kernel(uint32_t const* __restrict__ starts, size_t nl,
+                             uint64_t const* __restrict__ sk, int kb,
+                             Inst const* __restrict__ inst, uint32_t* __restrict__ count,
+                             uint32_t* __restrict__ ninst)
+{
+  CSPT_GRID_STRIDE(k, nl)
+  {
+    uint32_t const s = starts[k];
+    uint32_t const i = static_cast<uint32_t>(sk[s] >> kb);
+    count[k]         = node_end(starts, nl, k, inst[i].pt_end) - s;
+    ninst[k]         = i;
+  }
+}
+
+__global__ void child_count_kernel(uint32_t const* __restrict__ prev_starts, size_t nprev,
+                                   uint32_t const* __restrict__ prev_inst,
+                                   Inst const* __restrict__ inst,
+                                   uint32_t const* __restrict__ rank_cur,
+                                   uint32_t* __restrict__ child)
+{
+  CSPT_GRID_STRIDE(p, nprev)
+  {
+    uint32_t const e = node_end(prev_starts, nprev, p, inst[prev_inst[p]].pt_end);
+    child[p]         = rank_cur[e] - rank_cur[prev_starts[p]];
+  }
+}
+
+// phase_2.cuh:206-236 with the instance's max_size
+__global__ void keep_kernel(uint32_t const* __restrict__ starts, size_t nl,
+                            uint32_t const* __restrict__ ninst, uint8_t const* __restrict__ lvl,
+                            int prev_level, uint32_t const* __restrict__ rank_prev,
+                            uint32_t const* __restrict__ count_prev,
+                            Inst const* __restrict__ inst, uint8_t* __restrict__ keep)
+{
+  CSPT_GRID_STRIDE(k, nl)
+  {
+    uint32_t const i      = starts[k];
+    uint32_t const is_beg = static_cast<int>(lvl[i]) <= prev_level ? 1u : 0u;
+    uint32_t const parent = rank_prev[i] + is_beg - 1u;
+    keep[k]               = count_prev[parent] > inst[ninst[k]].max_size ? 1 : 0;
+  }
+}
+
+struct KeepIn {
+  uint8_t const* kp;
+  __device__ uint32_t operator()(size_t k) const { return kp ? kp[k] : 1u; }
+};
+struct PosOut {
+  uint32_t* ps;
+  __device__ void operator()(size_t k, uint32_t e, uint32_t) const { ps[k] = e; }
+};
+
+__global__ void compact_level_kernel(size_t nl, uint8_t const* __restrict__ kp,
+                                     uint32_t const* __restrict__ ps,
+                                     uint32_t const* __restrict__ starts,
+                                     uint32_t const* __restrict__ cnt,
+                                     uint32_t const* __restrict__ child,
+                                     uint32_t const* __restrict__ ninst,
+                                     uint64_t const* __restrict__ sk, int kb,
+                                     Inst const* __restrict__ inst, int level,
+                                     uint32_t* __restrict__ okey, uint32_t* __restrict__ ocount,
+                                     uint32_t* __restrict__ ochild, uint32_t* __restrict__ ostart,
+                                     uint32_t* __restrict__ oinst)
+{
+  uint64_t const mask = (uint64_t{1} << kb) - 1u;
+  CSPT_GRID_STRIDE(k, nl)
+  {
+    if (kp && !kp[k]) continue;
+    uint32_t const o   = ps[k];
+    uint32_t const i   = ninst[k];
+    int const shift    = 2 * (static_cast<int>(inst[i].d) - 1 - level);
+    uint32_t const key = static_cast<uint32_t>(sk[starts[k]] & mask);
+    okey[o]            = shift > 0 ? key >> shift : key;
+    ocount[o]          = cnt[k];
+    ochild[o]          = child ? child[k] : 0u;
+    ostart[o]          = starts[k];
+    oinst[o]           = i;
+  }
+}
+
+// first / one-past-last compacted index of each instance within a level
+__global__ void level_span_kernel(uint32_t const* __restrict__ oinst, size_t m, int level,
+                                  uint32_t* __restrict__ first, uint32_t* __restrict__ end)
+{
+  CSPT_GRID_STRIDE(k, m)
+  {
+    uint32_t const i = oinst[k];
+    if (k == 0 || oinst[k - 1] != i) first[i * kLevels + level] = static_cast<uint32_t>(k);
+    if (k + 1 == m || oinst[k + 1] != i) end[i * kLevels + level] = static_cast<uint32_t>(k + 1);
+  }
+}
+
+// Node bases of the instances and, per (instance, level), the shift from a
+// compacted level index to the output node index.
+__global__ void __launch_bounds__(1024)
+  layout_kernel(uint32_t const* __restrict__ first, uint32_t const* __restrict__ end,
+                uint32_t ni, Inst* __restrict__ inst, long long* __restrict__ out_shift,
+                uint64_t* __restrict__ node_offsets, int* __restrict__ error)
+{
+  uint32_t const per   = (ni + 1023u) / 1024u;
+  uint32_t const begin = threadIdx.x * per;
+  uint32_t const stop  = min(ni, begin + per);
+  uint64_t sum         = 0;
+  for (uint32_t i = begin; i < stop; ++i)
+    for (int l = 0; l < kLevels; ++l) sum += end[i * kLevels + l] - first[i * kLevels + l];
+  __shared__ uint64_t total;
+  uint64_t base = block_exclusive_scan<uint64_t, 1024>(sum, &total);
+  for (uint32_t i = begin; i < stop; ++i) {
+    uint64_t lb = 0;
+    for (int l = 0; l < kLevels; ++l) {
+      uint32_t const f = first[i * kLevels + l], e = end[i * kLevels + l];
+      out_shift[i * kLevels + l] =
+        static_cast<long long>(base + lb) - static_cast<long long>(f);
+      lb += e - f;
+    }
+    inst[i].node_base = static_cast<uint32_t>(base);
+    inst[i].nq        = static_cast<uint32_t>(lb);
+    inst[i].L0        = end[i * kLevels] - first[i * kLevels];
+    if (lb >= (uint64_t{1} << 28) || base + lb >= (uint64_t{1} << 32)) atomicExch(error, 1);
+    node_offsets[i] = base;
+    base += lb;
+  }
+  if (threadIdx.x == 0) node_offsets[ni] = total;
+}
+
+__global__ void assemble_kernel(uint32_t const* __restrict__ key, uint32_t const* __restrict__ cnt,
+                                uint32_t const* __restrict__ child,
+                                uint32_t const* __restrict__ start,
+                                uint32_t const* __restrict__ oinst, size_t m, int level,
+                                Inst const* __restrict__ inst,
+                                long long const* __restrict__ out_shift,
+                                uint32_t* __restrict__ okey, uint8_t* __restrict__ olevel,
+                                uint8_t* __restrict__ ointernal, uint32_t* __restrict__ olength,
+                                uint32_t* __restrict__ ooffset, uint32_t* __restrict__ ichild,
+                                uint32_t* __restrict__ node_inst)
+{
+  CSPT_GRID_STRIDE(k, m)
+  {
+    uint32_t const i    = oinst[k];
+    Inst const& I       = inst[i];
+    size_t const o      = static_cast<size_t>(out_shift[i * kLevels + level] + static_cast<long long>(k));
+    bool const internal = level + 2 <= static_cast<int>(I.d) && cnt[k] > I.max_size;
+    okey[o]             = key[k];
+    olevel[o]           = static_cast<uint8_t>(level);
+    ointernal[o]        = internal ? 1 : 0;
+    olength[o]          = internal ? child[k] : cnt[k];
+    ooffset[o]          = start[k] - I.pt_begin;
+    ichild[o]           = internal ? child[k] : 0u;
+    node_inst[o]        = i;
+  }
+}
+
+// detail/point_quadtree.cuh:82-109 per instance: internal offsets are the
+// instance's level-0 count plus the scan of child counts within the instance
+__global__ void offsets_kernel(uint8_t const* __restrict__ internal,
+                               uint32_t const* __restrict__ scanned,
+                               uint32_t const* __restrict__ node_inst,
+                               Inst const* __restrict__ inst, size_t q,
+                               uint32_t* __restrict__ offset, uint32_t* __restrict__ goff)
+{
+  CSPT_GRID_STRIDE(o, q)
+  {
+    Inst const& I = inst[node_inst[o]];
+    if (internal[o]) {
+      offset[o] = I.L0 + scanned[o] - scanned[I.node_base];
+      goff[o]   = 0u;
+    } else {
+      goff[o] = offset[o] + I.pt_begin;
+    }
+  }
+}
+
+__global__ void local_indices_kernel(uint32_t const* __restrict__ sidx,
+                                     uint64_t const* __restrict__ sk, int kb,
+                                     Inst const* __restrict__ inst, size_t n,
+                                     uint32_t* __restrict__ out)
+{
+  CSPT_GRID_STRIDE(i, n) { out[i] = sidx[i] - inst[sk[i] >> kb].pt_begin; }
+}
+
+__global__ void row_offsets_kernel(uint32_t const* __restrict__ pair_begin,
+                                   uint64_t const* __restrict__ pair_out, uint32_t ni,
+                                   uint64_t* __restrict__ row_offsets)
+{
+  CSPT_GRID_STRIDE(i, static_cast<size_t>(ni) + 1) { row_offsets[i] = pair_out[pair_begin[i]]; }
+}
+
+// rows -> instance-local point positions (and polygon indices when the
+// instances own polygon ranges)
+__global__ void localize_kernel(uint32_t* __restrict__ op, uint32_t* __restrict__ oq, size_t m,
+                                uint32_t const* __restrict__ pt_begin, uint32_t ni,
+                                Inst const* __restrict__ inst, bool local_polygons)
+{
+  CSPT_GRID_STRIDE(j, m)
+  {
+    uint32_t const pos = oq[j];
+    Inst const& I      = inst[find_instance(pt_begin, ni, pos)];
+    oq[j]              = pos - I.pt_begin;
+    if (local_polygons) op[j] = op[j] - I.poly_begin;
+  }
+}
+
+
+// the tree a box of instance `of(b)` walks
+template <typename InstanceOf>
+struct ForestTrees {
+  InstanceOf of;
+  Inst const* inst;
+  __device__ BoxTree<double> operator()(size_t b) const
+  {
+    Inst const& I = inst[of(b)];
+    return BoxTree<double>{I.node_base, I.nq,     I.L0,    I.pt_begin,
+                           I.minx,      I.miny,   I.scale, static_cast<int>(I.d)};
+  }
+};
+
+class Forest {
+ public:
+  explicit Forest(Allocator const& alloc) : alloc_(&alloc) {}
+
+  // Validates the parameters (the reference's join checks,
+  // quadtree_bbox_filtering.cu:100-106), applies the clamps of
+  // detail/point_quadtree.cuh:258-268 and uploads the instance table.
+  // poly_off (host, may be null) gives the instances' polygon ranges.
+  void setup(size_t ni, uint64_t const* h_pt_off, cspt_instance_params const* params,
+             uint64_t const* h_poly_off)
+  {
+    Allocator const& a   = *alloc_;
+    cudaStream_t const s = a.stream();
+    ni_                  = ni;
+    n_                   = h_pt_off[ni];
+    CSPT_EXPECTS(n_ < (size_t{1} << 32), "fewer than 2^32 points are supported");
+    std::vector<Inst> hi(ni);
+    std::vector<uint32_t> h_ptb(ni + 1), h_pob(ni + 1);
+    dmax_ = 1;
+    for (size_t i = 0; i < ni; ++i) {
+      cspt_instance_params const& p = params[i];
+      CSPT_EXPECTS(h_pt_off[i] <= h_pt_off[i + 1] &&
+                     (!h_poly_off || h_poly_off[i] <= h_poly_off[i + 1]),
+                   "instance offsets must be non-decreasing");
+      CSPT_EXPECTS(p.scale > 0, "scale must be positive");
+      CSPT_EXPECTS(p.x_min < p.x_max && p.y_min < p.y_max,
+                   "invalid bounding box (x_min, x_max, y_min, y_max)");
+      CSPT_EXPECTS(p.max_depth > 0 && p.max_depth < 16,
+                   "maximum depth must be positive and less than 16");
+      Inst& I           = hi[i];
+      I.minx            = p.x_min;
+      I.miny            = p.y_min;
+      I.maxx            = p.x_max;
+      I.maxy            = p.y_max;
+      I.d               = static_cast<uint32_t>(p.max_depth);
+      double const span = std::max(p.x_max - p.x_min, p.y_max - p.y_min);
+      double const ms   = span / static_cast<double>((1 << p.max_depth) + 2);
+      I.scale           = p.scale > ms ? p.scale : ms;
+      I.max_size        = static_cast<uint32_t>(p.max_size < 1 ? 1 : p.max_size);
+      I.pt_begin        = static_cast<uint32_t>(h_pt_off[i]);
+      I.pt_end          = static_cast<uint32_t>(h_pt_off[i + 1]);
+      I.poly_begin      = h_poly_off ? static_cast<uint32_t>(h_poly_off[i]) : 0u;
+      I.poly_end        = h_poly_off ? static_cast<uint32_t>(h_poly_off[i + 1]) : 0u;
+      I.node_base = I.nq = I.L0 = 0;
+      h_ptb[i]                  = I.pt_begin;
+      h_pob[i]                  = I.poly_begin;
+      dmax_                     = std::max(dmax_, p.max_depth);
+    }
+    h_ptb[ni] = static_cast<uint32_t>(n_);
+    h_pob[ni] = h_poly_off ? static_cast<uint32_t>(h_poly_off[ni]) : 0u;
+    inst_       = Buffer<Inst>(a, ni);
+    pt_begin_   = Buffer<uint32_t>(a, ni + 1);
+    poly_begin_ = Buffer<uint32_t>(a, ni + 1);
+    CSPT_CUDA_TRY(cudaMemcpyAsync(inst_.data(), hi.data(), ni * sizeof(Inst),
+                                  cudaMemcpyHostToDevice, s));
+    CSPT_CUDA_TRY(cudaMemcpyAsync(pt_begin_.data(), h_ptb.data(), (ni + 1) * 4,
+                                  cudaMemcpyHostToDevice, s));
+    CSPT_CUDA_TRY(cudaMemcpyAsync(poly_begin_.data(), h_pob.data(), (ni + 1) * 4,
+                                  cudaMemcpyHostToDevice, s));
+    // the host arrays above must outlive the copies
+    CSPT_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+
+  void build(double const* x, double const* y)
+  {
+    Allocator const& a   = *alloc_;
+    cudaStream_t const s = a.stream();
+    uint32_t const ni    = static_cast<uint32_t>(ni_);
+    size_t const n       = n_;
+    node_off_            = Buffer<uint64_t>(a, ni_ + 1);
+    if (n == 0) {
+      CSPT_CUDA_TRY(cudaMemsetAsync(node_off_.data(), 0, (ni_ + 1) * 8, s));
+      return;
+    }
+    KernelTimer timer("forest_build", s);
+    unsigned const grd   = grid_for(n, kBlk, kGridCap);
+    int const kb         = dmax_ >= 2 ? 2 * dmax_ + 2 : 2 * dmax_ + 4;
+    int ib               = 0;
+    while ((uint64_t{1} << ib) < ni_) ++ib;
+
+    Buffer<uint64_t> keys(a, n), keys_alt(a, n);
+    Buffer<uint32_t> idx(a, n), idx_alt(a, n);
+    keys_kernel<<<grd, kBlk, 0, s>>>(x, y, n, pt_begin_.data(), ni, inst_.data(), kb,
+                                     keys.data());
+    CSPT_CHECK_LAUNCH();
+    bool const alt = radix_sort_pairs<uint64_t>(keys.data(), idx.data(), keys_alt.data(),
+                                                idx_alt.data(), n, 0, kb + ib, true, a);
+    Buffer<uint64_t>& sk = alt ? keys_alt : keys;
+    sidx_                = std::move(alt ? idx_alt : idx);
+    (alt ? keys : keys_alt).reset();
+    (alt ? idx : idx_alt).reset();
+
+    Buffer<uint8_t> lvl(a, n), lim(a, n);
+    start_level_kernel<<<grd, kBlk, 0, s>>>(sk.data(), n, kb, inst_.data(), lvl.data(),
+                                            lim.data());
+    CSPT_CHECK_LAUNCH();
+    pidx_ = Buffer<uint32_t>(a, n);
+    local_indices_kernel<<<grd, kBlk, 0, s>>>(sidx_.data(), sk.data(), kb, inst_.data(), n,
+                                              pidx_.data());
+    CSPT_CHECK_LAUNCH();
+
+    struct Level {
+      Buffer<uint32_t> key, count, child, start, inst;
+      size_t size = 0;
+    };
+    std::vector<Level> levels(dmax_);
+    Buffer<uint32_t> first(a, ni_ * kLevels), end(a, ni_ * kLevels);
+    CSPT_CUDA_TRY(cudaMemsetAsync(first.data(), 0, ni_ * kLevels * 4, s));
+    CSPT_CUDA_TRY(cudaMemsetAsync(end.data(), 0, ni_ * kLevels * 4, s));
+    Buffer<uint32_t> total(a, 1);
+    Buffer<uint32_t> rank_prev(a, n + 1), rank_cur(a, n + 1);
+    Buffer<uint32_t> starts_prev, starts_cur, count_prev, count_cur, inst_prev, inst_cur;
+    Buffer<uint8_t> keep_prev, keep_cur;
+    size_t n_prev = 0;
+
+    auto emit = [&](int lv, Buffer<uint32_t>& starts, Buffer<uint32_t>& counts,
+                    Buffer<uint32_t>* childs, Buffer<uint32_t>& ninst, Buffer<uint8_t>* keep,
+                    size_t nl) {
+      Level& L          = levels[lv];
+      uint8_t const* kp = keep ? keep->data() : nullptr;
+      Buffer<uint32_t> pos(a, nl);
+      scan_apply<uint32_t>(KeepIn{kp}, PosOut{pos.data()}, nl, total.data(), a);
+      size_t const m = read_back(total.data(), s);
+      L.size         = m;
+      L.key          = Buffer<uint32_t>(a, m);
+      L.count        = Buffer<uint32_t>(a, m);
+      L.child        = Buffer<uint32_t>(a, m);
+      L.start        = Buffer<uint32_t>(a, m);
+      L.inst         = Buffer<uint32_t>(a, m);
+      if (nl) {
+        compact_level_kernel<<<grid_for(nl, kBlk, kGridCap), kBlk, 0, s>>>(
+          nl, kp, pos.data(), starts.data(), counts.data(), childs ? childs->data() : nullptr,
+          ninst.data(), sk.data(), kb, inst_.data(), lv, L.key.data(), L.count.data(),
+          L.child.data(), L.start.data(), L.inst.data());
+        CSPT_CHECK_LAUNCH();
+      }
+      if (m) {
+        level_span_kernel<<<grid_for(m, kBlk, kGridCap), kBlk, 0, s>>>(L.inst.data(), m, lv,
+                                                                       first.data(), end.data());
+        CSPT_CHECK_LAUNCH();
+      }
+    };
+
+    for (int l = 0; l < dmax_; ++l) {
+      starts_cur = Buffer<uint32_t>(a, n);
+      scan_apply<uint32_t>(StartFlag{lvl.data(), lim.data(), l},
+                           RankStore{rank_cur.data(), starts_cur.data()}, n,
+                           rank_cur.data() + n, a);
+      size_t const nl = read_back(rank_cur.data() + n, s);
+      count_cur       = Buffer<uint32_t>(a, nl);
+      inst_cur        = Buffer<uint32_t>(a, nl);
+      keep_cur        = Buffer<uint8_t>(a, nl);
+      unsigned const g = grid_for(nl, kBlk, kGridCap);
+      if (nl) {
+        count_kernel<<<g, kBlk, 0, s>>>(starts_cur.data(), nl, sk.data(), kb, inst_.data(),
+                                        count_cur.data(), inst_cur.data());
+        CSPT_CHECK_LAUNCH();
+      }
+      if (l == 0) {
+        if (nl) CSPT_CUDA_TRY(cudaMemsetAsync(keep_cur.data(), 1, nl, s));
+      } else {
+        if (nl) {
+          keep_kernel<<<g, kBlk, 0, s>>>(starts_cur.data(), nl, inst_cur.data(), lvl.data(),
+                                         l - 1, rank_prev.data(), count_prev.data(),
+                                         inst_.data(), keep_cur.data());
+          CSPT_CHECK_LAUNCH();
+        }
+        Buffer<uint32_t> child_prev(a, n_prev);
+        if (n_prev) {
+          child_count_kernel<<<grid_for(n_prev, kBlk, kGridCap), kBlk, 0, s>>>(
+            starts_prev.data(), n_prev, inst_prev.data(), inst_.data(), rank_cur.data(),
+            child_prev.data());
+          CSPT_CHECK_LAUNCH();
+        }
+        emit(l - 1, starts_prev, count_prev, &child_prev, inst_prev,
+             l - 1 == 0 ? nullptr : &keep_prev, n_prev);
+      }
+      std::swap(rank_prev, rank_cur);
+      starts_prev = std::move(starts_cur);
+      count_prev  = std::move(count_cur);
+      inst_prev   = std::move(inst_cur);
+      keep_prev   = std::move(keep_cur);
+      n_prev      = nl;
+    }
+    emit(dmax_ - 1, starts_prev, count_prev, nullptr, inst_prev, dmax_ - 1 == 0 ? nullptr : &keep_prev,
+         n_prev);
+    starts_prev.reset();
+    count_prev.reset();
+    inst_prev.reset();
+    keep_prev.reset();
+    rank_prev.reset();
+    rank_cur.reset();
+    lvl.reset();
+    lim.reset();
+    sk.reset();
+
+    Buffer<long long> shift(a, ni_ * kLevels);
+    Buffer<int> err(a, 1);
+    CSPT_CUDA_TRY(cudaMemsetAsync(err.data(), 0, sizeof(int), s));
+    layout_kernel<<<1, 1024, 0, s>>>(first.data(), end.data(), ni, inst_.data(), shift.data(),
+                                     node_off_.data(), err.data());
+    CSPT_CHECK_LAUNCH();
+    size_t q = 0;
+    for (auto& L : levels) q += L.size;
+    CSPT_EXPECTS(read_back(err.data(), s) == 0,
+                 "an instance's quadtree has too many nodes for the batched form");
+    q_        = q;
+    key_      = Buffer<uint32_t>(a, q);
+    length_   = Buffer<uint32_t>(a, q);
+    offset_   = Buffer<uint32_t>(a, q);
+    goff_     = Buffer<uint32_t>(a, q);
+    level_    = Buffer<uint8_t>(a, q);
+    internal_ = Buffer<uint8_t>(a, q);
+    if (q == 0) return;
+    Buffer<uint32_t> ichild(a, q), node_inst(a, q);
+    for (int l = 0; l < dmax_; ++l) {
+      Level& L = levels[l];
+      if (L.size) {
+        assemble_kernel<<<grid_for(L.size, kBlk, kGridCap), kBlk, 0, s>>>(
+          L.key.data(), L.count.data(), L.child.data(), L.start.data(), L.inst.data(), L.size,
+          l, inst_.data(), shift.data(), key_.data(), level_.data(), internal_.data(),
+          length_.data(), offset_.data(), ichild.data(), node_inst.data());
+        CSPT_CHECK_LAUNCH();
+      }
+      L = Level{};
+    }
+    exclusive_scan<uint32_t>(ichild.data(), ichild.data(), q, static_cast<uint32_t*>(nullptr), a);
+    offsets_kernel<<<grid_for(q, kBlk, kGridCap), kBlk, 0, s>>>(
+      internal_.data(), ichild.data(), node_inst.data(), inst_.data(), q, offset_.data(),
+      goff_.data());
+    CSPT_CHECK_LAUNCH();
+  }
+
+
+  TreeView view() const
+  {
+    return TreeView{key_.data(), level_.data(), internal_.data(), length_.data(), offset_.data(),
+                    q_};
+  }
+  cspt_quadtree tree() const
+  {
+    return cspt_quadtree{key_.data(), level_.data(), internal_.data(), length_.data(),
+                         offset_.data(), q_};
+  }
+
+  Allocator const* alloc_;
+  size_t ni_ = 0, n_ = 0, q_ = 0;
+  int dmax_  = 1;
+  Buffer<Inst> inst_;
+  Buffer<uint32_t> pt_begin_, poly_begin_;
+  Buffer<uint32_t> sidx_, pidx_;
+  Buffer<uint32_t> key_, length_, offset_, goff_;
+  Buffer<uint8_t> level_, internal_;
+  Buffer<uint64_t> node_off_;
+};
+
+}  // namespace
+}  // namespace cspt

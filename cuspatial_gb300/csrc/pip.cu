@@ -599,8 +599,8 @@ class PipExec::Impl {
                                   npairs, gstart_.data() + npairs, gpart_.data(), s);
   }
 
-  // launches the evaluation; outputs go to op/oq up to cap entries
-  void execute(cudaStream_t s, uint32_t* op, uint32_t* oq, uint64_t cap)
+  // the bitmask, counts and output offsets of all pairs
+  void evaluate(cudaStream_t s)
   {
     unsigned const blk = blk_;
     unsigned const grd = grid_for(np_ * 32, blk, 152u * 8u * 1024u / blk);
@@ -622,11 +622,24 @@ class PipExec::Impl {
     CSPT_CHECK_LAUNCH();
     scan_apply_prealloc<uint64_t>(CountsOf{counts_.data()}, Store64{out_off_.data()}, np_,
                                   out_off_.data() + np_, partials_.data(), s);
+  }
+
+  // writes the rows of the last evaluation to op/oq, up to cap entries
+  void expand(cudaStream_t s, uint32_t* op, uint32_t* oq, uint64_t cap)
+  {
+    unsigned const blk = blk_;
+    unsigned const grd = grid_for(np_ * 32, blk, 152u * 8u * 1024u / blk);
     pip_expand_kernel<<<grd, blk, 0, s>>>(pp_, pq_, np_, qlen_, qoff_, word_off_.data(),
                                           bits_.data(), out_off_.data(), op, oq, cap);
     CSPT_CHECK_LAUNCH();
     overflow_kernel<<<1, 1, 0, s>>>(out_off_.data() + np_, cap, flag_.data());
     CSPT_CHECK_LAUNCH();
+  }
+
+  void execute(cudaStream_t s, uint32_t* op, uint32_t* oq, uint64_t cap)
+  {
+    evaluate(s);
+    expand(s, op, oq, cap);
   }
 
   uint64_t const* total() const { return out_off_.data() + np_; }
@@ -664,6 +677,11 @@ PipExec::~PipExec() { delete impl_; }
 void PipExec::execute(cudaStream_t s, uint32_t* op, uint32_t* oq, uint64_t cap)
 {
   impl_->execute(s, op, oq, cap);
+}
+void PipExec::evaluate(cudaStream_t s) { impl_->evaluate(s); }
+void PipExec::expand(cudaStream_t s, uint32_t* op, uint32_t* oq, uint64_t cap)
+{
+  impl_->expand(s, op, oq, cap);
 }
 uint64_t const* PipExec::total() const { return impl_->total(); }
 uint64_t const* PipExec::pair_out_offsets() const { return impl_->pair_out_offsets(); }

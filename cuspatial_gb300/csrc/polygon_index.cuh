@@ -108,6 +108,8 @@ class PipExec {
   PipExec(PipExec const&)            = delete;
   PipExec& operator=(PipExec const&) = delete;
   void execute(cudaStream_t s, uint32_t* out_poly, uint32_t* out_point, uint64_t cap);
+  void evaluate(cudaStream_t s);  // bits, counts and output offsets
+  void expand(cudaStream_t s, uint32_t* out_poly, uint32_t* out_point, uint64_t cap);
   uint64_t const* total() const;             // device: number of output pairs
   uint64_t const* pair_out_offsets() const;  // device: first output of each pair
   int const* overflow() const;               // device: 1 when total > cap

@@ -16,6 +16,11 @@ machine.  All sizes can be scaled down (same distributions) for tests.
                        U[100, 10000] at a random origin; polygons per
                        instance log-uniform in [1, 2000], star-shaped with
                        4-256 vertices and radius 0.5%-5% of the box side.
+  serving_polygons     250,000 star polygons (8-256 vertices, radius U[1,30])
+                       centred on a jittered 500 x 500 grid over [0,20000)^2.
+  serving_requests     request point sets of log-uniform [1, 1e5] points,
+                       half uniform over the domain, half one Gaussian cluster
+                       (sigma U[5,500]).
   nearest_linestring   50,000,000 uniform points in [0,10000)^2, 200,000
                        random-walk linestrings (2-256 segments, step U[1,20],
                        heading change N(0, 0.3 rad)).
@@ -275,3 +280,43 @@ def batched_instances(n_instances=4096, points_range=(1e3, 1e6), polygons_range=
                           lambda g, pid: prad[pid] * g.uniform(0.5, 1.0, len(pid)))
     polygon_offsets = np.concatenate([[0], np.cumsum(npoly)]).astype(np.uint64)
     return BatchedWorkload(x, y, point_offsets, polys, polygon_offsets, boxes)
+
+
+def serving_polygons(grid=500, extent=20000.0, vertices_range=(8, 256), radius_range=(1.0, 30.0),
+                     seed_offset=0):
+    rng = np.random.Generator(np.random.PCG64(SEED + 3 + seed_offset))
+    step = extent / grid
+    gx, gy = np.meshgrid(np.arange(grid), np.arange(grid))
+    centers = np.stack([(gx.ravel() + rng.uniform(0.25, 0.75, grid * grid)) * step,
+                        (gy.ravel() + rng.uniform(0.25, 0.75, grid * grid)) * step], 1)
+    k = rng.integers(vertices_range[0], vertices_range[1] + 1, grid * grid)
+    prad = rng.uniform(radius_range[0], radius_range[1], grid * grid)
+    return star_polygons(rng, centers, k,
+                         lambda g, pid: prad[pid] * g.uniform(0.5, 1.0, len(pid)))
+
+
+@dataclass
+class Request:
+    x: np.ndarray
+    y: np.ndarray
+    kind: str
+
+
+def serving_requests(n_requests, points_range=(1, 100_000), extent=20000.0, seed_offset=0):
+    rng = np.random.Generator(np.random.PCG64(SEED + 13 + seed_offset))
+    sizes = _log_uniform_int(rng, points_range[0], points_range[1] + 1, n_requests)
+    hi = np.nextafter(extent, 0.0)
+    out = []
+    for i, n in enumerate(sizes):
+        if rng.random() < 0.5:
+            x = rng.uniform(0.0, extent, n)
+            y = rng.uniform(0.0, extent, n)
+            kind = "uniform"
+        else:
+            c = rng.uniform(0.0, extent, 2)
+            sig = rng.uniform(5.0, 500.0)
+            x = np.clip(c[0] + sig * rng.standard_normal(n), 0.0, hi)
+            y = np.clip(c[1] + sig * rng.standard_normal(n), 0.0, hi)
+            kind = "cluster"
+        out.append(Request(x, y, kind))
+    return out

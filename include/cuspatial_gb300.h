@@ -290,6 +290,89 @@ cspt_status cspt_batched_pip_refined_count(const cspt_batched_pip* plan, void* s
 /* Frees the plan; runs issued on it must have completed. */
 void cspt_batched_pip_free(cspt_batched_pip* plan);
 
+/* ------------------------------------------------------------------------
+ * Serving form (no counterpart in the reference): a device-resident polygon
+ * set answering point-in-polygon requests that arrive over time.
+ *
+ * A request is a host array of float64 points plus its quadtree parameters.
+ * Its answer is exactly what cspt_quadtree_on_points ->
+ * cspt_polygon_bounding_boxes (whole set) -> cspt_join_quadtree_and_bounding_boxes
+ * -> cspt_quadtree_point_in_polygon return for those points against the whole
+ * set: (polygon_index into the set, point_index = position in the request's
+ * point_indices) rows in the reference's order, plus point_indices.  The
+ * answer does not depend on which other requests share its batch.
+ *
+ * The server queues requests on submit; worker threads, one CUDA stream
+ * each, take batches of queued requests in arrival order as soon as a worker
+ * is free and the estimated device memory of all batches in flight stays
+ * within memory_budget_bytes.  Device memory of batches comes from a byte
+ * budget of that size; a batch that runs out is split and its requests are
+ * retried one at a time.  A request that cannot fit even alone fails with
+ * CSPT_OUT_OF_MEMORY; other requests are unaffected.
+ * ------------------------------------------------------------------------ */
+typedef struct cspt_polygon_set cspt_polygon_set;
+typedef struct cspt_server cspt_server;
+
+/* Copies the polygon column (device, float64; every polygon must have a
+ * vertex) into a resident set with its boxes, cell grid and point-in-polygon
+ * index.  Memory comes from mr on `stream`, which must stay valid until the
+ * set is freed; synchronises `stream`. */
+cspt_status cspt_polygon_set_create(const uint32_t* poly_offsets, size_t num_poly_offsets,
+                                    const uint32_t* ring_offsets, size_t num_ring_offsets,
+                                    const void* poly_x, const void* poly_y,
+                                    size_t num_poly_vertices, cspt_dtype dtype,
+                                    const cspt_allocator* mr, void* stream,
+                                    cspt_polygon_set** out);
+/* Frees the set; servers using it must be freed first. */
+void cspt_polygon_set_free(cspt_polygon_set* set);
+
+typedef struct cspt_server_options {
+  size_t memory_budget_bytes; /* device memory all batches in flight may hold */
+  int num_streams;            /* worker threads, one CUDA stream each */
+  size_t max_batch_points;    /* points per batch (a larger request runs alone) */
+  size_t max_batch_requests;  /* requests per batch */
+  cspt_method method;
+  int block_threads;          /* per-pair kernel block size: multiple of 32, <= 256 */
+} cspt_server_options;
+
+typedef struct cspt_server_stats {
+  uint64_t submitted, completed, failed, batches, split_batches, queued;
+  size_t reserved_bytes, peak_device_bytes, memory_budget_bytes;
+  uint64_t max_batch_requests_seen;
+} cspt_server_stats;
+
+typedef struct cspt_request_result {
+  int status;        /* cspt_status of the request */
+  const char* error; /* message when status != CSPT_OK */
+  const uint32_t* polygon_index;
+  const uint32_t* point_index;
+  size_t num_rows;
+  const uint32_t* point_indices;
+  size_t num_points;
+  double submit_s, admit_s, done_s; /* server clock (cspt_server_now) */
+  uint64_t batch;
+  uint32_t batch_requests;
+} cspt_request_result;
+
+cspt_status cspt_server_create(const cspt_polygon_set* set, const cspt_server_options* options,
+                               cspt_server** out);
+/* Queues a request.  x and y (host) must stay valid until the request
+ * completes; parameters are validated here (same messages as the join). */
+cspt_status cspt_server_submit(cspt_server* server, uint64_t request_id, const double* x,
+                               const double* y, size_t num_points,
+                               const cspt_instance_params* params);
+/* Ids of requests completed since the last poll (waits up to timeout_s for
+ * the first). */
+size_t cspt_server_poll(cspt_server* server, uint64_t* ids, size_t max_ids, double timeout_s);
+/* Result of a completed request; pointers stay valid until release. */
+cspt_status cspt_server_result(cspt_server* server, uint64_t request_id,
+                               cspt_request_result* out);
+void cspt_server_release(cspt_server* server, uint64_t request_id);
+double cspt_server_now(const cspt_server* server);
+cspt_status cspt_server_get_stats(cspt_server* server, cspt_server_stats* out);
+/* Finishes the queued requests, then stops the workers. */
+void cspt_server_free(cspt_server* server);
+
 #ifdef __cplusplus
 }
 #endif
