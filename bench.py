@@ -700,6 +700,9 @@ def run_serving(args, dist):
     dist.init("nccl")
     lib = _lib.load()
     lib.cspt_launch_count.restype = ctypes.c_uint64
+    lib.cspt_profile_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(ctypes.c_uint64)]
+    lib.cspt_profile_enable.argtypes = [ctypes.c_int]
     t0 = time.time()
     P = datasets.serving_polygons()
     reqs = datasets.serving_requests(args.requests)
@@ -725,11 +728,18 @@ def run_serving(args, dist):
             l0 = lib.cspt_launch_count()
             live = run_poisson(srv, reqs, rate=args.rate, params=params, seed=2)
             l1 = lib.cspt_launch_count()
+            lib.cspt_profile_enable(1)
             sat = run_poisson(srv, reqs, rate=0, params=params, seed=3)
+            stages = {}
+            for name in ("forest_build", "serving_join", "serving_sort", "serving_pip"):
+                ms_, cnt_ = ctypes.c_double(), ctypes.c_uint64()
+                lib.cspt_profile_read(name.encode(), ctypes.byref(ms_), ctypes.byref(cnt_))
+                stages[name] = {"ms": ms_.value, "launches": int(cnt_.value)}
+            lib.cspt_profile_enable(0)
             clock_info = clocks.stop()
             st = srv.stats()
         out[method] = {"live": live, "saturated": sat, "stats": st, "clocks": clock_info,
-                       "launches_live": int(l1 - l0)}
+                       "launches_live": int(l1 - l0), "stages_saturated": stages}
     f = out[args.method]
     value = f["saturated"]["points_per_s"] * args.gpus
     line = {
@@ -751,6 +761,7 @@ def run_serving(args, dist):
                            "p50/p99: latency at the offered Poisson rate)"},
         "polygon_set_ms": set_ms,
         "live": f["live"], "saturated": f["saturated"], "server_stats": f["stats"],
+        "stages_saturated_ms": f["stages_saturated"],
         "plain_fp64": ({"live": out["exact"]["live"], "saturated": out["exact"]["saturated"]}
                        if "exact" in out and args.method != "exact" else None),
         "gpu_launches": f["launches_live"], "clocks": f["clocks"], "generation_s": gen_s,

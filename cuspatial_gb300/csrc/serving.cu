@@ -415,6 +415,7 @@ class ServingBatch {
                                                  node.data());
       CSPT_CHECK_LAUNCH();
       int const bits = 32 + pbits;
+      KernelTimer timer("serving_sort", s);
       bool const alt = radix_sort_pairs<uint64_t>(key.data(), perm.data(), key_alt.data(),
                                                   perm_alt.data(), k_, 0, bits, true, a);
       pair_poly_ = Buffer<uint32_t>(a, k_);
