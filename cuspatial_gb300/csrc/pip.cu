@@ -152,6 +152,32 @@ __device__ bool pip_exact(T px, T py, PolygonIndexView<T> const& ix, uint32_t po
 }
 
 constexpr int kUndecided = 2;
+constexpr int kPipBlock = 256;
+// resident blocks per SM the registers are sized for (filtered / exact)
+#ifndef CSPT_PIP_MIN_BLOCKS
+#define CSPT_PIP_MIN_BLOCKS 6
+#endif
+#ifndef CSPT_PIP_MIN_BLOCKS_EXACT
+#define CSPT_PIP_MIN_BLOCKS_EXACT 8
+#endif
+constexpr int kPipMinBlocksFiltered = CSPT_PIP_MIN_BLOCKS;
+constexpr int kPipMinBlocksExact    = CSPT_PIP_MIN_BLOCKS_EXACT;
+
+// resident blocks of a pair kernel: the persistent grid
+template <typename K>
+unsigned pair_grid(K kernel, unsigned block, size_t npairs)
+{
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, static_cast<int>(block), 0) !=
+        cudaSuccess ||
+      per_sm < 1) {
+    (void)cudaGetLastError();
+    per_sm = 1;
+  }
+  size_t const want = (npairs * 32 + block - 1) / block;
+  size_t const cap  = static_cast<size_t>(num_sms()) * static_cast<size_t>(per_sm);
+  return static_cast<unsigned>(want < 1 ? 1 : (want < cap ? want : cap));
+}
 // float32 filter, in the leaf's frame (used by pip_group_kernel below).
 //
 // Maps: a point goes through f_l(v) = fl32(fl32(v - A_l) - d) with d the
@@ -178,8 +204,13 @@ constexpr int kUndecided = 2;
 // One warp per (polygon, quadrant) pair, lanes over the quadrant's points.
 // Filtered: float32 test in the leaf frame (bounds above), undecided points
 // re-evaluated with pip_exact.  Exact: pip_exact on float64 coordinates.
+//
+// Pairs are handed out dynamically: each warp takes the next pair index from
+// a device counter (zeroed before the launch), so warps that drew cheap pairs
+// keep working while others finish long ones; the grid holds only as many
+// blocks as are resident.
 template <bool Filtered>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : kPipMinBlocksExact)
   pip_pair_kernel(uint32_t const* __restrict__ pair_poly, uint32_t const* __restrict__ pair_quad,
                   uint32_t const* __restrict__ pair_group, size_t npairs,
                   uint32_t const* __restrict__ qlen, uint32_t const* __restrict__ qoff,
@@ -188,15 +219,18 @@ __global__ void __launch_bounds__(256)
                   float2 const* __restrict__ u, LeafFrame const* __restrict__ frames,
                   PolygonIndexView<double> ix, uint64_t const* __restrict__ word_off,
                   uint32_t* __restrict__ bits, uint32_t* __restrict__ counts,
-                  unsigned long long* __restrict__ refined)
+                  unsigned long long* __restrict__ refined,
+                  unsigned long long* __restrict__ next_pair)
 {
   int const lane      = threadIdx.x & 31;
-  size_t const nwarps = (static_cast<size_t>(gridDim.x) * blockDim.x) >> 5;
   float const gf      = Filtered ? static_cast<float>(*ix.grid) : 0.0f;
   bool const gok      = gf >= 1.17549435e-38f && gf < 1.0e30f;  // normal float grid step
   uint32_t nref       = 0;
-  for (size_t k = (blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5; k < npairs;
-       k += nwarps) {
+  for (;;) {
+    unsigned long long kk = 0;
+    if (lane == 0) kk = atomicAdd(next_pair, 1ull);
+    size_t const k = static_cast<size_t>(__shfl_sync(0xFFFFFFFFu, kk, 0));
+    if (k >= npairs) break;
     uint32_t const poly = pair_poly[k];
     uint32_t const quad = pair_quad[k];
     uint32_t const len  = qlen[quad];
@@ -448,8 +482,8 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
   size_t const nwords = read_back(wo + npairs, s);
   Buffer<uint32_t> bits(alloc, nwords);
   Buffer<uint32_t> counts(alloc, npairs);
-  Buffer<unsigned long long> refined(alloc, 1);
-  CSPT_CUDA_TRY(cudaMemsetAsync(refined.data(), 0, sizeof(unsigned long long), s));
+  Buffer<unsigned long long> refined(alloc, 2);  // [0] refined candidates, [1] next pair
+  CSPT_CUDA_TRY(cudaMemsetAsync(refined.data(), 0, 2 * sizeof(unsigned long long), s));
   unsigned const blk = 256;
   unsigned const grd = grid_for(npairs * 32, blk, 152u * 8u * 4u);
   if constexpr (std::is_same<T, double>::value) {
@@ -481,15 +515,17 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
     }
     KernelTimer timer("pip_bits", s);
     if (filtered)
-      pip_pair_kernel<true><<<grd, blk, 0, s>>>(pair_poly, pair_quad, pgroup.data(), npairs, qlen,
-                                                qoff, point_indices, npi, x, y, u.data(),
-                                                frames.data(), index.view(), word_off.data(),
-                                                bits.data(), counts.data(), refined.data());
+      pip_pair_kernel<true>
+        <<<pair_grid(pip_pair_kernel<true>, kPipBlock, npairs), kPipBlock, 0, s>>>(
+          pair_poly, pair_quad, pgroup.data(), npairs, qlen, qoff, point_indices, npi, x, y,
+          u.data(), frames.data(), index.view(), word_off.data(), bits.data(), counts.data(),
+          refined.data(), refined.data() + 1);
     else
-      pip_pair_kernel<false><<<grd, blk, 0, s>>>(pair_poly, pair_quad, nullptr, npairs, qlen,
-                                                 qoff, point_indices, npi, x, y, nullptr, nullptr,
-                                                 index.view(), word_off.data(), bits.data(),
-                                                 counts.data(), nullptr);
+      pip_pair_kernel<false>
+        <<<pair_grid(pip_pair_kernel<false>, kPipBlock, npairs), kPipBlock, 0, s>>>(
+          pair_poly, pair_quad, nullptr, npairs, qlen, qoff, point_indices, npi, x, y, nullptr,
+          nullptr, index.view(), word_off.data(), bits.data(), counts.data(), nullptr,
+          refined.data() + 1);
     CSPT_CHECK_LAUNCH();
   } else {
     KernelTimer timer("pip_bits", s);
@@ -589,8 +625,10 @@ class PipExec::Impl {
     pgroup_   = Buffer<uint32_t>(alloc, npairs);
     frames_   = Buffer<LeafFrame>(alloc, npairs);
     u_        = Buffer<float2>(alloc, filtered ? npi : 0);
-    refined_  = Buffer<unsigned long long>(alloc, 1);
+    refined_  = Buffer<unsigned long long>(alloc, 2);  // [0] refined, [1] next pair
     flag_     = Buffer<int>(alloc, 1);
+    grid_true_  = pair_grid(pip_pair_kernel<true>, blk_, npairs);
+    grid_false_ = pair_grid(pip_pair_kernel<false>, blk_, npairs);
     scan_apply_prealloc<uint64_t>(WordsOf{pair_quad, qlen}, Store64{word_off_.data()}, npairs,
                                   word_off_.data() + npairs, partials_.data(), s);
     nwords_ = read_back(word_off_.data() + npairs, s);
@@ -604,20 +642,20 @@ class PipExec::Impl {
   {
     unsigned const blk = blk_;
     unsigned const grd = grid_for(np_ * 32, blk, 152u * 8u * 1024u / blk);
-    CSPT_CUDA_TRY(cudaMemsetAsync(refined_.data(), 0, sizeof(unsigned long long), s));
+    CSPT_CUDA_TRY(cudaMemsetAsync(refined_.data(), 0, 2 * sizeof(unsigned long long), s));
     if (filtered_) {
       leaf_frame_kernel<<<grd, blk, 0, s>>>(gstart_.data(), gstart_.data() + np_, pq_, qlen_,
                                             qoff_, pi_, npi_, x_, y_, ix_.grid, u_.data(),
                                             frames_.data());
       CSPT_CHECK_LAUNCH();
-      pip_pair_kernel<true><<<grd, blk, 0, s>>>(pp_, pq_, pgroup_.data(), np_, qlen_, qoff_, pi_,
-                                                npi_, x_, y_, u_.data(), frames_.data(), ix_,
-                                                word_off_.data(), bits_.data(), counts_.data(),
-                                                refined_.data());
+      pip_pair_kernel<true><<<grid_true_, blk, 0, s>>>(
+        pp_, pq_, pgroup_.data(), np_, qlen_, qoff_, pi_, npi_, x_, y_, u_.data(),
+        frames_.data(), ix_, word_off_.data(), bits_.data(), counts_.data(), refined_.data(),
+        refined_.data() + 1);
     } else {
-      pip_pair_kernel<false><<<grd, blk, 0, s>>>(pp_, pq_, nullptr, np_, qlen_, qoff_, pi_, npi_,
-                                                 x_, y_, nullptr, nullptr, ix_, word_off_.data(),
-                                                 bits_.data(), counts_.data(), nullptr);
+      pip_pair_kernel<false><<<grid_false_, blk, 0, s>>>(
+        pp_, pq_, nullptr, np_, qlen_, qoff_, pi_, npi_, x_, y_, nullptr, nullptr, ix_,
+        word_off_.data(), bits_.data(), counts_.data(), nullptr, refined_.data() + 1);
     }
     CSPT_CHECK_LAUNCH();
     scan_apply_prealloc<uint64_t>(CountsOf{counts_.data()}, Store64{out_off_.data()}, np_,
@@ -656,6 +694,7 @@ class PipExec::Impl {
   PolygonIndexView<double> ix_;
   bool filtered_;
   unsigned blk_;
+  unsigned grid_true_ = 1, grid_false_ = 1;
   size_t nwords_ = 0;
   Buffer<uint64_t> word_off_, out_off_, partials_;
   Buffer<uint32_t> gpart_, counts_, gstart_, pgroup_, bits_;

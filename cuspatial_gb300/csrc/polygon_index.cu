@@ -18,11 +18,21 @@ constexpr int kMaxSlabs = 4096;
 
 // About two index entries per edge: with S slabs an edge of height h appears
 // in about h*S/H + 1 slabs, so S ~ V*H / sum(h), between 1 and min(V/2, 4096).
-__device__ inline uint32_t choose_slabs(uint32_t nv, double height, double sum_rise)
+// Slab count: with s = density * V * height / sum|rise| slabs, a slab lists
+// about (1 + 1/density) * sum|rise| / height edges (the edges crossing it plus
+// those ending inside it) and the index holds (1 + density) entries per edge.
+// Denser slabs shorten every candidate's edge walk at the cost of index
+// memory and build time; measured on the 100k-polygon, 8-512-vertex star
+// set, density 4 minimises build + float32 evaluation and density 8 the
+// float64-only evaluation.
+constexpr double kSlabDensityFloat32 = 4.0;
+constexpr double kSlabDensityFloat64 = 8.0;
+__device__ inline uint32_t choose_slabs(uint32_t nv, double height, double sum_rise,
+                                        double density)
 {
   if (nv < 8 || !(height > 0.0) || !(sum_rise > 0.0)) return 1;
-  double s         = static_cast<double>(nv) * height / sum_rise;
-  double const cap = fmin(static_cast<double>(nv) * 0.5, static_cast<double>(kMaxSlabs));
+  double s         = density * static_cast<double>(nv) * height / sum_rise;
+  double const cap = fmin(static_cast<double>(nv) * 0.5 * density, static_cast<double>(kMaxSlabs));
   if (!(s <= cap)) s = cap;
   if (s < 1.0) s = 1.0;
   return static_cast<uint32_t>(s);
@@ -153,7 +163,7 @@ __global__ void __launch_bounds__(kIdxBlock)
                      T const* __restrict__ vx, T const* __restrict__ vy, size_t np, T* pminx,
                      T* pminy, T* pmaxx, T* pmaxy, T* invh, uint32_t* nslab, uint32_t* nentries,
                      uint32_t* nvert, uint8_t* exact, uint32_t* __restrict__ prev_out,
-                     uint32_t* __restrict__ spans)
+                     uint32_t* __restrict__ spans, double density)
 {
   __shared__ uint32_t cnt[kMaxSlabs];
   __shared__ T shT[kIdxBlock / 32];
@@ -180,8 +190,8 @@ __global__ void __launch_bounds__(kIdxBlock)
     mxx      = block_max(mxx, shT);
     mxy      = block_max(mxy, shT);
     sum_rise = block_sum(sum_rise, shD);
-    uint32_t const ns =
-      choose_slabs(ve - vb, static_cast<double>(mxy) - static_cast<double>(mny), sum_rise);
+    uint32_t const ns = choose_slabs(
+      ve - vb, static_cast<double>(mxy) - static_cast<double>(mny), sum_rise, density);
     T const h  = mxy - mny;
     T const ih = (ns > 1 && h > T{0}) ? static_cast<T>(ns) / h : T{0};
     for (uint32_t j = threadIdx.x; j < ns; j += kIdxBlock) cnt[j] = 0;
@@ -359,6 +369,28 @@ __global__ void copy_totals_kernel(uint32_t const* a, uint32_t const* b, uint32_
   out[2] = *c;
 }
 
+// 64-bit sums of the per-polygon slab and entry counts: the 32-bit scans
+// above are only valid below 2^32
+__global__ void wide_totals_kernel(uint32_t const* __restrict__ nslab,
+                                   uint32_t const* __restrict__ nent, size_t np,
+                                   unsigned long long* out)
+{
+  unsigned long long a = 0, b = 0;
+  for (size_t p = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; p < np;
+       p += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    a += nslab[p];
+    b += nent[p];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xFFFFFFFFu, a, o);
+    b += __shfl_xor_sync(0xFFFFFFFFu, b, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(out, a);
+    atomicAdd(out + 1, b);
+  }
+}
+
 __global__ void vert_end_kernel(uint32_t const* __restrict__ vbeg,
                                 uint32_t const* __restrict__ nvert, size_t np,
                                 uint32_t* __restrict__ vend)
@@ -408,7 +440,7 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
     index_count_kernel<T><<<grd, kIdxBlock, 0, s>>>(
       po, ro, vx, vy, np, pminx_.data(), pminy_.data(), pmaxx_.data(), pmaxy_.data(),
       invh_.data(), nslab_.data(), nent.data(), nvert.data(), exact_.data(), prev_.data(),
-      spans.data());
+      spans.data(), build_float32 ? kSlabDensityFloat32 : kSlabDensityFloat64);
     CSPT_CHECK_LAUNCH();
   }
   grid_kernel<T><<<1, 1024, 0, s>>>(pminx_.data(), pminy_.data(), pmaxx_.data(), pmaxy_.data(),
@@ -420,9 +452,20 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
   copy_totals_kernel<<<1, 1, 0, s>>>(slab_base_.data() + np, ebase.data() + np,
                                      vbeg_.data() + np, totals.data());
   CSPT_CHECK_LAUNCH();
+  Buffer<unsigned long long> wide(alloc, 2);
+  CSPT_CUDA_TRY(cudaMemsetAsync(wide.data(), 0, 2 * sizeof(unsigned long long), s));
+  if (np > 0) {
+    wide_totals_kernel<<<grid_for(np, 256, 152u * 4u), 256, 0, s>>>(nslab_.data(), nent.data(),
+                                                                     np, wide.data());
+    CSPT_CHECK_LAUNCH();
+  }
   uint32_t tot[3];
+  unsigned long long wtot[2];
   CSPT_CUDA_TRY(cudaMemcpyAsync(tot, totals.data(), sizeof(tot), cudaMemcpyDeviceToHost, s));
+  CSPT_CUDA_TRY(cudaMemcpyAsync(wtot, wide.data(), sizeof(wtot), cudaMemcpyDeviceToHost, s));
   CSPT_CUDA_TRY(cudaStreamSynchronize(s));
+  CSPT_EXPECTS(wtot[0] < (1ull << 32) && wtot[1] < (1ull << 32),
+               "polygon set too large for the slab index (2^32 slab entries)");
   size_t const nslabs_total = tot[0], nentries = tot[1], nvertical = tot[2];
   slab_start_ = Buffer<uint32_t>(alloc, nslabs_total + 1);
   slab_edges_ = Buffer<uint32_t>(alloc, nentries);
