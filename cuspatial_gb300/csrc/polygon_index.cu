@@ -131,76 +131,192 @@ constexpr uint32_t kSpanSkip = 1u << 24, kSpanVertical = 1u << 25, kSpanTiny = 1
 __device__ inline uint32_t span_j0(uint32_t s) { return s & 0xFFFu; }
 __device__ inline uint32_t span_j1(uint32_t s) { return (s >> 12) & 0xFFFu; }
 
-// The slab coordinate (y - ymin) * inv_h is taken in float64 once per end
-// point and rounded to float32 (2.5e-4 slab at most for 4096 slabs); the
-// range is widened by 2^-36 of the edge height (on-edge band, see the header)
-// plus 1/32 slab, which covers that rounding and the float32 slab lookup of
-// the filter (below 1e-3 slab), so j0..j1 contains the float64 and float32
-// slab of every point the edge can matter to.
+// The slab coordinate (y - ymin) * inv_h is taken in float64 once per
+// vertex and rounded to float32 (2.5e-4 slab at most for 4096 slabs); an
+// edge's range is widened by 2^-36 of its height (on-edge band, see the
+// header) plus 1/32 slab, which covers that rounding and the float32 slab
+// lookup of the filter (below 1e-3 slab), so j0..j1 contains the float64 and
+// float32 slab of every point the edge can matter to.
+//
+// Degenerate and vertical edges are found on the bit patterns: for finite
+// coordinates the reference's float_equal(b - a, 0) holds exactly when
+// a == b, except where both coordinates lie below 2^-1019, where distinct
+// neighbours can be within 4 ULP of each other; such edges are flagged
+// (kSpanTiny) and their polygon is walked with the reference loop.
 template <typename T>
-__device__ inline uint32_t edge_span(T const* vx, T const* vy, uint32_t v, uint32_t pv, T ymin,
-                                     T ih, uint32_t ns)
+__device__ inline bool same_value(T a, T b)
 {
-  T const ax = vx[v], ay = vy[v], bx = vx[pv], by = vy[pv];
-  T const run = bx - ax, rise = by - ay;
-  bool const skip = float_equal(run, T{0}) && float_equal(rise, T{0});
-  if (skip) return kSpanSkip | ((run != T{0} || rise != T{0}) ? kSpanTiny : 0u);
-  float const fa = static_cast<float>((ay - ymin) * ih);
-  float const fb = static_cast<float>((by - ymin) * ih);
+  return a == b;
+}
+template <>
+__device__ inline bool same_value<double>(double a, double b)
+{
+  unsigned long long const x = __double_as_longlong(a), y = __double_as_longlong(b);
+  return x == y || ((x | y) << 1) == 0ull;  // equal bits, or +0 and -0
+}
+// exponent field <= 3: |a| < 2^-1019 (double), 2^-123 (float)
+__device__ inline bool below_tiny(float a) { return ((__float_as_uint(a) >> 23) & 0xFFu) <= 3u; }
+__device__ inline bool below_tiny(double a)
+{
+  return ((static_cast<unsigned long long>(__double_as_longlong(a)) >> 52) & 0x7FFull) <= 3ull;
+}
+
+template <typename T>
+__device__ inline uint32_t edge_span(T ax, T ay, T bx, T by, float fa, float fb, uint32_t ns)
+{
+  bool const ex = same_value(ax, bx), ey = same_value(ay, by);
+  bool const nx = ex || (below_tiny(ax) && below_tiny(bx));
+  bool const ny = ey || (below_tiny(ay) && below_tiny(by));
+  if (ex && ey) return kSpanSkip;
+  if (nx && ny) return kSpanSkip | kSpanTiny;
   float const lo = fminf(fa, fb), hi = fmaxf(fa, fb);
   float const mg = (hi - lo) * 1.4551915228366852e-11f + 0.03125f;
   float const l  = lo - mg, h = hi + mg;
   float const top = static_cast<float>(ns);
   uint32_t const j0 = !(l > 0.0f) ? 0u : (l >= top ? ns - 1 : min(static_cast<uint32_t>(l), ns - 1));
   uint32_t const j1 = !(h > 0.0f) ? 0u : (h >= top ? ns - 1 : min(static_cast<uint32_t>(h), ns - 1));
-  return j0 | (j1 << 12) | (run == T{0} ? kSpanVertical : 0u);
+  return j0 | (j1 << 12) | (ex ? kSpanVertical : 0u);
+}
+
+// Order-preserving integer image of a non-NaN double (min/max on the
+// integer pipe; float64 comparisons run at a small fraction of that rate).
+__device__ inline long long order_key(double v)
+{
+  long long const b = __double_as_longlong(v);
+  return b >= 0 ? b : (b ^ 0x7FFFFFFFFFFFFFFFLL);
+}
+__device__ inline double from_order_key(long long k)
+{
+  return __longlong_as_double(k >= 0 ? k : (k ^ 0x7FFFFFFFFFFFFFFFLL));
+}
+__device__ inline bool is_nan_bits(double v)
+{
+  unsigned long long const b = static_cast<unsigned long long>(__double_as_longlong(v));
+  return (b & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull;
+}
+__device__ inline bool is_finite_bits(double v)
+{
+  unsigned long long const b = static_cast<unsigned long long>(__double_as_longlong(v));
+  return (b & 0x7FF0000000000000ull) != 0x7FF0000000000000ull;
+}
+
+__device__ inline long long block_min_ll(long long v, long long* sh)
+{
+  for (int o = 16; o > 0; o >>= 1) {
+    long long const t = __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    v                 = t < v ? t : v;
+  }
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  long long r = sh[0];
+  for (int w = 1; w < kIdxBlock / 32; ++w) r = sh[w] < r ? sh[w] : r;
+  __syncthreads();
+  return r;
+}
+__device__ inline long long block_max_ll(long long v, long long* sh)
+{
+  for (int o = 16; o > 0; o >>= 1) {
+    long long const t = __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    v                 = t > v ? t : v;
+  }
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  long long r = sh[0];
+  for (int w = 1; w < kIdxBlock / 32; ++w) r = sh[w] > r ? sh[w] : r;
+  __syncthreads();
+  return r;
 }
 
 // Pass 1: per polygon box, slab count, entries, vertical edges, flags.
+// Per-polygon quantities are computed once (thread 0) and shared; each
+// vertex's slab coordinate is computed once (yslab) and read by both edges
+// that end at it.
 template <typename T>
 __global__ void __launch_bounds__(kIdxBlock)
   index_count_kernel(uint32_t const* __restrict__ po, uint32_t const* __restrict__ ro,
                      T const* __restrict__ vx, T const* __restrict__ vy, size_t np, T* pminx,
                      T* pminy, T* pmaxx, T* pmaxy, T* invh, uint32_t* nslab, uint32_t* nentries,
                      uint32_t* nvert, uint8_t* exact, uint32_t* __restrict__ prev_out,
-                     uint32_t* __restrict__ spans, double density)
+                     uint32_t* __restrict__ spans, float* __restrict__ yslab, double density)
 {
   __shared__ uint32_t cnt[kMaxSlabs];
   __shared__ T shT[kIdxBlock / 32];
+  __shared__ long long shL[kIdxBlock / 32];
   __shared__ double shD[kIdxBlock / 32];
   __shared__ uint32_t shU[kIdxBlock / 32];
+  __shared__ T s_ymin, s_ih;
+  __shared__ uint32_t s_ns;
   for (size_t p = blockIdx.x; p < np; p += gridDim.x) {
     uint32_t const r0 = po[p], r1 = po[p + 1];
     uint32_t const vb = ro[r0], ve = ro[r1];
-    T mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
+    T mnx, mny, mxx, mxy;
     double sum_rise = 0.0;
     uint32_t bad    = 0;
-    for (uint32_t v = vb + threadIdx.x; v < ve; v += kIdxBlock) {
-      T const x = vx[v], y = vy[v];
-      mnx       = fmin(mnx, x);
-      mny       = fmin(mny, y);
-      mxx       = fmax(mxx, x);
-      mxy       = fmax(mxy, y);
-      bad |= (isfinite(x) && isfinite(y)) ? 0u : 1u;
-      uint32_t const pv = prev_in_ring(ro, r0, r1, v);
-      sum_rise += fabs(static_cast<double>(vy[pv]) - static_cast<double>(y));
+    if constexpr (std::is_same<T, double>::value) {
+      long long kx0 = order_key(INFINITY), ky0 = order_key(INFINITY);
+      long long kx1 = order_key(-INFINITY), ky1 = order_key(-INFINITY);
+      for (uint32_t v = vb + threadIdx.x; v < ve; v += kIdxBlock) {
+        double const x = vx[v], y = vy[v];
+        bad |= (is_finite_bits(x) && is_finite_bits(y)) ? 0u : 1u;
+        if (!is_nan_bits(x)) {
+          long long const k = order_key(x);
+          kx0               = k < kx0 ? k : kx0;
+          kx1               = k > kx1 ? k : kx1;
+        }
+        if (!is_nan_bits(y)) {
+          long long const k = order_key(y);
+          ky0               = k < ky0 ? k : ky0;
+          ky1               = k > ky1 ? k : ky1;
+        }
+        uint32_t const pv = prev_in_ring(ro, r0, r1, v);
+        prev_out[v]       = pv;
+        sum_rise += fabs(vy[pv] - y);
+      }
+      mnx = from_order_key(block_min_ll(kx0, shL));
+      mny = from_order_key(block_min_ll(ky0, shL));
+      mxx = from_order_key(block_max_ll(kx1, shL));
+      mxy = from_order_key(block_max_ll(ky1, shL));
+    } else {
+      mnx = INFINITY;
+      mny = INFINITY;
+      mxx = -INFINITY;
+      mxy = -INFINITY;
+      for (uint32_t v = vb + threadIdx.x; v < ve; v += kIdxBlock) {
+        T const x = vx[v], y = vy[v];
+        mnx       = fmin(mnx, x);
+        mny       = fmin(mny, y);
+        mxx       = fmax(mxx, x);
+        mxy       = fmax(mxy, y);
+        bad |= (isfinite(x) && isfinite(y)) ? 0u : 1u;
+        uint32_t const pv = prev_in_ring(ro, r0, r1, v);
+        prev_out[v]       = pv;
+        sum_rise += fabs(static_cast<double>(vy[pv]) - static_cast<double>(y));
+      }
+      mnx = block_min(mnx, shT);
+      mny = block_min(mny, shT);
+      mxx = block_max(mxx, shT);
+      mxy = block_max(mxy, shT);
     }
-    mnx      = block_min(mnx, shT);
-    mny      = block_min(mny, shT);
-    mxx      = block_max(mxx, shT);
-    mxy      = block_max(mxy, shT);
     sum_rise = block_sum(sum_rise, shD);
-    uint32_t const ns = choose_slabs(
-      ve - vb, static_cast<double>(mxy) - static_cast<double>(mny), sum_rise, density);
-    T const h  = mxy - mny;
-    T const ih = (ns > 1 && h > T{0}) ? static_cast<T>(ns) / h : T{0};
-    for (uint32_t j = threadIdx.x; j < ns; j += kIdxBlock) cnt[j] = 0;
+    if (threadIdx.x == 0) {
+      uint32_t const ns = choose_slabs(
+        ve - vb, static_cast<double>(mxy) - static_cast<double>(mny), sum_rise, density);
+      T const h = mxy - mny;
+      s_ns      = ns;
+      s_ih      = (ns > 1 && h > T{0}) ? static_cast<T>(ns) / h : T{0};
+      s_ymin    = mny;
+    }
     __syncthreads();
+    uint32_t const ns = s_ns;
+    T const ih = s_ih, ymin = s_ymin;
+    for (uint32_t j = threadIdx.x; j < ns; j += kIdxBlock) cnt[j] = 0;
+    for (uint32_t v = vb + threadIdx.x; v < ve; v += kIdxBlock)
+      yslab[v] = static_cast<float>((vy[v] - ymin) * ih);
+    __syncthreads();  // counters cleared, yslab of every vertex visible
     uint32_t verts = 0;
     for (uint32_t v = vb + threadIdx.x; v < ve; v += kIdxBlock) {
-      uint32_t const pv = prev_in_ring(ro, r0, r1, v);
-      uint32_t const sp = edge_span<T>(vx, vy, v, pv, mny, ih, ns);
-      prev_out[v]       = pv;
+      uint32_t const pv = prev_out[v];
+      uint32_t const sp = edge_span<T>(vx[v], vy[v], vx[pv], vy[pv], yslab[v], yslab[pv], ns);
       spans[v]          = sp;
       bad |= (sp & kSpanTiny) ? 1u : 0u;
       if (sp & kSpanSkip) continue;
@@ -268,37 +384,49 @@ __global__ void __launch_bounds__(kIdxBlock)
                     bool float32, T* anchor_x, T* anchor_y, long long* aix, long long* aiy,
                     float4* box32, float* invh32, float* maxoff, uint32_t const* __restrict__ prev,
                     uint32_t const* __restrict__ spans, float4* edge32, uint32_t* slab_start,
-                    uint32_t* slab_edges, float4* slab_e32, T* vert_x, float* vert_x32)
+                    uint32_t* slab_edges, float4* slab_e32, T* vert_x, float* vert_x32,
+                    float2* __restrict__ vxy32)
 {
   __shared__ uint32_t cur[kMaxSlabs];
   __shared__ uint32_t shU[kIdxBlock / 32];
   __shared__ float shF[kIdxBlock / 32];
   __shared__ uint32_t vcur;
-  T const g = *grid;
+  __shared__ T s_cx, s_cy;
+  T const g    = *grid;
+  T const ginv = T{1} / g;  // g is a power of two: v * ginv == v / g while 1/g is finite
+  bool const gi = isfinite(ginv);
   for (size_t p = blockIdx.x; p < np; p += gridDim.x) {
     uint32_t const r0 = po[p], r1 = po[p + 1];
     uint32_t const vb = ro[r0], ve = ro[r1];
     uint32_t const ns = nslab[p];
-    T const ymin = pminy[p], ih = invh[p];
-    T cx = T{0}, cy = T{0};
-    if (ve > vb) {
-      cx = rint((pminx[p] + pmaxx[p]) * T{0.5} / g) * g;
-      cy = rint((ymin + pmaxy[p]) * T{0.5} / g) * g;
-      if (!isfinite(cx)) cx = T{0};
-      if (!isfinite(cy)) cy = T{0};
-    }
     if (threadIdx.x == 0) {
+      T const ymin = pminy[p];
+      T cx = T{0}, cy = T{0};
+      if (ve > vb) {
+        T const mx = (pminx[p] + pmaxx[p]) * T{0.5}, my = (ymin + pmaxy[p]) * T{0.5};
+        cx = rint(gi ? mx * ginv : mx / g) * g;
+        cy = rint(gi ? my * ginv : my / g) * g;
+        if (!isfinite(cx)) cx = T{0};
+        if (!isfinite(cy)) cy = T{0};
+      }
+      s_cx        = cx;
+      s_cy        = cy;
       anchor_x[p] = cx;
       anchor_y[p] = cy;
-      aix[p]      = llrint(cx / g);
-      aiy[p]      = llrint(cy / g);
+      aix[p]      = llrint(gi ? cx * ginv : cx / g);
+      aiy[p]      = llrint(gi ? cy * ginv : cy / g);
       box32[p]    = make_float4(static_cast<float>(pminx[p] - cx), static_cast<float>(ymin - cy),
                                 static_cast<float>(pmaxx[p] - cx), static_cast<float>(pmaxy[p] - cy));
-      invh32[p]   = static_cast<float>(ih);
+      invh32[p]   = static_cast<float>(invh[p]);
       vcur        = 0;
     }
     for (uint32_t j = threadIdx.x; j < ns; j += kIdxBlock) cur[j] = 0;
     __syncthreads();
+    T const cx = s_cx, cy = s_cy;
+    // each vertex's float32 offset once (both of its edges read it)
+    if (float32)
+      for (uint32_t v = vb + threadIdx.x; v < ve; v += kIdxBlock)
+        vxy32[v] = make_float2(static_cast<float>(vx[v] - cx), static_cast<float>(vy[v] - cy));
     // slab sizes again, then their offsets
     for (uint32_t v = vb + threadIdx.x; v < ve; v += kIdxBlock) {
       uint32_t const sp = spans[v];
@@ -319,11 +447,9 @@ __global__ void __launch_bounds__(kIdxBlock)
       uint32_t const pv = prev[v];
       float4 ef{};
       if (float32) {
-        ef.x      = static_cast<float>(vx[v] - cx);
-        ef.y      = static_cast<float>(vy[v] - cy);
-        ef.z      = static_cast<float>(vx[pv] - cx);
-        ef.w      = static_cast<float>(vy[pv] - cy);
-        edge32[v] = ef;
+        float2 const a = vxy32[v], b = vxy32[pv];
+        ef             = make_float4(a.x, a.y, b.x, b.y);
+        edge32[v]      = ef;
         local_max = fmaxf(local_max, fmaxf(fmaxf(fabsf(ef.x), fabsf(ef.y)),
                                            fmaxf(fabsf(ef.z), fabsf(ef.w))));
       }
@@ -434,13 +560,14 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
   Buffer<uint32_t> nent(alloc, np + 1), ebase(alloc, np + 1), nvert(alloc, np + 1);
   Buffer<uint32_t> totals(alloc, 3);
   Buffer<uint32_t> spans(alloc, nv);
+  Buffer<float> yslab(alloc, nv);
 
   unsigned const grd = static_cast<unsigned>(np < 152u * 64u ? (np ? np : 1) : 152u * 64u);
   if (np > 0) {
     index_count_kernel<T><<<grd, kIdxBlock, 0, s>>>(
       po, ro, vx, vy, np, pminx_.data(), pminy_.data(), pmaxx_.data(), pmaxy_.data(),
       invh_.data(), nslab_.data(), nent.data(), nvert.data(), exact_.data(), prev_.data(),
-      spans.data(), build_float32 ? kSlabDensityFloat32 : kSlabDensityFloat64);
+      spans.data(), yslab.data(), build_float32 ? kSlabDensityFloat32 : kSlabDensityFloat64);
     CSPT_CHECK_LAUNCH();
   }
   grid_kernel<T><<<1, 1024, 0, s>>>(pminx_.data(), pminy_.data(), pmaxx_.data(), pmaxy_.data(),
@@ -474,6 +601,8 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
   if (build_float32) vert_x32_ = Buffer<float>(alloc, nvertical);
   if (nslabs_total == 0)
     CSPT_CUDA_TRY(cudaMemsetAsync(slab_start_.data(), 0, sizeof(uint32_t), s));
+  yslab.reset();
+  Buffer<float2> vxy32(alloc, build_float32 ? nv : 0);
   if (np > 0) {
     index_fill_kernel<T><<<grd, kIdxBlock, 0, s>>>(
       po, ro, vx, vy, np, pminx_.data(), pminy_.data(), pmaxx_.data(), pmaxy_.data(),
@@ -481,7 +610,7 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
       build_float32, ax_.data(), ay_.data(), aix_.data(), aiy_.data(), box32_.data(),
       invh32_.data(), maxoff_.data(), prev_.data(), spans.data(), edge32_.data(),
       slab_start_.data(),
-      slab_edges_.data(), slab_e32_.data(), vert_x_.data(), vert_x32_.data());
+      slab_edges_.data(), slab_e32_.data(), vert_x_.data(), vert_x32_.data(), vxy32.data());
     CSPT_CHECK_LAUNCH();
     vert_end_kernel<<<grid_for(np, 256, 152u * 16u), 256, 0, s>>>(vbeg_.data(), nvert.data(),
                                                                   np, vend_.data());
