@@ -344,7 +344,10 @@ def run_ours(args, dist):
                 "kernel_ms_per_launch": bits_ms / max(bits_n, 1),
                 "note": "traffic from ncu is recorded in profiles/"}
 
-    # end to end through the public API from pinned host buffers
+    # end to end through the public API from pinned host buffers: host->device
+    # copies of points and polygons, quadtree build, boxes, join, PiP and the
+    # device->host copy of the pairs into pinned buffers allocated once (their
+    # capacity comes from the untimed first pass)
     e2e = None
     if args.e2e_steps > 0:
         hx = torch.from_numpy(w.x).pin_memory()
@@ -353,10 +356,11 @@ def run_ours(args, dist):
         hro = torch.from_numpy(P.ring_offset).pin_memory()
         hpo = torch.from_numpy(P.part_offset).pin_memory()
         hgo = torch.from_numpy(P.geometry_offset).pin_memory()
-        ems, h2d, d2h = [], 0, 0
+        o1 = o2 = None
+        ems, phases, h2d, d2h = [], [], 0, 0
         for it in range(args.e2e_steps + 1):
-            a, b = ev(), ev()
-            a.record(stream)
+            ph = [ev() for _ in range(5)]
+            ph[0].record(stream)
             dx = hx.to("cuda", non_blocking=True)
             dy = hy.to("cuda", non_blocking=True)
             dxy = hpxy.to("cuda", non_blocking=True)
@@ -364,27 +368,35 @@ def run_ours(args, dist):
             epolys = cs.GeoSeries.from_polygons_xy(dxy, hro.to("cuda", non_blocking=True),
                                                    hpo.to("cuda", non_blocking=True),
                                                    hgo.to("cuda", non_blocking=True))
+            ph[1].record(stream)
             epi, etree = cs.quadtree_on_points(epts, w.x_min, w.x_max, w.y_min, w.y_max, w.scale,
                                                w.max_depth, w.max_size)
+            ph[2].record(stream)
             ebb = cs.polygon_bounding_boxes(epolys)
             ej = cs.join_quadtree_and_bounding_boxes(etree, ebb, w.x_min, w.x_max, w.y_min,
                                                      w.y_max, w.scale, w.max_depth)
             er = cs.quadtree_point_in_polygon(ej, etree, epi, epts, epolys, method=args.method)
-            o1 = torch.empty(er["polygon_index"].shape, dtype=torch.int32, pin_memory=True)
-            o2 = torch.empty(er["point_index"].shape, dtype=torch.int32, pin_memory=True)
-            o1.copy_(er["polygon_index"], non_blocking=True)
-            o2.copy_(er["point_index"], non_blocking=True)
-            b.record(stream)
-            b.synchronize()
-            if it > 0:  # first pass warms the allocator
-                ems.append(a.elapsed_time(b))
+            ph[3].record(stream)
+            m = int(er["polygon_index"].numel())
+            if o1 is None or o1.numel() < m:
+                o1 = torch.empty(m, dtype=torch.int32, pin_memory=True)
+                o2 = torch.empty(m, dtype=torch.int32, pin_memory=True)
+            o1[:m].copy_(er["polygon_index"], non_blocking=True)
+            o2[:m].copy_(er["point_index"], non_blocking=True)
+            ph[4].record(stream)
+            ph[4].synchronize()
+            if it > 0:  # the first pass warms the allocators and sizes the host buffers
+                ems.append(ph[0].elapsed_time(ph[4]))
+                phases.append([ph[k].elapsed_time(ph[k + 1]) for k in range(4)])
             h2d = (hx.numel() + hy.numel() + hpxy.numel()) * 8 + (hro.numel() + hpo.numel() +
                                                                    hgo.numel()) * 4
-            d2h = (o1.numel() + o2.numel()) * 4
+            d2h = 2 * m * 4
         e2e_ms = dist.max(statistics.mean(ems))
         e2e = {"value": n * args.gpus / (e2e_ms / 1e3), "unit": "points/s",
                "ms_per_step": e2e_ms, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h),
+               "phases_ms": dict(zip(["h2d", "quadtree_build", "boxes_join_pip", "d2h"],
+                                     [statistics.mean(p[k] for p in phases) for k in range(4)])),
                "pairs_identical": bool(torch.equal(er["polygon_index"], res["polygon_index"]))}
 
     cpu = None

@@ -255,6 +255,35 @@ __host__ __device__ inline uint32_t gather16(uint32_t v)
   return v;
 }
 
+// static_cast<uint16_t>(t / s) for t >= 0 (the reference's cell index,
+// phase_1.cuh:73-85) without a float64 division in the common case.  With
+// r = fl(1/s) (host-rounded) and q0 = fl(t * r):
+//   |q0 - t/s| <= (t/s)(2^-52 + 2^-106)   and   |fl(t/s) - t/s| <= 2^-53 t/s,
+// so for t/s < 2^16 the two differ by less than 2^-35.  When q0 lies more
+// than 2^-30 away from every integer, q0 and fl(t/s) have the same integer
+// part; the fraction test reads q0's bits.  Every other case (near an
+// integer, below 2^-30, 2^16 and above, non-finite) divides.
+__device__ inline uint16_t cell_of_quotient(double t, double s, double r)
+{
+  double const q0          = t * r;
+  unsigned long long const b = static_cast<unsigned long long>(__double_as_longlong(q0));
+  int const e              = static_cast<int>((b >> 52) & 0x7FFull) - 1023;
+  if (e >= 0 && e < 16 && !(b >> 63)) {
+    unsigned long long const m    = (b & ((1ull << 52) - 1ull)) | (1ull << 52);
+    int const sh                  = 52 - e;  // fraction bits, >= 37
+    unsigned long long const frac = m & ((1ull << sh) - 1ull);
+    unsigned long long const mg   = 1ull << (sh - 30);
+    if (frac > mg && frac < (1ull << sh) - mg) return static_cast<uint16_t>(m >> sh);
+  } else if (b > 0x3E10000000000000ull && b < 0x3FEFFFFFFF800000ull) {
+    return 0;  // 2^-30 < q0 < 1 - 2^-30 (positive doubles order as integers)
+  }
+  return static_cast<uint16_t>(t / s);
+}
+__device__ inline uint16_t cell_of_quotient(float t, float s, float)
+{
+  return static_cast<uint16_t>(t / s);
+}
+
 // Explicitly rounded arithmetic: the library is compiled with -fmad=false,
 // and the few products the reference's build contracts into FMAs are written
 // as fma_rn.

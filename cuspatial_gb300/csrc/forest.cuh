@@ -38,7 +38,7 @@ constexpr unsigned kBlk     = 256;
 constexpr unsigned kGridCap = 152u * 16u;
 
 struct Inst {
-  double minx, miny, maxx, maxy, scale;
+  double minx, miny, maxx, maxy, scale, rscale;
   uint32_t d, max_size;
   uint32_t pt_begin, pt_end;
   uint32_t poly_begin, poly_end;
@@ -79,8 +79,8 @@ __global__ void keys_kernel(double const* __restrict__ x, double const* __restri
     if (px < I.minx || px > I.maxx || py < I.miny || py > I.maxy) {
       key = (1u << (2 * I.d)) - 1u;
     } else {
-      uint16_t const cx = static_cast<uint16_t>((px - I.minx) / I.scale);
-      uint16_t const cy = static_cast<uint16_t>((py - I.miny) / I.scale);
+      uint16_t const cx = cell_of_quotient(px - I.minx, I.scale, I.rscale);
+      uint16_t const cy = cell_of_quotient(py - I.miny, I.scale, I.rscale);
       key               = (spread16(cy) << 1) | spread16(cx);
     }
     keys[i] = (static_cast<uint64_t>(k) << kb) | key;
@@ -392,6 +392,7 @@ class Forest {
       double const span = std::max(p.x_max - p.x_min, p.y_max - p.y_min);
       double const ms   = span / static_cast<double>((1 << p.max_depth) + 2);
       I.scale           = p.scale > ms ? p.scale : ms;
+      I.rscale          = 1.0 / I.scale;
       I.max_size        = static_cast<uint32_t>(p.max_size < 1 ? 1 : p.max_size);
       I.pt_begin        = static_cast<uint32_t>(h_pt_off[i]);
       I.pt_end          = static_cast<uint32_t>(h_pt_off[i + 1]);

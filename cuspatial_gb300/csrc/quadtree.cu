@@ -30,7 +30,7 @@ constexpr uint8_t kNoStart = 0xFF;
 // level; others interleave the truncated cell coordinates.
 template <typename T>
 __global__ void morton_keys_kernel(T const* __restrict__ x, T const* __restrict__ y, size_t n,
-                                   T minx, T miny, T maxx, T maxy, T scale, int d,
+                                   T minx, T miny, T maxx, T maxy, T scale, T rscale, int d,
                                    uint32_t* __restrict__ keys)
 {
   for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
@@ -40,8 +40,8 @@ __global__ void morton_keys_kernel(T const* __restrict__ x, T const* __restrict_
     if (px < minx || px > maxx || py < miny || py > maxy) {
       k = static_cast<uint32_t>((1 << (2 * d)) - 1);
     } else {
-      uint16_t const cx = static_cast<uint16_t>((px - minx) / scale);
-      uint16_t const cy = static_cast<uint16_t>((py - miny) / scale);
+      uint16_t const cx = cell_of_quotient(px - minx, scale, rscale);
+      uint16_t const cy = cell_of_quotient(py - miny, scale, rscale);
       k                 = (spread16(cy) << 1) | spread16(cx);
     }
     keys[i] = k;
@@ -105,6 +105,92 @@ __global__ void keep_kernel(uint32_t const* __restrict__ starts, size_t nl,
     uint32_t const is_beg = (lvl[i] != kNoStart && lvl[i] <= prev_level) ? 1u : 0u;
     uint32_t const parent = rank_prev[i] + is_beg - 1u;
     keep[k]               = count_prev[parent] > max_size ? 1 : 0;
+  }
+}
+
+// finest level (d-1): every position whose key differs from its predecessor
+struct FinestStart {
+  uint8_t const* lvl;
+  __device__ uint32_t operator()(size_t i) const { return lvl[i] != kNoStart ? 1u : 0u; }
+};
+struct FinestStore {
+  uint8_t const* lvl;
+  uint32_t* S;
+  uint8_t* LV;
+  __device__ void operator()(size_t i, uint32_t e, uint32_t f) const
+  {
+    if (f) {
+      S[e]  = static_cast<uint32_t>(i);
+      LV[e] = lvl[i];
+    }
+  }
+};
+// level l from level l+1: the starts whose lvl is <= l
+struct CoarserStart {
+  uint8_t const* LV;
+  int l;
+  __device__ uint32_t operator()(size_t k) const
+  {
+    return static_cast<int>(LV[k]) <= l ? 1u : 0u;
+  }
+};
+struct CoarserStore {
+  uint32_t const* FS;
+  uint8_t const* FLV;
+  uint32_t* S;
+  uint32_t* X;
+  uint8_t* LV;
+  uint32_t* FP;
+  __device__ void operator()(size_t k, uint32_t e, uint32_t f) const
+  {
+    if (f) {
+      S[e]  = FS[k];
+      X[e]  = static_cast<uint32_t>(k);
+      LV[e] = FLV[k];
+    }
+    FP[k] = e + f - 1u;  // the level-l node holding level-(l+1) start k
+  }
+};
+
+// Point counts, child counts and the keep rule of one level's nodes.  A
+// level-l node (l >= 1) survives iff its parent holds more than max_size
+// points (phase_2.cuh:206-236).
+__global__ void level_nodes_kernel(uint32_t const* __restrict__ S, uint32_t const* __restrict__ X,
+                                   size_t nl, size_t n, size_t n_finer,
+                                   uint32_t const* __restrict__ P,
+                                   uint32_t const* __restrict__ parent_count, uint32_t max_size,
+                                   uint32_t* __restrict__ count, uint32_t* __restrict__ child,
+                                   uint8_t* __restrict__ keep)
+{
+  for (size_t j = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; j < nl;
+       j += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    size_t const e = j + 1 < nl ? S[j + 1] : n;
+    count[j]       = static_cast<uint32_t>(e - S[j]);
+    if (child) {
+      size_t const ce = j + 1 < nl ? X[j + 1] : n_finer;
+      child[j]        = static_cast<uint32_t>(ce - X[j]);
+    }
+    keep[j] = P ? (parent_count[P[j]] > max_size ? 1 : 0) : 1;
+  }
+}
+
+__global__ void compact_nodes_kernel(size_t nl, uint8_t const* __restrict__ keep,
+                                     uint32_t const* __restrict__ pos,
+                                     uint32_t const* __restrict__ S,
+                                     uint32_t const* __restrict__ count,
+                                     uint32_t const* __restrict__ child,
+                                     uint32_t const* __restrict__ skeys, int shift,
+                                     uint32_t* __restrict__ okey, uint32_t* __restrict__ ocount,
+                                     uint32_t* __restrict__ ochild, uint32_t* __restrict__ ostart)
+{
+  for (size_t k = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; k < nl;
+       k += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    if (!keep[k]) continue;
+    uint32_t const o = pos[k];
+    okey[o]          = skeys[S[k]] >> shift;
+    ocount[o]        = count[k];
+    ochild[o]        = child ? child[k] : 0u;
+    ostart[o]        = S[k];
   }
 }
 
@@ -175,8 +261,8 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
 
   Buffer<uint32_t> keys(alloc, n), keys_alt(alloc, n);
   Buffer<uint32_t> idx(alloc, n), idx_alt(alloc, n);
-  morton_keys_kernel<T>
-    <<<grd, blk, 0, s>>>(x, y, n, minx, miny, maxx, maxy, scale, d, keys.data());
+  morton_keys_kernel<T><<<grd, blk, 0, s>>>(x, y, n, minx, miny, maxx, maxy, scale,
+                                            T{1} / scale, d, keys.data());
   CSPT_CHECK_LAUNCH();
   // cells reach 2^d + 2, so the key needs 2(d+1) bits (2(d+2) below d = 2)
   int const key_bits = d >= 2 ? 2 * d + 2 : 2 * d + 4;
@@ -226,97 +312,87 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
     return;
   }
 
-  // Levels 0..d-1, top-down.
-  Buffer<uint32_t> rank_prev(alloc, n + 1), rank_cur(alloc, n + 1);
-  Buffer<uint32_t> starts_prev, starts_cur;
-  Buffer<uint32_t> count_prev, count_cur;
-  Buffer<uint8_t> keep_prev, keep_cur;
-  size_t n_prev = 0;
+  // Levels, bottom-up.  A position starts a level-l node iff lvl <= l, so
+  // the level-l starts are the level-(l+1) starts whose lvl is <= l: each
+  // level is ranked by a scan over the next finer level only (about 1.3 N
+  // elements in all instead of d N).  For a level-l node j: S = first sorted
+  // position, X = its index among the level-(l+1) starts; for a level-(l+1)
+  // start k: P = the level-l node holding it (its parent).
+  struct Raw {
+    Buffer<uint32_t> S, X, P, count;
+    Buffer<uint8_t> LV;
+    size_t n = 0;
+  };
+  std::vector<Raw> raw(d);
+  {
+    Raw& R = raw[d - 1];
+    R.S    = Buffer<uint32_t>(alloc, n);
+    R.LV   = Buffer<uint8_t>(alloc, n);
+    scan_apply<uint32_t>(FinestStart{lv}, FinestStore{lv, R.S.data(), R.LV.data()}, n,
+                         total.data(), alloc);
+    R.n = read_back(total.data(), s);
+  }
+  for (int l = d - 2; l >= 0; --l) {
+    Raw& F = raw[l + 1];
+    Raw& R = raw[l];
+    R.S    = Buffer<uint32_t>(alloc, F.n);
+    R.X    = Buffer<uint32_t>(alloc, F.n);
+    R.LV   = Buffer<uint8_t>(alloc, F.n);
+    F.P    = Buffer<uint32_t>(alloc, F.n);
+    scan_apply<uint32_t>(CoarserStart{F.LV.data(), l},
+                         CoarserStore{F.S.data(), F.LV.data(), R.S.data(), R.X.data(),
+                                      R.LV.data(), F.P.data()},
+                         F.n, total.data(), alloc);
+    R.n = read_back(total.data(), s);
+    F.LV.reset();
+  }
+  raw[0].LV.reset();
+  size_t const level_1_size = raw[0].n;
   std::vector<LevelNodes> levels(d);
-  size_t level_1_size = 0;
-
-  // emits the kept nodes of level `lv_out` once its child counts are known
-  auto emit = [&](int lv_out, Buffer<uint32_t>& starts, Buffer<uint32_t>& counts,
-                  Buffer<uint32_t>* childs, Buffer<uint8_t>* keep, size_t nl) {
-    LevelNodes& L      = levels[lv_out];
-    uint32_t const* st = starts.data();
-    uint8_t const* kp  = keep ? keep->data() : nullptr;
+  for (int l = 0; l < d; ++l) {
+    Raw& R        = raw[l];
+    size_t const nl = R.n;
+    R.count       = Buffer<uint32_t>(alloc, nl);
+    Buffer<uint32_t> child(alloc, l + 1 < d ? nl : 0);
+    Buffer<uint8_t> keep(alloc, nl);
+    if (nl) {
+      level_nodes_kernel<<<grid_for(nl, blk, 152u * 16u), blk, 0, s>>>(
+        R.S.data(), R.X.data(), nl, n, l + 1 < d ? raw[l + 1].n : 0, l > 0 ? R.P.data() : nullptr,
+        l > 0 ? raw[l - 1].count.data() : nullptr, max_size, R.count.data(),
+        l + 1 < d ? child.data() : nullptr, keep.data());
+      CSPT_CHECK_LAUNCH();
+    }
+    // compact the kept nodes of the level
+    LevelNodes& L = levels[l];
     Buffer<uint32_t> pos(alloc, nl);
-    uint32_t* ps = pos.data();
-    scan_apply<uint32_t>(
-      [kp] __device__(size_t k) { return kp ? static_cast<uint32_t>(kp[k]) : 1u; },
-      [ps] __device__(size_t k, uint32_t e, uint32_t) { ps[k] = e; }, nl, total.data(), alloc);
+    uint8_t const* kp = keep.data();
+    uint32_t* ps      = pos.data();
+    scan_apply<uint32_t>([kp] __device__(size_t k) { return static_cast<uint32_t>(kp[k]); },
+                         [ps] __device__(size_t k, uint32_t e, uint32_t) { ps[k] = e; }, nl,
+                         total.data(), alloc);
     size_t const m = read_back(total.data(), s);
     L.size         = m;
     L.key          = Buffer<uint32_t>(alloc, m);
     L.count        = Buffer<uint32_t>(alloc, m);
     L.child        = Buffer<uint32_t>(alloc, m);
     L.start        = Buffer<uint32_t>(alloc, m);
-    uint32_t *ok = L.key.data(), *oc = L.count.data(), *och = L.child.data(),
-             *os = L.start.data();
-    uint32_t const* sk  = skeys.data();
-    uint32_t const* cn  = counts.data();
-    uint32_t const* chp = childs ? childs->data() : nullptr;
-    int const shift     = 2 * (d - 1 - lv_out);
-    scan_apply<uint32_t>([] __device__(size_t) { return 0u; },
-                         [=] __device__(size_t k, uint32_t, uint32_t) {
-                           if (kp && !kp[k]) return;
-                           uint32_t const o = ps[k];
-                           ok[o]            = sk[st[k]] >> shift;
-                           oc[o]            = cn[k];
-                           och[o]           = chp ? chp[k] : 0u;
-                           os[o]            = st[k];
-                         },
-                         nl, static_cast<uint32_t*>(nullptr), alloc);
-  };
-
-  for (int l = 0; l < d; ++l) {
-    // rank the level-l starts and gather their positions
-    starts_cur     = Buffer<uint32_t>(alloc, n);
-    uint32_t* rk   = rank_cur.data();
-    uint32_t* st   = starts_cur.data();
-    int const ll   = l;
-    scan_apply<uint32_t>(
-      [lv, ll] __device__(size_t i) {
-        return (lv[i] != kNoStart && static_cast<int>(lv[i]) <= ll) ? 1u : 0u;
-      },
-      [rk, st] __device__(size_t i, uint32_t e, uint32_t f) {
-        rk[i] = e;
-        if (f) st[e] = static_cast<uint32_t>(i);
-      },
-      n, rank_cur.data() + n, alloc);
-    size_t const nl = read_back(rank_cur.data() + n, s);
-    if (l == 0) level_1_size = nl;
-    count_cur = Buffer<uint32_t>(alloc, nl);
-    node_count_kernel<<<grid_for(nl, blk, 152u * 16u), blk, 0, s>>>(st, nl, n, count_cur.data());
-    CSPT_CHECK_LAUNCH();
-    keep_cur = Buffer<uint8_t>(alloc, nl);
-    if (l == 0) {
-      CSPT_CUDA_TRY(cudaMemsetAsync(keep_cur.data(), 1, nl, s));
-    } else {
-      keep_kernel<<<grid_for(nl, blk, 152u * 16u), blk, 0, s>>>(
-        st, nl, lv, l - 1, rank_prev.data(), count_prev.data(), max_size, keep_cur.data());
+    if (nl) {
+      compact_nodes_kernel<<<grid_for(nl, blk, 152u * 16u), blk, 0, s>>>(
+        nl, kp, ps, R.S.data(), R.count.data(), l + 1 < d ? child.data() : nullptr,
+        skeys.data(), 2 * (d - 1 - l), L.key.data(), L.count.data(), L.child.data(),
+        L.start.data());
       CSPT_CHECK_LAUNCH();
-      // the previous level's child counts, then emit it
-      Buffer<uint32_t> child_prev(alloc, n_prev);
-      child_count_kernel<<<grid_for(n_prev, blk, 152u * 16u), blk, 0, s>>>(
-        starts_prev.data(), n_prev, rank_cur.data(), n, child_prev.data());
-      CSPT_CHECK_LAUNCH();
-      emit(l - 1, starts_prev, count_prev, &child_prev, l - 1 == 0 ? nullptr : &keep_prev,
-           n_prev);
     }
-    std::swap(rank_prev, rank_cur);
-    starts_prev = std::move(starts_cur);
-    count_prev  = std::move(count_cur);
-    keep_prev   = std::move(keep_cur);
-    n_prev      = nl;
+    // the parent level's counts are no longer needed
+    if (l > 0) {
+      raw[l - 1].count.reset();
+      raw[l - 1].S.reset();
+      raw[l - 1].X.reset();
+      raw[l - 1].P.reset();
+    }
+    R.P.reset();
   }
-  emit(d - 1, starts_prev, count_prev, nullptr, &keep_prev, n_prev);
-  starts_prev.reset();
-  count_prev.reset();
-  keep_prev.reset();
-  rank_prev.reset();
-  rank_cur.reset();
+  raw.clear();
   lvl.reset();
 
   size_t q = 0;
