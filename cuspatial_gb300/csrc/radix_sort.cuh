@@ -12,7 +12,7 @@
 
 namespace cspt {
 
-constexpr int kSortBlock = 256;
+constexpr int kSortBlock = 256;  // one thread per 8-bit digit in the scatter
 constexpr int kSortWarps = kSortBlock / 32;
 constexpr int kSortRound = 8;  // rounds of 32 items per warp
 constexpr int kSortTile  = kSortBlock * kSortRound;
@@ -46,6 +46,12 @@ __global__ void __launch_bounds__(kSortBlock)
   }
 }
 
+static_assert(kSortBlock == 256, "the scatter assigns one thread per digit");
+
+// Stable scatter of one tile: items are ranked per warp with
+// __match_any_sync (rounds in input order), placed in shared memory in the
+// tile's digit order, then written out in that order, so the global writes
+// of each digit's run are contiguous.
 template <typename K>
 __global__ void __launch_bounds__(kSortBlock)
   radix_scatter_kernel(K const* keys_in, uint32_t const* vals_in, K* keys_out, uint32_t* vals_out,
@@ -53,12 +59,18 @@ __global__ void __launch_bounds__(kSortBlock)
                        unsigned ntiles)
 {
   __shared__ uint32_t wcount[kSortWarps][256];
+  __shared__ uint32_t tile_start[256];
+  __shared__ uint32_t global_base[256];
+  __shared__ K skey[kSortTile];
+  __shared__ uint32_t sval[kSortTile];
+  __shared__ uint32_t total_s;
   for (int i = threadIdx.x; i < kSortWarps * 256; i += kSortBlock) (&wcount[0][0])[i] = 0;
   __syncthreads();
-  int const warp     = threadIdx.x >> 5;
-  int const lane     = threadIdx.x & 31;
-  unsigned const lt  = (1u << lane) - 1u;
-  size_t const base  = static_cast<size_t>(blockIdx.x) * kSortTile + warp * (32 * kSortRound);
+  int const warp       = threadIdx.x >> 5;
+  int const lane       = threadIdx.x & 31;
+  unsigned const lt    = (1u << lane) - 1u;
+  size_t const tbase   = static_cast<size_t>(blockIdx.x) * kSortTile;
+  size_t const base    = tbase + warp * (32 * kSortRound);
   K key[kSortRound];
   uint32_t val[kSortRound];
   uint32_t pos[kSortRound];
@@ -81,24 +93,38 @@ __global__ void __launch_bounds__(kSortBlock)
     __syncwarp();
   }
   __syncthreads();
-  // per digit: prefix over warps, plus the tile's global base
-  for (int d = threadIdx.x; d < 256; d += kSortBlock) {
-    uint32_t run = offsets[static_cast<size_t>(d) * ntiles + blockIdx.x];
+  // per digit (one thread each): prefix over warps, the tile's digit start
+  // and the digit's global base
+  {
+    int const d    = threadIdx.x;  // kSortBlock == 256 digits
+    uint32_t run   = 0;
 #pragma unroll
     for (int w = 0; w < kSortWarps; ++w) {
       uint32_t const c = wcount[w][d];
       wcount[w][d]     = run;
       run += c;
     }
+    uint32_t const start = block_exclusive_scan<uint32_t, kSortBlock>(run, &total_s);
+    tile_start[d]        = start;
+    global_base[d]       = offsets[static_cast<size_t>(d) * ntiles + blockIdx.x];
   }
   __syncthreads();
 #pragma unroll
   for (int r = 0; r < kSortRound; ++r) {
     if (dig[r] != kNoDigit) {
-      uint32_t const dst = wcount[warp][dig[r]] + pos[r];
-      keys_out[dst]      = key[r];
-      vals_out[dst]      = val[r];
+      uint32_t const t = tile_start[dig[r]] + wcount[warp][dig[r]] + pos[r];
+      skey[t]          = key[r];
+      sval[t]          = val[r];
     }
+  }
+  __syncthreads();
+  uint32_t const m = total_s;
+  for (uint32_t t = threadIdx.x; t < m; t += kSortBlock) {
+    K const k        = skey[t];
+    unsigned const d = static_cast<unsigned>((k >> shift) & mask);
+    uint32_t const g = global_base[d] + (t - tile_start[d]);
+    keys_out[g]      = k;
+    vals_out[g]      = sval[t];
   }
 }
 
