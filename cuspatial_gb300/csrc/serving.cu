@@ -14,10 +14,10 @@
 // v_min + k * scale * 2^s computed with one rounding, and a parent's corners
 // coincide bit for bit with its outer children's, so a box meeting a leaf
 // meets every ancestor.  The resident set keeps its polygon boxes in a
-// uniform cell grid; a leaf scans the cells its extent covers and keeps a
-// polygon when the reference's closed-interval overlap test holds, counting
-// it only in the first cell (in both axes) that the leaf's and the box's cell
-// ranges share.  The cell of a coordinate is floor((v - v0) / w) clamped to
+// uniform cell grid; every (leaf, covered cell) is one work item that keeps
+// a polygon of the cell when the reference's closed-interval overlap test
+// holds, counting it only in the first cell (in both axes) that the leaf's
+// and the box's cell ranges share.  The cell of a coordinate is floor((v - v0) / w) clamped to
 // the grid, a monotone function of v, so any common point of box and extent
 // lies in a cell of both ranges and every pair is found exactly once.  Pairs
 // are then sorted by (leaf first position, polygon), the reference's order.
@@ -157,75 +157,91 @@ __device__ inline uint32_t node_instance(uint64_t const* __restrict__ node_off, 
   return lo;
 }
 
-// A leaf's pairs with the resident polygons, one warp per node; lanes take
-// the cells the leaf's extent covers.  The count pass stores pairs per node;
-// the write pass emits (leaf first position << pbits | polygon, polygon, node).
-template <bool Write>
-__global__ void leaf_join_kernel(TreeView t, uint64_t const* __restrict__ node_off, uint32_t ni,
-                                 Inst const* __restrict__ inst,
-                                 uint32_t const* __restrict__ goff, GridView g,
-                                 uint32_t* __restrict__ counts, uint32_t const* __restrict__ pos,
-                                 int pbits, uint64_t* __restrict__ okey,
-                                 uint32_t* __restrict__ opoly, uint32_t* __restrict__ onode)
+// The cells a leaf's extent covers, one work item per (leaf, cell), so a
+// large leaf (a sparse request's leaves can cover thousands of cells) is
+// spread over the whole GPU.
+struct LeafCells {
+  double x0, y0, x1, y1;  // leaf extent (intersection.cuh:104-128)
+  int cx0, cy0, ncx;
+  uint32_t ncells;
+};
+
+__global__ void leaf_cells_kernel(TreeView t, uint64_t const* __restrict__ node_off, uint32_t ni,
+                                  Inst const* __restrict__ inst, GridView g,
+                                  LeafCells* __restrict__ lc, uint32_t* __restrict__ ncells)
 {
-  int const lane      = threadIdx.x & 31;
-  size_t const nwarps = (static_cast<size_t>(gridDim.x) * blockDim.x) >> 5;
-  for (size_t n = (blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5; n < t.nq;
-       n += nwarps) {
-    bool const leaf = !t.internal[n];
-    double x0 = 0, y0 = 0, x1 = -1, y1 = -1;
-    int cx0 = 0, cy0 = 0, ncx = 0, ncells = 0;
-    if (leaf) {
+  CSPT_GRID_STRIDE(n, t.nq)
+  {
+    LeafCells c{0.0, 0.0, -1.0, -1.0, 0, 0, 0, 0u};
+    if (!t.internal[n]) {
       Inst const& I      = inst[node_instance(node_off, ni, n)];
       uint32_t const key = t.key[n];
       int const sh       = static_cast<int>(I.d) - 1 - static_cast<int>(t.level[n]);
       if (sh >= 0) {
-        // intersection.cuh:104-128 (as in the box-side join's classify)
         double const kx = static_cast<double>(gather16(key));
         double const ky = static_cast<double>(gather16(key >> 1));
         double const ls = I.scale * static_cast<double>(1 << sh);
-        x0              = fma_rn(kx, ls, I.minx);
-        y0              = fma_rn(ky, ls, I.miny);
-        x1              = fma_rn(kx + 1.0, ls, I.minx);
-        y1              = fma_rn(ky + 1.0, ls, I.miny);
-        cx0             = cell_of(x0, g.x0, g.cw, g.gx);
-        cy0             = cell_of(y0, g.y0, g.ch, g.gy);
-        ncx             = cell_of(x1, g.x0, g.cw, g.gx) - cx0 + 1;
-        ncells          = ncx * (cell_of(y1, g.y0, g.ch, g.gy) - cy0 + 1);
+        c.x0            = fma_rn(kx, ls, I.minx);
+        c.y0            = fma_rn(ky, ls, I.miny);
+        c.x1            = fma_rn(kx + 1.0, ls, I.minx);
+        c.y1            = fma_rn(ky + 1.0, ls, I.miny);
+        c.cx0           = cell_of(c.x0, g.x0, g.cw, g.gx);
+        c.cy0           = cell_of(c.y0, g.y0, g.ch, g.gy);
+        c.ncx           = cell_of(c.x1, g.x0, g.cw, g.gx) - c.cx0 + 1;
+        c.ncells =
+          static_cast<uint32_t>(c.ncx * (cell_of(c.y1, g.y0, g.ch, g.gy) - c.cy0 + 1));
       }
     }
-    // pass over the lane's cells: count (and, when writing, emit)
-    auto scan_cells = [&](bool emit, uint32_t base) {
-      uint32_t c = 0;
-      for (int k = lane; k < ncells; k += 32) {
-        int const cx = cx0 + k % ncx, cy = cy0 + k / ncx;
-        int const cell = cy * g.gx + cx;
-        for (uint32_t j = g.cell_start[cell]; j < g.cell_start[cell + 1]; ++j) {
-          uint32_t const p = g.cell_poly[j];
-          int2 const pc    = g.poly_cell[p];
-          if (max(pc.x, cx0) != cx || max(pc.y, cy0) != cy) continue;
-          if (x0 > g.bmaxx[p] || x1 < g.bminx[p] || y0 > g.bmaxy[p] || y1 < g.bminy[p]) continue;
-          if (emit) {
-            uint32_t const d = base + c;
-            okey[d]  = (static_cast<uint64_t>(goff[n]) << pbits) | p;
-            opoly[d] = p;
-            onode[d] = static_cast<uint32_t>(n);
-          }
-          ++c;
-        }
-      }
-      return c;
-    };
-    uint32_t const mine = scan_cells(false, 0);
-    if (!Write) {
-      uint32_t tot = mine;
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) tot += __shfl_xor_sync(0xFFFFFFFFu, tot, off);
-      if (lane == 0) counts[n] = tot;
-    } else {
-      uint32_t const incl = warp_inclusive_scan(mine);
-      if (mine) scan_cells(true, pos[n] + incl - mine);
+    lc[n]     = c;
+    ncells[n] = c.ncells;
+  }
+}
+
+// One thread per (leaf, cell): the polygons of the cell whose box meets the
+// leaf's extent, counted only in the first cell both cell ranges share.
+template <bool Write>
+__global__ void leaf_cell_join_kernel(LeafCells const* __restrict__ lc,
+                                      uint32_t const* __restrict__ cell_off, size_t q,
+                                      size_t nitems, GridView g, uint32_t const* __restrict__ goff,
+                                      uint32_t* __restrict__ counts,
+                                      uint32_t const* __restrict__ pos, int pbits,
+                                      uint64_t* __restrict__ okey, uint32_t* __restrict__ opoly,
+                                      uint32_t* __restrict__ onode)
+{
+  CSPT_GRID_STRIDE(i, nitems)
+  {
+    // the node whose cell range holds item i: cell_off[n] <= i < cell_off[n + 1]
+    size_t lo = 0, hi = q;
+    while (hi - lo > 1) {
+      size_t const mid = (lo + hi) >> 1;
+      if (cell_off[mid] <= i)
+        lo = mid;
+      else
+        hi = mid;
     }
+    size_t const n  = lo;
+    LeafCells const c = lc[n];
+    uint32_t const k  = static_cast<uint32_t>(i - cell_off[n]);
+    int const cx = c.cx0 + static_cast<int>(k % static_cast<uint32_t>(c.ncx));
+    int const cy = c.cy0 + static_cast<int>(k / static_cast<uint32_t>(c.ncx));
+    int const cell = cy * g.gx + cx;
+    uint32_t found = 0;
+    uint32_t const base = Write ? pos[i] : 0u;
+    for (uint32_t j = g.cell_start[cell]; j < g.cell_start[cell + 1]; ++j) {
+      uint32_t const p = g.cell_poly[j];
+      int2 const pc    = g.poly_cell[p];
+      if (max(pc.x, c.cx0) != cx || max(pc.y, c.cy0) != cy) continue;
+      if (c.x0 > g.bmaxx[p] || c.x1 < g.bminx[p] || c.y0 > g.bmaxy[p] || c.y1 < g.bminy[p])
+        continue;
+      if (Write) {
+        uint32_t const d = base + found;
+        okey[d]          = (static_cast<uint64_t>(goff[n]) << pbits) | p;
+        opoly[d]         = p;
+        onode[d]         = static_cast<uint32_t>(n);
+      }
+      ++found;
+    }
+    if (!Write) counts[i] = found;
   }
 }
 
@@ -388,19 +404,28 @@ class ServingBatch {
     size_t const q      = f_.q_;
     GridView const g    = set.grid();
     int const pbits     = set.pbits();
-    Buffer<uint32_t> counts(a, q + 1);
     unsigned const blk = 256;
-    unsigned const grd = grid_for(q * 32, blk, 152u * 16u);
+    Buffer<LeafCells> lc(a, q);
+    Buffer<uint32_t> cell_off(a, q + 1);
+    Buffer<uint32_t> counts;
+    size_t nitems = 0;
     {
       KernelTimer timer("serving_join", s);
-      leaf_join_kernel<false><<<grd, blk, 0, s>>>(f_.view(), f_.node_off_.data(), ni32,
-                                                  f_.inst_.data(), f_.goff_.data(), g,
-                                                  counts.data(), nullptr, pbits, nullptr,
-                                                  nullptr, nullptr);
+      leaf_cells_kernel<<<grid_for(q, blk, 152u * 16u), blk, 0, s>>>(
+        f_.view(), f_.node_off_.data(), ni32, f_.inst_.data(), g, lc.data(), cell_off.data());
       CSPT_CHECK_LAUNCH();
+      exclusive_scan<uint32_t>(cell_off.data(), cell_off.data(), q, cell_off.data() + q, a);
+      nitems = read_back(cell_off.data() + q, s);
+      counts = Buffer<uint32_t>(a, nitems + 1);
+      if (nitems) {
+        leaf_cell_join_kernel<false><<<grid_for(nitems, blk, 152u * 16u), blk, 0, s>>>(
+          lc.data(), cell_off.data(), q, nitems, g, f_.goff_.data(), counts.data(), nullptr,
+          pbits, nullptr, nullptr, nullptr);
+        CSPT_CHECK_LAUNCH();
+      }
+      exclusive_scan<uint32_t>(counts.data(), counts.data(), nitems, counts.data() + nitems, a);
     }
-    exclusive_scan<uint32_t>(counts.data(), counts.data(), q, counts.data() + q, a);
-    k_ = read_back(counts.data() + q, s);
+    k_ = read_back(counts.data() + nitems, s);
     pair_begin_ = Buffer<uint32_t>(a, ni + 1);
     if (k_ == 0) {
       CSPT_CUDA_TRY(cudaMemsetAsync(row_off_.data(), 0, (ni + 1) * 8, s));
@@ -409,10 +434,9 @@ class ServingBatch {
     {
       Buffer<uint64_t> key(a, k_), key_alt(a, k_);
       Buffer<uint32_t> poly(a, k_), node(a, k_), perm(a, k_), perm_alt(a, k_);
-      leaf_join_kernel<true><<<grd, blk, 0, s>>>(f_.view(), f_.node_off_.data(), ni32,
-                                                 f_.inst_.data(), f_.goff_.data(), g, nullptr,
-                                                 counts.data(), pbits, key.data(), poly.data(),
-                                                 node.data());
+      leaf_cell_join_kernel<true><<<grid_for(nitems, blk, 152u * 16u), blk, 0, s>>>(
+        lc.data(), cell_off.data(), q, nitems, g, f_.goff_.data(), nullptr, counts.data(), pbits,
+        key.data(), poly.data(), node.data());
       CSPT_CHECK_LAUNCH();
       int const bits = 32 + pbits;
       KernelTimer timer("serving_sort", s);
