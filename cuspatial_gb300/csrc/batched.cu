@@ -205,7 +205,8 @@ class BatchedPip {
       return;
     }
     bool const filtered = method == CSPT_METHOD_FILTERED;
-    index_.reset(new PolygonIndex<double>(po, np_ + 1, ro, nro, vx, vy, nv, filtered, a));
+    index_.reset(new PolygonIndex<double>(po, np_ + 1, ro, nro, vx, vy, nv, filtered, a,
+                                          /*order_slabs=*/true));
     pip_.reset(new PipExec(pair_poly_.data(), pair_quad_.data(), k_, f_.length_.data(),
                            f_.goff_.data(), f_.sidx_.data(), f_.n_, x, y, index_->view(),
                            filtered, static_cast<unsigned>(block), a));

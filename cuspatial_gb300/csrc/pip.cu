@@ -130,7 +130,7 @@ __device__ bool pip_exact(T px, T py, PolygonIndexView<T> const& ix, uint32_t po
   uint32_t const e0 = ix.slab_start[s], e1 = ix.slab_start[s + 1];
   bool within       = false;
   for (uint32_t k = e0; k < e1; ++k) {
-    uint32_t const v  = ix.slab_edges[k];
+    uint32_t const v  = ix.slab_edges[k] & kEntryVertex;
     uint32_t const pv = ix.prev_vertex[v];
     T const ax = ix.vx[v], ay = ix.vy[v], bx = ix.vx[pv], by = ix.vy[pv];
     T const run = bx - ax, rise = by - ay;
@@ -209,7 +209,9 @@ unsigned pair_grid(K kernel, unsigned block, size_t npairs)
 // a device counter (zeroed before the launch), so warps that drew cheap pairs
 // keep working while others finish long ones; the grid holds only as many
 // blocks as are resident.
-template <bool Filtered>
+// Ordered: the index's slabs are ordered (slab_order_kernel) and the
+// per-(slab, x-bin) windows are used.
+template <bool Filtered, bool Ordered = false>
 __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : kPipMinBlocksExact)
   pip_pair_kernel(uint32_t const* __restrict__ pair_poly, uint32_t const* __restrict__ pair_quad,
                   uint32_t const* __restrict__ pair_group, size_t npairs,
@@ -270,6 +272,7 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
         }
       }
       float const invh     = ix.inv_slab_h32[poly];
+      float const invw     = Ordered ? ix.inv_bin_w32[poly] : 0.0f;
       uint32_t const ns    = ix.num_slabs[poly];
       uint32_t const slab0 = ix.slab_base[poly];
       uint32_t const vb = ix.vert_begin[poly], ve = ix.vert_end[poly];
@@ -315,9 +318,31 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
                 uint32_t sj    = 0;
                 if (fs > 0.0f) sj = fs >= static_cast<float>(ns) ? ns - 1 : static_cast<uint32_t>(fs);
                 if (sj >= ns) sj = ns - 1;
-                uint32_t const e0 = ix.slab_start[slab0 + sj], e1 = ix.slab_start[slab0 + sj + 1];
-                bool within       = false;
-                for (uint32_t k2 = e0; k2 < e1; ++k2) {
+                uint32_t const sidx = slab0 + sj;
+                uint32_t const e0 = ix.slab_start[sidx], e1 = ix.slab_start[sidx + 1];
+                // crossing edges [e0, e0 + nf): only the point's x-bin window
+                // [wlo, whi) is tested, those after it all toggle (parity bit);
+                // the other edges [e0 + nf, e1) are all tested
+                uint32_t const nf = Ordered ? ix.slab_nfull[sidx] : 0u;
+                uint32_t wlo = 0, whi = nf;
+                bool within = false;
+                if (Ordered && nf > 0 && m * invw <= 16384.0f) {
+                  float const fb   = (qx - bx.x) * invw;
+                  uint32_t const top = static_cast<uint32_t>(kSlabBins - 1);
+                  uint32_t const b   = fb > 0.0f ? (fb < static_cast<float>(top)
+                                                      ? static_cast<uint32_t>(fb)
+                                                      : top)
+                                                 : 0u;
+                  uint32_t const rec = ix.slab_bins[static_cast<size_t>(sidx) * kSlabBins + b];
+                  wlo    = rec & 0x7FFFu;
+                  whi    = (rec >> 15) & 0x7FFFu;
+                  within = (rec >> 30) & 1u;
+                }
+                uint32_t const nwin = whi - wlo;
+                uint32_t const ntot = nwin + (e1 - e0 - nf);
+                for (uint32_t t = 0; t < ntot; ++t) {
+                  uint32_t const k2 =
+                    Ordered ? (t < nwin ? e0 + wlo + t : e0 + nf + (t - nwin)) : e0 + t;
                   float4 const e = ix.slab_e32[k2];  // (ax, ay, bx, by)
                   float const ya = e.y - qy, yb = e.w - qy;
                   bool const y1  = ya > 0.0f;
@@ -339,7 +364,7 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
                     py64              = y[pi];
                     have64            = true;
                   }
-                  uint32_t const v  = ix.slab_edges[k2];
+                  uint32_t const v  = ix.slab_edges[k2] & kEntryVertex;
                   uint32_t const pv = ix.prev_vertex[v];
                   int const ee =
                     exact_edge<double>(px64, py64, ix.vx[v], ix.vy[v], ix.vx[pv], ix.vy[pv]);
@@ -627,7 +652,8 @@ class PipExec::Impl {
     u_        = Buffer<float2>(alloc, filtered ? npi : 0);
     refined_  = Buffer<unsigned long long>(alloc, 2);  // [0] refined, [1] next pair
     flag_     = Buffer<int>(alloc, 1);
-    grid_true_  = pair_grid(pip_pair_kernel<true>, blk_, npairs);
+    grid_true_    = pair_grid(pip_pair_kernel<true>, blk_, npairs);
+    grid_ordered_ = pair_grid(pip_pair_kernel<true, true>, blk_, npairs);
     grid_false_ = pair_grid(pip_pair_kernel<false>, blk_, npairs);
     scan_apply_prealloc<uint64_t>(WordsOf{pair_quad, qlen}, Store64{word_off_.data()}, npairs,
                                   word_off_.data() + npairs, partials_.data(), s);
@@ -648,10 +674,16 @@ class PipExec::Impl {
                                             qoff_, pi_, npi_, x_, y_, ix_.grid, u_.data(),
                                             frames_.data());
       CSPT_CHECK_LAUNCH();
-      pip_pair_kernel<true><<<grid_true_, blk, 0, s>>>(
-        pp_, pq_, pgroup_.data(), np_, qlen_, qoff_, pi_, npi_, x_, y_, u_.data(),
-        frames_.data(), ix_, word_off_.data(), bits_.data(), counts_.data(), refined_.data(),
-        refined_.data() + 1);
+      if (ix_.slab_nfull)
+        pip_pair_kernel<true, true><<<grid_ordered_, blk, 0, s>>>(
+          pp_, pq_, pgroup_.data(), np_, qlen_, qoff_, pi_, npi_, x_, y_, u_.data(),
+          frames_.data(), ix_, word_off_.data(), bits_.data(), counts_.data(), refined_.data(),
+          refined_.data() + 1);
+      else
+        pip_pair_kernel<true><<<grid_true_, blk, 0, s>>>(
+          pp_, pq_, pgroup_.data(), np_, qlen_, qoff_, pi_, npi_, x_, y_, u_.data(),
+          frames_.data(), ix_, word_off_.data(), bits_.data(), counts_.data(), refined_.data(),
+          refined_.data() + 1);
     } else {
       pip_pair_kernel<false><<<grid_false_, blk, 0, s>>>(
         pp_, pq_, nullptr, np_, qlen_, qoff_, pi_, npi_, x_, y_, nullptr, nullptr, ix_,
@@ -694,7 +726,7 @@ class PipExec::Impl {
   PolygonIndexView<double> ix_;
   bool filtered_;
   unsigned blk_;
-  unsigned grid_true_ = 1, grid_false_ = 1;
+  unsigned grid_true_ = 1, grid_false_ = 1, grid_ordered_ = 1;
   size_t nwords_ = 0;
   Buffer<uint64_t> word_off_, out_off_, partials_;
   Buffer<uint32_t> gpart_, counts_, gstart_, pgroup_, bits_;

@@ -385,7 +385,7 @@ __global__ void __launch_bounds__(kIdxBlock)
                     float4* box32, float* invh32, float* maxoff, uint32_t const* __restrict__ prev,
                     uint32_t const* __restrict__ spans, float4* edge32, uint32_t* slab_start,
                     uint32_t* slab_edges, float4* slab_e32, T* vert_x, float* vert_x32,
-                    float2* __restrict__ vxy32)
+                    float2* __restrict__ vxy32, float const* __restrict__ yslab)
 {
   __shared__ uint32_t cur[kMaxSlabs];
   __shared__ uint32_t shU[kIdxBlock / 32];
@@ -454,9 +454,15 @@ __global__ void __launch_bounds__(kIdxBlock)
                                            fmaxf(fabsf(ef.z), fabsf(ef.w))));
       }
       if (sp & kSpanSkip) continue;
+      float const fa = yslab[v], fb = yslab[pv];
+      float const flo = fminf(fa, fb), fhi = fmaxf(fa, fb);
       for (uint32_t j = span_j0(sp); j <= span_j1(sp); ++j) {
         uint32_t const k = eb + atomicAdd(&cur[j], 1u);
-        slab_edges[k]    = v;
+        // bit 31: the edge crosses the whole slab (ends more than 1/16 slab
+        // beyond it), used by the float32 ordering pass
+        bool const crossing = flo < static_cast<float>(j) - 0.0625f &&
+                              fhi > static_cast<float>(j) + 1.0625f;
+        slab_edges[k]       = v | (crossing ? kEntryCrossing : 0u);
         if (float32) slab_e32[k] = ef;
       }
       if (sp & kSpanVertical) {
@@ -484,6 +490,164 @@ __global__ void __launch_bounds__(kIdxBlock)
           vert_x32[vbase + i] = static_cast<float>(vert_x[vbase + i] - cx);
     }
     __syncthreads();
+  }
+}
+
+// Pass 3 (float32 index): within each slab, the edges that cross the whole
+// slab (both ends more than 1/16 slab beyond it) come first, sorted left to
+// right by their x at the slab's middle; the edges ending inside the slab
+// follow.  Per slab and x-bin (kSlabBins bins across the polygon box) a
+// record gives the window [lo, hi) of crossing edges to test: the crossing
+// edges before lo end more than 1/16 bin left of the bin (certainly left of
+// any point of the bin), those from hi on start more than 1/16 bin right of
+// it (certainly right: each one toggles, so their count's parity is stored).
+// The runs are found on the sorted order itself, so the records are valid
+// whatever the order; the sort only makes the windows short.  Slabs with more
+// than kSortSlab entries get an empty crossing set (every edge is tested).
+constexpr int kSortSlab = 64;
+
+__device__ inline uint32_t warp_min_u32(uint32_t v)
+{
+  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+  return v;
+}
+__device__ inline uint32_t warp_max_u32(uint32_t v)
+{
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+  return v;
+}
+
+// One warp per slab; lane l holds entries l and l + 32 (kSortSlab = 64).
+__global__ void __launch_bounds__(kIdxBlock)
+  slab_order_kernel(size_t np, uint32_t const* __restrict__ nslab,
+                    uint32_t const* __restrict__ slab_base, uint32_t const* __restrict__ slab_start,
+                    uint8_t const* __restrict__ exact, float4 const* __restrict__ box32,
+                    uint32_t const* __restrict__ in_edges, float4 const* __restrict__ in_e32,
+                    uint32_t* __restrict__ out_edges, float4* __restrict__ out_e32,
+                    uint32_t* __restrict__ nfull_out, uint32_t* __restrict__ bins_out,
+                    float* __restrict__ inv_bin_w)
+{
+  constexpr int kWarps = kIdxBlock / 32;
+  __shared__ float2 sx[kWarps][kSortSlab];  // (x_min, x_max) of the crossing entries by rank
+  int const lane = threadIdx.x & 31;
+  int const warp = threadIdx.x >> 5;
+  for (size_t p = blockIdx.x; p < np; p += gridDim.x) {
+    uint32_t const ns = nslab[p], sb = slab_base[p];
+    float4 const bx   = box32[p];
+    float const width = bx.z - bx.x;
+    bool const binned = !exact[p] && width > 0.0f && isfinite(width);
+    float const invw  = binned ? static_cast<float>(kSlabBins) / width : 0.0f;
+    float const w     = binned ? width / static_cast<float>(kSlabBins) : 0.0f;
+    float const hstep = (bx.w - bx.y) / static_cast<float>(ns);
+    if (threadIdx.x == 0) inv_bin_w[p] = invw;
+    for (uint32_t j = warp; j < ns; j += kWarps) {
+      uint32_t const sidx = sb + j;
+      uint32_t const e0 = slab_start[sidx], e1 = slab_start[sidx + 1];
+      uint32_t const n  = e1 - e0;
+      if (!binned || n > static_cast<uint32_t>(kSortSlab) || n < 2) {
+        // every entry is tested: copy, no crossing set
+        for (uint32_t k = lane; k < n; k += 32) {
+          out_edges[e0 + k] = in_edges[e0 + k];
+          out_e32[e0 + k]   = in_e32[e0 + k];
+        }
+        if (lane < kSlabBins) bins_out[static_cast<size_t>(sidx) * kSlabBins + lane] = 0u;
+        if (lane == 0) nfull_out[sidx] = 0;
+        continue;
+      }
+      int const halves = n > 32u ? 2 : 1;
+      float const ymid = bx.y + (static_cast<float>(j) + 0.5f) * hstep;
+      uint32_t ev[2] = {0u, 0u};
+      float4 ee[2];
+      bool cross[2] = {false, false};
+      float key[2]  = {0.0f, 0.0f};
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        uint32_t const k = lane + 32u * h;
+        ee[h]            = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (h < halves && k < n) {
+          ev[h]          = in_edges[e0 + k];
+          ee[h]          = in_e32[e0 + k];
+          cross[h]       = (ev[h] & kEntryCrossing) != 0u;
+          float const t  = (ymid - ee[h].y) / (ee[h].w - ee[h].y);
+          float const tc = t > 0.0f ? (t < 1.0f ? t : 1.0f) : 0.0f;
+          float const km = ee[h].x + tc * (ee[h].z - ee[h].x);
+          key[h]         = km == km ? km : 0.0f;  // ranks need a total order
+        }
+      }
+      unsigned const c0 = __ballot_sync(0xFFFFFFFFu, cross[0]);
+      unsigned const c1 = __ballot_sync(0xFFFFFFFFu, cross[1]);
+      uint32_t const nf = __popc(c0) + __popc(c1);
+      // crossing entries ranked by (key, entry index); the other entries
+      // follow them in their original order
+      unsigned const valid0 = n >= 32u ? 0xFFFFFFFFu : ((1u << n) - 1u);
+      unsigned const valid1 = n >= 64u ? 0xFFFFFFFFu : (n > 32u ? ((1u << (n - 32u)) - 1u) : 0u);
+      unsigned const part0  = valid0 & ~c0, part1 = valid1 & ~c1;
+      unsigned const lt     = (1u << lane) - 1u;
+      uint32_t rank[2]      = {nf + __popc(part0 & lt), nf + __popc(part0) + __popc(part1 & lt)};
+      if (nf) {
+        for (int h = 0; h < halves; ++h) {
+          uint32_t const k = lane + 32u * h;
+          uint32_t r       = 0;
+          for (int src = 0; src < static_cast<int>(n); ++src) {
+            int const sl      = src & 31, sh = src >> 5;
+            float const okey  = __shfl_sync(0xFFFFFFFFu, sh ? key[1] : key[0], sl);
+            bool const ocross = ((sh ? c1 : c0) >> sl) & 1u;
+            r += (ocross &&
+                  (okey < key[h] || (okey == key[h] && static_cast<uint32_t>(src) < k)))
+                   ? 1u
+                   : 0u;
+          }
+          if (cross[h]) {
+            rank[h]             = r;
+            sx[warp][r]         = make_float2(fminf(ee[h].x, ee[h].z), fmaxf(ee[h].x, ee[h].z));
+          }
+        }
+      }
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        uint32_t const k = lane + 32u * h;
+        if (h < halves && k < n) {
+          out_edges[e0 + rank[h]] = ev[h];
+          out_e32[e0 + rank[h]]   = ee[h];
+        }
+      }
+      if (lane == 0) nfull_out[sidx] = nf;
+      if (nf == 0) {
+        if (lane < kSlabBins) bins_out[static_cast<size_t>(sidx) * kSlabBins + lane] = 0u;
+        continue;
+      }
+      __syncwarp();
+      // sorted crossing entries: lane i holds ranks i and i + 32
+      float2 const s0 = lane < static_cast<int>(nf) ? sx[warp][lane] : make_float2(0.0f, 0.0f);
+      float2 const s1 =
+        lane + 32 < static_cast<int>(nf) ? sx[warp][lane + 32] : make_float2(0.0f, 0.0f);
+      unsigned const in0 = nf >= 32u ? 0xFFFFFFFFu : ((1u << nf) - 1u);
+      unsigned const in1 = nf >= 64u ? 0xFFFFFFFFu : (nf > 32u ? ((1u << (nf - 32u)) - 1u) : 0u);
+      uint32_t rec = 0;
+      for (int b = 0; b < kSlabBins; ++b) {
+        float const blo = bx.x + static_cast<float>(b) * w - 0.0625f * w;
+        float const bhi = bx.x + static_cast<float>(b + 1) * w + 0.0625f * w;
+        // leading run of certainly-left entries, trailing run of certainly-right ones
+        unsigned const l0 = __ballot_sync(0xFFFFFFFFu, s0.y < blo) & in0;
+        unsigned const l1 = __ballot_sync(0xFFFFFFFFu, s1.y < blo) & in1;
+        unsigned const r0 = __ballot_sync(0xFFFFFFFFu, s0.x > bhi) & in0;
+        unsigned const r1 = __ballot_sync(0xFFFFFFFFu, s1.x > bhi) & in1;
+        // lo: length of the run of ones from rank 0 (never past nf: bits
+        // from nf on are zero unless nf = 64)
+        unsigned long long const ll = (static_cast<unsigned long long>(l1) << 32) | l0;
+        uint32_t const lo          = ~ll ? static_cast<uint32_t>(__ffsll(~ll) - 1) : 64u;
+        // hi: one past the last rank that is not certainly right
+        unsigned long long const rr = (static_cast<unsigned long long>(r1) << 32) | r0;
+        unsigned long long const valid =
+          nf >= 64u ? ~0ull : ((1ull << nf) - 1ull);
+        unsigned long long const notr = ~rr & valid;  // entries that are not certainly right
+        uint32_t hi = notr ? 64u - static_cast<uint32_t>(__clzll(notr)) : 0u;
+        if (hi < lo) hi = lo;
+        if (lane == b) rec = lo | (hi << 15) | (((nf - hi) & 1u) << 30);
+      }
+      if (lane < kSlabBins) bins_out[static_cast<size_t>(sidx) * kSlabBins + lane] = rec;
+      __syncwarp();
+    }
   }
 }
 
@@ -531,12 +695,13 @@ __global__ void vert_end_kernel(uint32_t const* __restrict__ vbeg,
 template <typename T>
 PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro, size_t nro,
                               T const* vx, T const* vy, size_t nv, bool build_float32,
-                              Allocator const& alloc)
+                              Allocator const& alloc, bool order_slabs)
 {
   (void)nro;
   cudaStream_t const s = alloc.stream();
   KernelTimer timer("polygon_index", s);
   size_t const np = npo > 0 ? npo - 1 : 0;
+  CSPT_EXPECTS(nv < (size_t{1} << 31), "the polygon index takes fewer than 2^31 vertices");
   pminx_     = Buffer<T>(alloc, np);
   pminy_     = Buffer<T>(alloc, np);
   pmaxx_     = Buffer<T>(alloc, np);
@@ -601,7 +766,6 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
   if (build_float32) vert_x32_ = Buffer<float>(alloc, nvertical);
   if (nslabs_total == 0)
     CSPT_CUDA_TRY(cudaMemsetAsync(slab_start_.data(), 0, sizeof(uint32_t), s));
-  yslab.reset();
   Buffer<float2> vxy32(alloc, build_float32 ? nv : 0);
   if (np > 0) {
     index_fill_kernel<T><<<grd, kIdxBlock, 0, s>>>(
@@ -610,12 +774,30 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
       build_float32, ax_.data(), ay_.data(), aix_.data(), aiy_.data(), box32_.data(),
       invh32_.data(), maxoff_.data(), prev_.data(), spans.data(), edge32_.data(),
       slab_start_.data(),
-      slab_edges_.data(), slab_e32_.data(), vert_x_.data(), vert_x32_.data(), vxy32.data());
+      slab_edges_.data(), slab_e32_.data(), vert_x_.data(), vert_x32_.data(), vxy32.data(),
+      yslab.data());
     CSPT_CHECK_LAUNCH();
     vert_end_kernel<<<grid_for(np, 256, 152u * 16u), 256, 0, s>>>(vbeg_.data(), nvert.data(),
                                                                   np, vend_.data());
     CSPT_CHECK_LAUNCH();
   }
+  vxy32.reset();
+  bool const ordered = build_float32 && order_slabs;
+  slab_nfull_ = Buffer<uint32_t>(alloc, ordered ? nslabs_total : 0);
+  slab_bins_  = Buffer<uint32_t>(alloc, ordered ? nslabs_total * kSlabBins : 0);
+  invw32_     = Buffer<float>(alloc, ordered ? np : 0);
+  if (ordered && np > 0) {
+    Buffer<uint32_t> edges2(alloc, nentries);
+    Buffer<float4> e32b(alloc, nentries);
+    slab_order_kernel<<<grd, kIdxBlock, 0, s>>>(
+      np, nslab_.data(), slab_base_.data(), slab_start_.data(), exact_.data(), box32_.data(),
+      slab_edges_.data(), slab_e32_.data(), edges2.data(),
+      e32b.data(), slab_nfull_.data(), slab_bins_.data(), invw32_.data());
+    CSPT_CHECK_LAUNCH();
+    slab_edges_ = std::move(edges2);
+    slab_e32_   = std::move(e32b);
+  }
+  yslab.reset();
   v_ = PolygonIndexView<T>{po,
                            ro,
                            vx,
@@ -645,7 +827,10 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
                            slab_edges_.data(),
                            slab_e32_.data(),
                            prev_.data(),
-                           edge32_.data()};
+                           edge32_.data(),
+                           slab_nfull_.data(),
+                           slab_bins_.data(),
+                           invw32_.data()};
 }
 
 template class PolygonIndex<float>;

@@ -41,6 +41,13 @@
 
 namespace cspt {
 
+// x-bins per slab of the float32 index (window records per slab)
+constexpr int kSlabBins = 8;
+// slab entries: vertex id in bits 0-30, bit 31 set when the edge crosses the
+// whole slab (float32 index)
+constexpr uint32_t kEntryCrossing = 1u << 31;
+constexpr uint32_t kEntryVertex   = kEntryCrossing - 1u;
+
 template <typename T>
 struct PolygonIndexView {
   // polygon topology (caller's arrays)
@@ -72,19 +79,30 @@ struct PolygonIndexView {
   float const* vert_x32;
   // per slab: entries [slab_start[s], slab_start[s+1])
   uint32_t const* slab_start;
-  uint32_t const* slab_edges;  // vertex index of the edge's end point
+  uint32_t const* slab_edges;  // vertex index of the edge's end point | kEntryCrossing
   float4 const* slab_e32;      // the entry's edge (ax, ay, bx, by) as float32 offsets
   // per vertex
   uint32_t const* prev_vertex;
   float4 const* edge32;        // (ax, ay, bx, by) offsets from the anchor
+  // float32 index: per slab, the entries crossing the whole slab come first
+  // (sorted left to right); per (slab, x-bin) a window record
+  // lo | hi << 15 | parity << 30 (see slab_order_kernel)
+  uint32_t const* slab_nfull;  // null: slabs not ordered
+  uint32_t const* slab_bins;
+  float const* inv_bin_w32;    // x-bins per unit of x (0: no bins)
 };
 
 template <typename T>
 class PolygonIndex {
  public:
+  // order_slabs (float32 index only): sort each slab's crossing edges and
+  // build the per-(slab, x-bin) windows.  It costs a pass over all slab
+  // entries and pays off where the index is evaluated many times (batched
+  // plans, resident polygon sets).
   PolygonIndex(uint32_t const* poly_offsets, size_t num_poly_offsets,
                uint32_t const* ring_offsets, size_t num_ring_offsets, T const* vx, T const* vy,
-               size_t num_vertices, bool build_float32, Allocator const& alloc);
+               size_t num_vertices, bool build_float32, Allocator const& alloc,
+               bool order_slabs = false);
   PolygonIndexView<T> view() const { return v_; }
 
  private:
@@ -94,6 +112,8 @@ class PolygonIndex {
   Buffer<uint32_t> nslab_, slab_base_, vbeg_, vend_, slab_start_, slab_edges_, prev_;
   Buffer<uint8_t> exact_;
   Buffer<float4> edge32_, box32_, slab_e32_;
+  Buffer<uint32_t> slab_nfull_, slab_bins_;
+  Buffer<float> invw32_;
   PolygonIndexView<T> v_{};
 };
 

@@ -317,7 +317,7 @@ class PolygonSet {
                            CSPT_FLOAT64, 0.0, bminx_.data(), bminy_.data(), bmaxx_.data(),
                            bmaxy_.data(), a);
     index_.reset(new PolygonIndex<double>(po_.data(), npo, ro_.data(), nro, vx_.data(),
-                                          vy_.data(), nv, true, a));
+                                          vy_.data(), nv, true, a, /*order_slabs=*/true));
     // cell grid over the boxes
     Buffer<double> dom(a, 4);
     domain_kernel<<<1, 1024, 0, s>>>(bminx_.data(), bminy_.data(), bmaxx_.data(),
