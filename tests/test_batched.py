@@ -193,3 +193,45 @@ def test_batched_validation():
     with pytest.raises(TypeError):
         BatchedPointInPolygon(x.float(), y.float(), wl.point_offsets, _polygons(wl),
                               wl.polygon_offsets, params)
+
+
+@pytest.mark.parametrize("method", ["exact", "filtered"])
+def test_batched_boundary_points(method):
+    """Points on polygon vertices and within 1e-9 of edges (half of them),
+    through the ordered-slab index of the batched plan."""
+    wl = D.batched_instances(12, points_range=(2000, 8000), polygons_range=(20, 120),
+                             side_range=(200.0, 2000.0), vertices_range=(8, 200),
+                             seed_offset=7)
+    rng = np.random.default_rng(11)
+    P = wl.polygons
+    x, y = wl.x.copy(), wl.y.copy()
+    po = wl.point_offsets.astype(np.int64)
+    qo = wl.polygon_offsets.astype(np.int64)
+    for i in range(wl.num_instances):
+        a, b = po[i], po[i + 1]
+        r0, r1 = int(P.part_offset[qo[i]]), int(P.part_offset[qo[i + 1]])
+        sub = D.Polygons(P.x, P.y, P.ring_offset[r0:r1 + 1], P.part_offset, P.geometry_offset)
+        k = (b - a) // 2
+        bx, by = D._near_boundary(rng, sub, k)
+        sel = rng.choice(np.arange(a, b), k, replace=False)
+        x[sel], y[sel] = bx, by
+    wl.x, wl.y = x, y
+    params = autotune_free_params(wl)
+    plan = BatchedPointInPolygon(torch.from_numpy(wl.x).cuda(), torch.from_numpy(wl.y).cuda(),
+                                 wl.point_offsets, _polygons(wl), wl.polygon_offsets, params,
+                                 method=method)
+    plan.run(graph=True)
+    torch.cuda.synchronize()
+    # against the plain float64 single-instance calls, whatever the method
+    out = _check_plan(plan, wl, params, "exact")
+    assert sum(len(o[2][0]) for o in out if o is not None) > 5000
+    plan.close()
+
+
+def autotune_free_params(wl):
+    params = []
+    for i in range(wl.num_instances):
+        x0, x1, y0, y1 = wl.boxes[i]
+        params.append(dict(x_min=x0, x_max=x1, y_min=y0, y_max=y1,
+                           scale=max(x1 - x0, y1 - y0) / 64.0, max_depth=6, max_size=40))
+    return params
