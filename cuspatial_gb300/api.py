@@ -43,15 +43,6 @@ def _tree_struct(quadtree):
     return st, keep
 
 
-def _u32(t):
-    """uint32 data carried in an int32 tensor (torch has limited uint32 ops)."""
-    return as_device_tensor(t).to(torch.int32) if t.dtype not in (torch.int32,) else t
-
-
-def _adopt_u32(alloc, p, n):
-    return alloc.adopt(p, n, torch.int32)
-
-
 def quadtree_on_points(points: GeoSeries, x_min, x_max, y_min, y_max, scale, max_depth,
                        max_size):
     """Construct a quadtree on points (reference: core/spatial/indexing.py:15).

@@ -23,14 +23,15 @@
 //      no toggle, result false.
 //   4. An edge toggles only if its y-range contains py; a non-vertical edge
 //      can be "collinear and within x-range" only if py lies within
-//      2^-48 * |rise| of its y-range.  The slab margin (2^-36 of the edge
-//      height plus 2^-40 of the polygon height, the latter also absorbing
-//      the slab-index rounding) covers both.
+//      2^-48 * |rise| of its y-range.  Each edge is binned over its y-range
+//      widened by 2^-36 of its height, which covers both.
 //   5. An exactly vertical edge reports "on edge" for any py whenever
 //      px == its x (x-range check only, is_point_in_polygon.cuh:75-83); that
 //      case is caught by a lookup in the sorted vertical-x list.
-//   6. Slabs are also widened by 1/64 of a slab so that a float32 evaluation
-//      of the slab index (error below 1e-3 slab) still finds every edge.
+//   6. Slab coordinates are float32 roundings of the float64 (y - ymin) *
+//      inv_h (2.5e-4 slab at most); edges are further widened by 1/32 of a
+//      slab, which covers that and the float32 slab lookup of the filter
+//      (below 1e-2 slab under its guard), so every lookup finds every edge.
 //
 // Anchors lie on a power-of-two grid (2^(e-22) for coordinates below 2^e), so
 // the offset between a polygon anchor and a leaf anchor on the same grid is

@@ -1,7 +1,6 @@
 """The C-ABI library builds for sm_103a, loads without a GPU and exports every
 function include/cuspatial_gb300.h declares (no compute calls here)."""
 
-import ctypes
 import os
 import re
 

@@ -4,7 +4,6 @@ concurrent requests; admission by memory budget and per-request failures."""
 
 import numpy as np
 import pytest
-import torch
 
 import cuspatial_gb300 as cs
 from cuspatial_gb300 import datasets as D
