@@ -46,17 +46,22 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="target CPU time of the oracle baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", choices=["precision", "batched", "serving", "nearest"],
+    ap.add_argument("--workload", choices=["precision", "batched", "serving", "nearest",
+                                           "unindexed"],
                     default="precision",
                     help="precision: the 100M-point join (default line); batched: 4096 "
                          "independent instances through the batched plan; serving: Poisson "
                          "requests against a resident 250k-polygon set; nearest: 50M points "
-                         "to 200k linestrings")
+                         "to 200k linestrings; unindexed: 10M points against 31 polygons "
+                         "without an index (the reference's point_in_polygon benchmark)")
     ap.add_argument("--requests", type=int, default=4000)
     ap.add_argument("--rate", type=float, default=2000.0)
     ap.add_argument("--streams", type=int, default=4)
     ap.add_argument("--nearest-points", type=int, default=50_000_000)
     ap.add_argument("--instances", type=int, default=4096)
+    ap.add_argument("--sides", type=int, default=100,
+                    help="polygon sides of the unindexed workload (reference: 4, 10, 100)")
+    ap.add_argument("--unindexed-points", type=int, default=10_000_000)
     ap.add_argument("--single-sample", type=int, default=64,
                     help="instances timed through the single-instance calls (batched)")
     return ap.parse_args()
@@ -911,6 +916,135 @@ def run_nearest(args, dist):
         print(json.dumps(line), flush=True)
 
 
+def run_unindexed(args, dist):
+    """The reference's point_in_polygon benchmark shape
+    (cpp/benchmarks/point_in_polygon/point_in_polygon.cu): 10,000,000 points
+    uniform in [-20,20]^2 against 31 regular polygons of 100 sides, radius 10,
+    all centred on the origin; float64.  A step is one point_in_polygon call
+    (polygon index + one thread per point through all 31 polygons); value is
+    points per second.  e2e adds the host->device copies of the points and
+    polygons and the device->host copy of the int32 bitmask."""
+    import torch
+
+    import cuspatial_gb300 as cs
+    from cuspatial_gb300 import _lib, datasets
+    from oracle import oracle as O
+
+    torch.cuda.set_device(dist.local)
+    dist.init("nccl")
+    lib = _lib.load()
+    lib.cspt_launch_count.restype = ctypes.c_uint64
+    lib.cspt_profile_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(ctypes.c_uint64)]
+    lib.cspt_profile_enable.argtypes = [ctypes.c_int]
+    w = datasets.unindexed_pip(n_points=args.unindexed_points, sides=args.sides)
+    P = w.polygons
+    n = len(w.x)
+    pts = cs.GeoSeries.from_points(w.x, w.y)
+    polys = cs.GeoSeries.from_polygons_xy(polygons_xy(P), P.ring_offset, P.part_offset,
+                                          P.geometry_offset)
+    stream = torch.cuda.current_stream()
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def timed(method, steps):
+        for _ in range(args.warmup):
+            cs.point_in_polygon_bitmask(pts, polys, method)
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(steps):
+            a, b = ev(), ev()
+            a.record(stream)
+            r = cs.point_in_polygon_bitmask(pts, polys, method)
+            b.record(stream)
+            times.append((a, b))
+        torch.cuda.synchronize()
+        return r, [x.elapsed_time(y) for x, y in times]
+
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    l0 = lib.cspt_launch_count()
+    lib.cspt_profile_enable(1)
+    res, ms = timed(args.method, args.steps)
+    lib.cspt_profile_enable(0)
+    launches = int(lib.cspt_launch_count() - l0)
+    clock_info = clocks.stop()
+    refined = cs.last_refined_count()
+    kern = {}
+    for name in ("points_pip", "polygon_index"):
+        t, c = ctypes.c_double(), ctypes.c_uint64()
+        lib.cspt_profile_read(name.encode(), ctypes.byref(t), ctypes.byref(c))
+        kern[name] = t.value / max(c.value, 1)
+    f_ms = dist.max(statistics.mean(ms))
+    ex_res, ex_ms = timed("exact", max(1, args.plain_steps))
+    same = bool(torch.equal(res, ex_res))
+
+    # e2e from pinned host buffers
+    hx = torch.from_numpy(w.x).pin_memory()
+    hy = torch.from_numpy(w.y).pin_memory()
+    hpxy = torch.from_numpy(polygons_xy(P)).pin_memory()
+    hoff = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+            for a in (P.ring_offset, P.part_offset, P.geometry_offset)]
+    hout = torch.empty(n, dtype=torch.int32).pin_memory()
+    h2d = n * 16 + hpxy.numel() * 8 + sum(a.numel() * 4 for a in hoff)
+    e2e = []
+    for i in range(args.warmup + args.e2e_steps):
+        a, b = ev(), ev()
+        a.record(stream)
+        dx = hx.to("cuda", non_blocking=True)
+        dy = hy.to("cuda", non_blocking=True)
+        dxy = hpxy.to("cuda", non_blocking=True)
+        doff = [t.to("cuda", non_blocking=True) for t in hoff]
+        p2 = cs.GeoSeries.from_points(dx, dy)
+        g2 = cs.GeoSeries.from_polygons_xy(dxy, *doff)
+        m = cs.point_in_polygon_bitmask(p2, g2, args.method)
+        hout.copy_(m, non_blocking=True)
+        b.record(stream)
+        b.synchronize()
+        if i >= args.warmup:
+            e2e.append(a.elapsed_time(b))
+    e2e_ms = dist.max(statistics.mean(e2e))
+    e2e_same = bool(torch.equal(hout, res.cpu()))
+
+    # parity of a sample against the oracle, and the CPU baseline on it
+    k = min(n, 200_000)
+    t0 = time.time()
+    want = O.point_in_polygon(w.x[:k], w.y[:k], P.part_offset, P.ring_offset, P.x, P.y)
+    cpu_s = time.time() - t0
+    parity = bool(np.array_equal(res[:k].cpu().numpy(), want))
+    algo_bytes = n * (16 + 4) + len(P.x) * 16
+    hbm, hbm_kind = measured_peak_hbm()
+    pip_ms = kern["points_pip"]
+    line = {
+        "metric": "point_in_polygon points/s (31 polygons, unindexed)", "workload": "unindexed",
+        "value": n * args.gpus / (f_ms / 1e3), "unit": "points/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": f_ms,
+        "p50_ms": percentile(ms, 0.5), "p99_ms": percentile(ms, 0.99),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded numpy PCG64; the reference benchmark's shapes)",
+        "config": {"workload": "point_in_polygon: %d points uniform in [-20,20]^2, 31 regular "
+                               "%d-gons of radius 10 at the origin" % (n, args.sides),
+                   "points": n, "polygons": 31, "sides": args.sides, "method": args.method,
+                   "l2": "inputs (%.0f MB) larger than L2" % (n * 16 / 1e6)},
+        "kernels_ms": kern, "exact_ms_per_step": statistics.mean(ex_ms),
+        "filtered_equals_exact": same, "refined_tests": refined,
+        "oracle_sample_identical": parity,
+        "e2e": {"value": n * args.gpus / (e2e_ms / 1e3), "unit": "points/s",
+                "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": n * 4, "result_identical": e2e_same},
+        "roofline": {"bound": "hbm", "achieved": algo_bytes / (pip_ms / 1e3) / 1e9,
+                     "peak": hbm, "unit": "GB/s",
+                     "frac": algo_bytes / (pip_ms / 1e3) / 1e9 / hbm if hbm else None,
+                     "traffic": None,
+                     "peak_kind": hbm_kind,
+                     "note": "points_pip kernel: 16 B read + 4 B written per point"},
+        "cpu_baseline": {"value": k / cpu_s, "unit": "points/s", "cores": 1, "kind": "port",
+                         "sample": "first %d points, all 31 polygons" % k},
+        "gpu_launches": launches, "clocks": clock_info,
+    }
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     dist = Dist()
@@ -922,6 +1056,8 @@ def main():
         run_serving(args, dist)
     elif args.workload == "nearest":
         run_nearest(args, dist)
+    elif args.workload == "unindexed":
+        run_unindexed(args, dist)
     else:
         run_ours(args, dist)
 

@@ -2,12 +2,14 @@
 
 Functions mirror cuspatial.quadtree_on_points, polygon_bounding_boxes,
 linestring_bounding_boxes, join_quadtree_and_bounding_boxes,
-quadtree_point_in_polygon and quadtree_point_to_nearest_linestring; they run
+quadtree_point_in_polygon and quadtree_point_to_nearest_linestring, and the
+unindexed point_in_polygon / pairwise_point_in_polygon; they run
 hand-written CUDA kernels in libcuspatial_gb300.so through its C ABI.
 """
 
 from .api import (join_quadtree_and_bounding_boxes, last_refined_count,
-                  linestring_bounding_boxes, polygon_bounding_boxes, quadtree_on_points,
+                  linestring_bounding_boxes, pairwise_point_in_polygon, point_in_polygon,
+                  point_in_polygon_bitmask, polygon_bounding_boxes, quadtree_on_points,
                   quadtree_point_in_polygon, quadtree_point_to_nearest_linestring)
 from .geoseries import GeoSeries, Table
 
@@ -17,6 +19,9 @@ __all__ = [
     "join_quadtree_and_bounding_boxes",
     "last_refined_count",
     "linestring_bounding_boxes",
+    "pairwise_point_in_polygon",
+    "point_in_polygon",
+    "point_in_polygon_bitmask",
     "polygon_bounding_boxes",
     "quadtree_on_points",
     "quadtree_point_in_polygon",

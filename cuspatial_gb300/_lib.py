@@ -109,6 +109,10 @@ def _declare(lib):
         _vp, _vp, _sz, ctypes.POINTER(CsptQuadtree), _vp, _sz, _vp, _vp, _sz, _vp, _sz, _vp, _vp,
         _sz, ctypes.c_int, ctypes.c_int, ctypes.POINTER(CsptAllocator), _vp, _vp, _vp, _vp,
         ctypes.POINTER(_sz)]
+    for name in ("cspt_point_in_polygon", "cspt_pairwise_point_in_polygon"):
+        getattr(lib, name).argtypes = [
+            _vp, _vp, _sz, _vp, _sz, _vp, _sz, _vp, _vp, _sz, ctypes.c_int, ctypes.c_int,
+            ctypes.POINTER(CsptAllocator), _vp, _vp]
     _u64p = ctypes.POINTER(ctypes.c_uint64)
     lib.cspt_batched_pip_plan.argtypes = [
         _sz, _u64p, _vp, _vp, _u64p, _vp, _sz, _vp, _sz, _vp, _vp, _sz,

@@ -232,6 +232,73 @@ def quadtree_point_to_nearest_linestring(linestring_quad_pairs, quadtree, point_
     return out
 
 
+def _single_polygons(polygons):
+    poly = polygons.polygons
+    # the C++ API takes single polygons only (join.py:69-74)
+    if int(poly.part_offset.numel()) != int(poly.geometry_offset.numel()):
+        raise ValueError("GeoSeries cannot contain multipolygon.")
+    return poly
+
+
+def point_in_polygon(points: GeoSeries, polygons: GeoSeries, method="exact"):
+    """Which points fall in which of at most 31 polygons (join.py:23-102).
+
+    Returns a Table with one bool column per polygon, named by the polygon's
+    position (the reference names them by the GeoSeries index, 0..n-1 by
+    default); an empty Table when there are no polygons.
+    """
+    if len(polygons) == 0:
+        return Table()
+    if not contains_only_points(points):
+        raise ValueError("`point` Geoseries must contains only point geometries.")
+    if not contains_only_polygons(polygons):
+        raise ValueError("`polygons` Geoseries must contains only polygons geometries.")
+    poly = _single_polygons(polygons)
+    mask = point_in_polygon_bitmask(points, polygons, method)
+    out = Table()
+    for p in range(int(poly.part_offset.numel()) - 1):
+        out[p] = ((mask >> p) & 1).bool()
+    return out
+
+
+def point_in_polygon_bitmask(points: GeoSeries, polygons: GeoSeries, method="exact"):
+    """The C++ API's int32 column (point_in_polygon.hpp:75): bit p of row i
+    is point i inside polygon p."""
+    poly = polygons.polygons
+    pts = points.points
+    n = int(pts.x.numel())
+    mask = torch.empty(n, dtype=torch.int32, device=pts.x.device)
+    lib = _lib.load()
+    alloc = _lib.TorchAllocator(pts.x.device)
+    _lib.check(lib.cspt_point_in_polygon(
+        _lib.ptr(pts.x), _lib.ptr(pts.y), n, _lib.ptr(poly.part_offset),
+        int(poly.part_offset.numel()), _lib.ptr(poly.ring_offset), int(poly.ring_offset.numel()),
+        _lib.ptr(poly.x), _lib.ptr(poly.y), int(poly.x.numel()), _dtype_code(pts.x),
+        _METHODS[method], alloc.ref, _lib.stream_ptr(), _lib.ptr(mask)), lib)
+    return mask
+
+
+def pairwise_point_in_polygon(points: GeoSeries, polygons: GeoSeries, method="exact"):
+    """Point i against polygon i (point_in_polygon.hpp:124; the binding
+    used by core/binpreds/contains.py:146): a uint8 column, 1 inside."""
+    if not contains_only_points(points):
+        raise ValueError("`point` Geoseries must contains only point geometries.")
+    if not contains_only_polygons(polygons):
+        raise ValueError("`polygons` Geoseries must contains only polygons geometries.")
+    poly = _single_polygons(polygons)
+    lib = _lib.load()
+    pts = points.points
+    n = int(pts.x.numel())
+    out = torch.empty(n, dtype=torch.uint8, device=pts.x.device)
+    alloc = _lib.TorchAllocator(pts.x.device)
+    _lib.check(lib.cspt_pairwise_point_in_polygon(
+        _lib.ptr(pts.x), _lib.ptr(pts.y), n, _lib.ptr(poly.part_offset),
+        int(poly.part_offset.numel()), _lib.ptr(poly.ring_offset), int(poly.ring_offset.numel()),
+        _lib.ptr(poly.x), _lib.ptr(poly.y), int(poly.x.numel()), _dtype_code(pts.x),
+        _METHODS[method], alloc.ref, _lib.stream_ptr(), _lib.ptr(out)), lib)
+    return out
+
+
 def last_refined_count():
     """Candidates re-evaluated in float64 by the last filtered PiP call."""
     return int(_lib.load().cspt_last_refined_count())

@@ -42,6 +42,14 @@ void quadtree_point_to_nearest_linestring(uint32_t const* pair_ls, uint32_t cons
                                           cspt_dtype dtype, cspt_method method,
                                           Allocator const& alloc, uint32_t* opt, uint32_t* ols,
                                           void* od);
+void point_in_polygon(void const* x, void const* y, size_t n, uint32_t const* po, size_t npo,
+                      uint32_t const* ro, size_t nro, void const* vx, void const* vy, size_t nv,
+                      cspt_dtype dtype, cspt_method method, Allocator const& alloc, int32_t* out,
+                      uint64_t* out_refined);
+void pairwise_point_in_polygon(void const* x, void const* y, size_t n, uint32_t const* po,
+                               uint32_t const* ro, void const* vx, void const* vy, size_t nv,
+                               cspt_dtype dtype, cspt_method method, Allocator const& alloc,
+                               uint8_t* out, uint64_t* out_refined);
 
 namespace {
 thread_local std::string t_last_error;
@@ -351,6 +359,68 @@ cspt_status cspt_quadtree_point_to_nearest_linestring(
                                          dtype, method, alloc, out_point_index,
                                          out_linestring_index, out_distance);
     *out_num_rows = num_point_indices;
+  });
+}
+
+cspt_status cspt_point_in_polygon(const void* x, const void* y, size_t num_points,
+                                  const uint32_t* poly_offsets, size_t num_poly_offsets,
+                                  const uint32_t* ring_offsets, size_t num_ring_offsets,
+                                  const void* poly_x, const void* poly_y,
+                                  size_t num_poly_vertices, cspt_dtype dtype, cspt_method method,
+                                  const cspt_allocator* mr, void* stream, int32_t* out)
+{
+  return guarded([&] {
+    t_last_refined = 0;
+    check_dtype(dtype);
+    CSPT_EXPECTS(method == CSPT_METHOD_EXACT || method == CSPT_METHOD_FILTERED,
+                 "unknown point-in-polygon method");
+    // point_in_polygon.cu:64-66: an empty point column returns before the
+    // polygon count is checked
+    if (num_points == 0) return;
+    size_t const npoly = num_poly_offsets > 0 ? num_poly_offsets - 1 : 0;
+    // detail/point_in_polygon.cuh:93-94
+    CSPT_EXPECTS(npoly <= 31, "Number of polygons cannot exceed 31");
+    CSPT_EXPECTS(out, "output pointers must not be null");
+    Allocator alloc(mr, as_stream(stream));
+    if (npoly == 0) {
+      CSPT_CUDA_TRY(cudaMemsetAsync(out, 0, num_points * sizeof(int32_t), as_stream(stream)));
+      return;
+    }
+    CSPT_EXPECTS(num_ring_offsets > 0,
+                 "Polygon ring offsets must contain at least one (1) value");
+    uint64_t refined = 0;
+    point_in_polygon(x, y, num_points, poly_offsets, num_poly_offsets, ring_offsets,
+                     num_ring_offsets, poly_x, poly_y, num_poly_vertices, dtype, method, alloc,
+                     out, &refined);
+    t_last_refined = refined;
+  });
+}
+
+cspt_status cspt_pairwise_point_in_polygon(const void* x, const void* y, size_t num_points,
+                                           const uint32_t* poly_offsets, size_t num_poly_offsets,
+                                           const uint32_t* ring_offsets, size_t num_ring_offsets,
+                                           const void* poly_x, const void* poly_y,
+                                           size_t num_poly_vertices, cspt_dtype dtype,
+                                           cspt_method method, const cspt_allocator* mr,
+                                           void* stream, uint8_t* out)
+{
+  return guarded([&] {
+    t_last_refined = 0;
+    check_dtype(dtype);
+    CSPT_EXPECTS(method == CSPT_METHOD_EXACT || method == CSPT_METHOD_FILTERED,
+                 "unknown point-in-polygon method");
+    // point_in_polygon.cu:133-136
+    size_t const npoly = num_poly_offsets > 0 ? num_poly_offsets - 1 : 0;
+    CSPT_EXPECTS(num_points == npoly, "Must pass in the same number of points as polygons.");
+    if (num_points == 0) return;
+    CSPT_EXPECTS(out, "output pointers must not be null");
+    CSPT_EXPECTS(num_ring_offsets > 0,
+                 "Polygon ring offsets must contain at least one (1) value");
+    Allocator alloc(mr, as_stream(stream));
+    uint64_t refined = 0;
+    pairwise_point_in_polygon(x, y, num_points, poly_offsets, ring_offsets, poly_x, poly_y,
+                              num_poly_vertices, dtype, method, alloc, out, &refined);
+    t_last_refined = refined;
   });
 }
 

@@ -24,6 +24,13 @@ machine.  All sizes can be scaled down (same distributions) for tests.
   nearest_linestring   50,000,000 uniform points in [0,10000)^2, 200,000
                        random-walk linestrings (2-256 segments, step U[1,20],
                        heading change N(0, 0.3 rad)).
+  unindexed_pip        10,000,000 uniform points in [-20,20]^2 against 31
+                       regular polygons of 100 sides, radius 10, all centred
+                       on the origin (one closed ring each), as in the
+                       reference's point-in-polygon benchmark
+                       (cpp/benchmarks/point_in_polygon/point_in_polygon.cu).
+  pairwise_pip         one point per star polygon: 4-400 vertices, 10% with
+                       a hole, points inside, outside and on the boundary.
 """
 
 import math
@@ -320,3 +327,59 @@ def serving_requests(n_requests, points_range=(1, 100_000), extent=20000.0, seed
             kind = "cluster"
         out.append(Request(x, y, kind))
     return out
+
+
+@dataclass
+class PointsPolygons:
+    x: np.ndarray
+    y: np.ndarray
+    polygons: Polygons
+
+
+def regular_polygons(n_polygons, sides, radius=10.0, center=(0.0, 0.0)):
+    """n identical closed regular polygons (sides + 1 vertices per ring)."""
+    k = np.arange(sides + 1)
+    ang = 2.0 * math.pi * (k % sides) / sides
+    rx = center[0] + radius * np.cos(ang)
+    ry = center[1] + radius * np.sin(ang)
+    x = np.tile(rx, n_polygons)
+    y = np.tile(ry, n_polygons)
+    ring_offset = np.arange(n_polygons + 1, dtype=np.int32) * (sides + 1)
+    part_offset = np.arange(n_polygons + 1, dtype=np.int32)
+    return Polygons(x, y, ring_offset, part_offset, part_offset.copy())
+
+
+def unindexed_pip(n_points=10_000_000, n_polygons=31, sides=100, radius=10.0, seed_offset=0):
+    rng = np.random.Generator(np.random.PCG64(SEED + 7 + seed_offset))
+    x = rng.uniform(-2 * radius, 2 * radius, n_points)
+    y = rng.uniform(-2 * radius, 2 * radius, n_points)
+    return PointsPolygons(x, y, regular_polygons(n_polygons, sides, radius))
+
+
+def pairwise_pip(n=100_000, vertices_range=(4, 400), boundary_fraction=0.2, seed_offset=0):
+    """Point i paired with star polygon i: inside, outside or on the boundary."""
+    rng = np.random.Generator(np.random.PCG64(SEED + 8 + seed_offset))
+    centers = rng.uniform(-1000, 1000, (n, 2))
+    k = _log_uniform_int(rng, vertices_range[0], vertices_range[1], n)
+    polys = star_polygons(rng, centers, k, lambda g, pid: g.uniform(1, 20, len(pid)),
+                          hole_fraction=0.1)
+    # a point at a random offset from the centre, radius U[0, 25]
+    ang = rng.uniform(0, 2 * math.pi, n)
+    rad = rng.uniform(0, 25, n)
+    x = centers[:, 0] + rad * np.cos(ang)
+    y = centers[:, 1] + rad * np.sin(ang)
+    # some points moved onto a vertex or next to an edge of their own polygon
+    b = np.nonzero(rng.random(n) < boundary_fraction)[0]
+    if len(b):
+        ring = polys.part_offset[b]  # the outer ring of polygon b
+        rb = polys.ring_offset[ring].astype(np.int64)
+        rl = polys.ring_offset[ring + 1].astype(np.int64) - rb
+        j = rb + (rng.random(len(b)) * (rl - 1)).astype(np.int64)
+        t = np.where(rng.random(len(b)) < 0.5, 0.0, rng.random(len(b)))
+        dx, dy = polys.x[j + 1] - polys.x[j], polys.y[j + 1] - polys.y[j]
+        ln = np.hypot(dx, dy)
+        ln[ln == 0] = 1.0
+        off = np.where(t == 0.0, 0.0, rng.uniform(-1e-9, 1e-9, len(b)))
+        x[b] = polys.x[j] + t * dx - dy / ln * off
+        y[b] = polys.y[j] + t * dy + dx / ln * off
+    return PointsPolygons(x, y, polys)

@@ -211,6 +211,37 @@ cspt_status cspt_quadtree_point_to_nearest_linestring(
   uint32_t* out_point_index, uint32_t* out_linestring_index, void* out_distance,
   size_t* out_num_rows);
 
+/*
+ * Replaces cuspatial::point_in_polygon
+ * (cpp/include/cuspatial/point_in_polygon.hpp:75-82;
+ * cpp/src/point_in_polygon/point_in_polygon.cu:108-150).
+ * Every point against every polygon (at most 31): out[i] bit p is set when
+ * point i is inside polygon p.  out holds num_points int32 values (caller's
+ * device memory).  poly_offsets holds num_polygons + 1 ring offsets.
+ */
+cspt_status cspt_point_in_polygon(const void* x, const void* y, size_t num_points,
+                                  const uint32_t* poly_offsets, size_t num_poly_offsets,
+                                  const uint32_t* ring_offsets, size_t num_ring_offsets,
+                                  const void* poly_x, const void* poly_y,
+                                  size_t num_poly_vertices, cspt_dtype dtype, cspt_method method,
+                                  const cspt_allocator* mr, void* stream, int32_t* out);
+
+/*
+ * Replaces cuspatial::pairwise_point_in_polygon
+ * (cpp/include/cuspatial/point_in_polygon.hpp:124-131;
+ * cpp/src/point_in_polygon/point_in_polygon.cu:108-150 with pairwise).
+ * Point i against polygon i: out[i] = 1 inside, 0 outside (num_points
+ * uint8 values, caller's device memory); num_points must equal the number
+ * of polygons.
+ */
+cspt_status cspt_pairwise_point_in_polygon(const void* x, const void* y, size_t num_points,
+                                           const uint32_t* poly_offsets, size_t num_poly_offsets,
+                                           const uint32_t* ring_offsets, size_t num_ring_offsets,
+                                           const void* poly_x, const void* poly_y,
+                                           size_t num_poly_vertices, cspt_dtype dtype,
+                                           cspt_method method, const cspt_allocator* mr,
+                                           void* stream, uint8_t* out);
+
 /* ------------------------------------------------------------------------
  * Batched point-in-polygon join (no counterpart in the reference, which
  * joins one point set with one polygon set per call).

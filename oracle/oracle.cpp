@@ -787,6 +787,39 @@ int oracle_is_point_in_polygon(double px, double py, uint32_t const* ring_offset
            : 0;
 }
 
+// detail/point_in_polygon.cuh:41-66 (pip_functor) — bit p of out[i] is point i
+// inside polygon p, for at most 31 polygons; detail/point_in_polygon.cuh:
+// 112-140 — pairwise form, point i against polygon i.
+int oracle_point_in_polygon(void const* x, void const* y, size_t n, uint32_t const* poly_offsets,
+                            size_t npoly, uint32_t const* ring_offsets, void const* vx,
+                            void const* vy, int dtype, int pairwise, void* out)
+{
+  for (size_t i = 0; i < n; ++i) {
+    size_t const p0 = pairwise ? i : 0;
+    size_t const p1 = pairwise ? i + 1 : npoly;
+    int32_t mask    = 0;
+    for (size_t p = p0; p < p1; ++p) {
+      bool hit;
+      if (dtype == 1)
+        hit = is_point_in_polygon<double, uint32_t>(
+          static_cast<double const*>(x)[i], static_cast<double const*>(y)[i], ring_offsets,
+          poly_offsets[p], poly_offsets[p + 1], static_cast<double const*>(vx),
+          static_cast<double const*>(vy));
+      else
+        hit = is_point_in_polygon<float, uint32_t>(
+          static_cast<float const*>(x)[i], static_cast<float const*>(y)[i], ring_offsets,
+          poly_offsets[p], poly_offsets[p + 1], static_cast<float const*>(vx),
+          static_cast<float const*>(vy));
+      if (hit) mask |= pairwise ? 1 : (1 << p);
+    }
+    if (pairwise)
+      static_cast<uint8_t*>(out)[i] = static_cast<uint8_t>(mask);
+    else
+      static_cast<int32_t*>(out)[i] = mask;
+  }
+  return 0;
+}
+
 int oracle_quadtree_point_to_nearest_linestring(uint32_t const* pair_ls,
                                                 uint32_t const* pair_quad, size_t np,
                                                 uint32_t const* length, uint32_t const* offset,

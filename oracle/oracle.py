@@ -58,6 +58,8 @@ def _load():
         ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_sz)]
     lib.oracle_is_point_in_polygon.argtypes = [
         ctypes.c_double, ctypes.c_double, _vp, ctypes.c_int64, ctypes.c_int64, _vp, _vp]
+    lib.oracle_point_in_polygon.argtypes = [
+        _vp, _vp, _sz, _vp, _sz, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp]
     lib.oracle_quadtree_point_to_nearest_linestring.argtypes = [
         _vp, _vp, _sz, _vp, _vp, _vp, _sz, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp, _vp, _vp]
     _lib = lib
@@ -190,6 +192,27 @@ def is_point_in_polygon(px, py, ring_offsets, ring_begin, ring_end, vx, vy):
     vy = np.ascontiguousarray(vy, dtype=np.float64)
     return bool(lib.oracle_is_point_in_polygon(float(px), float(py), _ptr(ro), int(ring_begin),
                                                int(ring_end), _ptr(vx), _ptr(vy)))
+
+
+def point_in_polygon(x, y, poly_offsets, ring_offsets, px, py, pairwise=False):
+    """Unindexed test: int32 bitmask per point over all polygons (bit p =
+    inside polygon p), or with ``pairwise`` a uint8 per point for polygon i."""
+    lib = _load()
+    x = np.ascontiguousarray(x)
+    y = np.ascontiguousarray(y, dtype=x.dtype)
+    po = np.ascontiguousarray(poly_offsets, dtype=np.uint32)
+    ro = np.ascontiguousarray(ring_offsets, dtype=np.uint32)
+    px = np.ascontiguousarray(px, dtype=x.dtype)
+    py = np.ascontiguousarray(py, dtype=x.dtype)
+    npoly = max(po.size - 1, 0)
+    if pairwise:
+        assert x.size == npoly
+    else:
+        assert npoly <= 31
+    out = np.zeros(x.size, dtype=np.uint8 if pairwise else np.int32)
+    lib.oracle_point_in_polygon(_ptr(x), _ptr(y), x.size, _ptr(po), npoly, _ptr(ro), _ptr(px),
+                                _ptr(py), _dtype_code(x), int(bool(pairwise)), _ptr(out))
+    return out
 
 
 def quadtree_point_to_nearest_linestring(pairs, tree, point_indices, x, y, ls_offsets, lx, ly):

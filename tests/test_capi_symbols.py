@@ -17,7 +17,8 @@ def test_header_declares_reference_entry_points():
     names = declared_functions()
     for f in ("cspt_quadtree_on_points", "cspt_polygon_bounding_boxes",
               "cspt_linestring_bounding_boxes", "cspt_join_quadtree_and_bounding_boxes",
-              "cspt_quadtree_point_in_polygon", "cspt_quadtree_point_to_nearest_linestring"):
+              "cspt_quadtree_point_in_polygon", "cspt_quadtree_point_to_nearest_linestring",
+              "cspt_point_in_polygon", "cspt_pairwise_point_in_polygon"):
         assert f in names
 
 
@@ -33,3 +34,33 @@ def test_last_error_empty_on_fresh_thread():
     from cuspatial_gb300 import _lib
     lib = _lib.load()
     assert lib.cspt_last_error_message() == b""
+
+
+def test_point_in_polygon_argument_checks_on_host():
+    # the reference's checks run before any device work, so they can be
+    # exercised without a GPU (point_in_polygon.cu:118-136 and
+    # detail/point_in_polygon.cuh:93-94)
+    import ctypes
+
+    import numpy as np
+
+    from cuspatial_gb300 import _lib
+    lib = _lib.load()
+    po = np.arange(33, dtype=np.uint32)
+    ro = np.arange(33, dtype=np.uint32) * 4
+    p = po.ctypes.data_as(ctypes.c_void_p)
+    r = ro.ctypes.data_as(ctypes.c_void_p)
+    st = lib.cspt_point_in_polygon(None, None, 5, p, 33, r, 33, None, None, 128, _lib.FLOAT64,
+                                   _lib.METHOD_EXACT, None, None, None)
+    assert st == _lib.INVALID_ARGUMENT
+    assert lib.cspt_last_error_message() == b"Number of polygons cannot exceed 31"
+    # an empty point column returns before the polygon count is checked
+    assert lib.cspt_point_in_polygon(None, None, 0, p, 33, r, 33, None, None, 128, _lib.FLOAT64,
+                                     _lib.METHOD_EXACT, None, None, None) == _lib.OK
+    st = lib.cspt_pairwise_point_in_polygon(None, None, 5, p, 33, r, 33, None, None, 128,
+                                            _lib.FLOAT64, _lib.METHOD_EXACT, None, None, None)
+    assert st == _lib.INVALID_ARGUMENT
+    assert lib.cspt_last_error_message() == b"Must pass in the same number of points as polygons."
+    st = lib.cspt_pairwise_point_in_polygon(None, None, 5, p, 6, r, 6, None, None, 20, 7,
+                                            _lib.METHOD_EXACT, None, None, None)
+    assert st == _lib.UNSUPPORTED

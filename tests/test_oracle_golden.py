@@ -84,6 +84,30 @@ def test_point_in_polygon_boundary_rule(golden):
 
 
 @pytest.mark.parametrize("dtype", DTYPES)
+def test_point_in_polygon_bitmask_and_pairwise(golden, dtype):
+    # cpp/tests/point_in_polygon/point_in_polygon_test.cu:108-441, through
+    # the unindexed entry points: the bitmask over all polygons, and each
+    # point paired with its own copy of a single-polygon case
+    for c in golden("point_in_polygon.json")["cases"]:
+        x = np.array(c["x"], dtype)
+        y = np.array(c["y"], dtype)
+        px = np.array(c["px"], dtype)
+        py = np.array(c["py"], dtype)
+        want = [int(e) for e in c["expected"]]
+        got = O.point_in_polygon(x, y, c["poly_offsets"], c["ring_offsets"], px, py)
+        assert got.tolist() == want, c["name"]
+        if len(c["poly_offsets"]) == 2:
+            n = len(x)
+            nv = len(px)
+            ro = np.concatenate([np.asarray(c["ring_offsets"][:-1]) + i * nv for i in range(n)]
+                                + [[n * nv]])
+            nr = len(c["ring_offsets"]) - 1
+            pw = O.point_in_polygon(x, y, np.arange(n + 1) * nr, ro, np.tile(px, n),
+                                    np.tile(py, n), pairwise=True)
+            assert pw.tolist() == want, c["name"]
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
 def test_linestring_bounding_boxes_small(golden, dtype):
     # python/.../bounding/test_linestring_bounding_boxes.py:48-140
     d = golden("linestring_bounding_boxes_small.json")
