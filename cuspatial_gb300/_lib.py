@@ -113,6 +113,10 @@ def _declare(lib):
         getattr(lib, name).argtypes = [
             _vp, _vp, _sz, _vp, _sz, _vp, _sz, _vp, _vp, _sz, ctypes.c_int, ctypes.c_int,
             ctypes.POINTER(CsptAllocator), _vp, _vp]
+    lib.cspt_quadtree_contains_properly.argtypes = [
+        _vp, _vp, _sz, _vp, _sz, _vp, _sz, _vp, _sz, _vp, _vp, _sz, ctypes.c_int, ctypes.c_int,
+        ctypes.POINTER(CsptAllocator), _vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp),
+        ctypes.POINTER(_vp), ctypes.POINTER(_sz)]
     _u64p = ctypes.POINTER(ctypes.c_uint64)
     lib.cspt_batched_pip_plan.argtypes = [
         _sz, _u64p, _vp, _vp, _u64p, _vp, _sz, _vp, _sz, _vp, _vp, _sz,

@@ -50,6 +50,12 @@ void pairwise_point_in_polygon(void const* x, void const* y, size_t n, uint32_t 
                                uint32_t const* ro, void const* vx, void const* vy, size_t nv,
                                cspt_dtype dtype, cspt_method method, Allocator const& alloc,
                                uint8_t* out, uint64_t* out_refined);
+void quadtree_contains_properly(void const* x, void const* y, size_t n, uint32_t const* go,
+                                size_t ngo, uint32_t const* po, size_t npo, uint32_t const* ro,
+                                size_t nro, void const* vx, void const* vy, size_t nv,
+                                cspt_dtype dtype, cspt_method method, cspt_allocator const* mr,
+                                void* stream, uint32_t** out_point, uint32_t** out_part,
+                                uint32_t** out_geom, size_t* out_n);
 
 namespace {
 thread_local std::string t_last_error;
@@ -421,6 +427,34 @@ cspt_status cspt_pairwise_point_in_polygon(const void* x, const void* y, size_t 
     pairwise_point_in_polygon(x, y, num_points, poly_offsets, ring_offsets, poly_x, poly_y,
                               num_poly_vertices, dtype, method, alloc, out, &refined);
     t_last_refined = refined;
+  });
+}
+
+cspt_status cspt_quadtree_contains_properly(
+  const void* x, const void* y, size_t num_points, const uint32_t* geometry_offsets,
+  size_t num_geometry_offsets, const uint32_t* part_offsets, size_t num_part_offsets,
+  const uint32_t* ring_offsets, size_t num_ring_offsets, const void* poly_x, const void* poly_y,
+  size_t num_poly_vertices, cspt_dtype dtype, cspt_method method, const cspt_allocator* mr,
+  void* stream, uint32_t** out_point_index, uint32_t** out_part_index,
+  uint32_t** out_geometry_index, size_t* out_num_pairs)
+{
+  return guarded([&] {
+    CSPT_EXPECTS(out_point_index && out_part_index && out_geometry_index && out_num_pairs,
+                 "output pointers must not be null");
+    *out_point_index    = nullptr;
+    *out_part_index     = nullptr;
+    *out_geometry_index = nullptr;
+    *out_num_pairs      = 0;
+    check_dtype(dtype);
+    CSPT_EXPECTS(method == CSPT_METHOD_EXACT || method == CSPT_METHOD_FILTERED,
+                 "unknown point-in-polygon method");
+    // contains.py:46-47: no polygons, no rows
+    if (num_part_offsets < 2 || num_poly_vertices == 0) return;
+    quadtree_contains_properly(x, y, num_points, geometry_offsets, num_geometry_offsets,
+                               part_offsets, num_part_offsets, ring_offsets, num_ring_offsets,
+                               poly_x, poly_y, num_poly_vertices, dtype, method, mr, stream,
+                               out_point_index, out_part_index, out_geometry_index,
+                               out_num_pairs);
   });
 }
 

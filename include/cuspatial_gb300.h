@@ -242,6 +242,27 @@ cspt_status cspt_pairwise_point_in_polygon(const void* x, const void* y, size_t 
                                            cspt_method method, const cspt_allocator* mr,
                                            void* stream, uint8_t* out);
 
+/*
+ * contains_properly in quadtree mode
+ * (python/cuspatial/cuspatial/core/binpreds/contains.py:19-74): the
+ * reference's parameters (max_depth 15, max_size ceil(sqrt(num_points)), the
+ * polygons' vertex extent as the tree's box and the smallest unclamped
+ * scale) run through cspt_quadtree_on_points, cspt_polygon_bounding_boxes,
+ * cspt_join_quadtree_and_bounding_boxes and cspt_quadtree_point_in_polygon.
+ * Rows in the join's order: out_point_index is the point's index in the
+ * input (point_indices[point_index], contains.py:65-67), out_part_index the
+ * polygon (part), out_geometry_index the multipolygon owning the part
+ * (core/binpreds/contains_geometry_processor.py:72-116; equal to the part
+ * when geometry_offsets is null).  Arrays allocated with mr.
+ */
+cspt_status cspt_quadtree_contains_properly(
+  const void* x, const void* y, size_t num_points, const uint32_t* geometry_offsets,
+  size_t num_geometry_offsets, const uint32_t* part_offsets, size_t num_part_offsets,
+  const uint32_t* ring_offsets, size_t num_ring_offsets, const void* poly_x, const void* poly_y,
+  size_t num_poly_vertices, cspt_dtype dtype, cspt_method method, const cspt_allocator* mr,
+  void* stream, uint32_t** out_point_index, uint32_t** out_part_index,
+  uint32_t** out_geometry_index, size_t* out_num_pairs);
+
 /* ------------------------------------------------------------------------
  * Batched point-in-polygon join (no counterpart in the reference, which
  * joins one point set with one polygon set per call).
