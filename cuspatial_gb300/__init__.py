@@ -3,14 +3,17 @@
 Functions mirror cuspatial.quadtree_on_points, polygon_bounding_boxes,
 linestring_bounding_boxes, join_quadtree_and_bounding_boxes,
 quadtree_point_in_polygon and quadtree_point_to_nearest_linestring, the
-unindexed point_in_polygon / pairwise_point_in_polygon and contains_properly;
+unindexed point_in_polygon / pairwise_point_in_polygon, contains_properly and
+the pairwise point-linestring distance and nearest points;
 they run hand-written CUDA kernels in libcuspatial_gb300.so through its C ABI.
 """
 
 from .api import (join_quadtree_and_bounding_boxes, last_refined_count,
-                  linestring_bounding_boxes, pairwise_point_in_polygon, point_in_polygon,
-                  point_in_polygon_bitmask, polygon_bounding_boxes, quadtree_on_points,
-                  quadtree_point_in_polygon, quadtree_point_to_nearest_linestring)
+                  linestring_bounding_boxes, pairwise_point_in_polygon,
+                  pairwise_point_linestring_distance, pairwise_point_linestring_nearest_points,
+                  point_in_polygon, point_in_polygon_bitmask, polygon_bounding_boxes,
+                  quadtree_on_points, quadtree_point_in_polygon,
+                  quadtree_point_to_nearest_linestring)
 from .contains import contains_properly, polygons_contains_properly
 from .geoseries import GeoSeries, Table
 
@@ -22,6 +25,8 @@ __all__ = [
     "last_refined_count",
     "linestring_bounding_boxes",
     "pairwise_point_in_polygon",
+    "pairwise_point_linestring_distance",
+    "pairwise_point_linestring_nearest_points",
     "point_in_polygon",
     "point_in_polygon_bitmask",
     "polygon_bounding_boxes",

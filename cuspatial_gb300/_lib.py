@@ -117,6 +117,12 @@ def _declare(lib):
         _vp, _vp, _sz, _vp, _sz, _vp, _sz, _vp, _sz, _vp, _vp, _sz, ctypes.c_int, ctypes.c_int,
         ctypes.POINTER(CsptAllocator), _vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp),
         ctypes.POINTER(_vp), ctypes.POINTER(_sz)]
+    lib.cspt_pairwise_point_linestring_distance.argtypes = [
+        _vp, _sz, _vp, _vp, _sz, _vp, _sz, _vp, _sz, _vp, _vp, _sz, ctypes.c_int, ctypes.c_int,
+        _vp, _vp]
+    lib.cspt_pairwise_point_linestring_nearest_points.argtypes = [
+        _vp, _sz, _vp, _vp, _sz, _vp, _sz, _vp, _sz, _vp, _vp, _sz, ctypes.c_int, ctypes.c_int,
+        _vp, _vp, _vp, _vp, _vp]
     _u64p = ctypes.POINTER(ctypes.c_uint64)
     lib.cspt_batched_pip_plan.argtypes = [
         _sz, _u64p, _vp, _vp, _u64p, _vp, _sz, _vp, _sz, _vp, _vp, _sz,

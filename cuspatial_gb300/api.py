@@ -13,8 +13,9 @@ import warnings
 import torch
 
 from . import _lib
-from .geoseries import (GeoSeries, Table, as_device_tensor, contains_only_linestrings,
-                        contains_only_points, contains_only_polygons)
+from .geoseries import (MULTIPOINT, GeoSeries, Table, as_device_tensor,
+                        contains_only_linestrings, contains_only_points,
+                        contains_only_points_or_multipoints, contains_only_polygons)
 
 _METHODS = {"exact": _lib.METHOD_EXACT, "filtered": _lib.METHOD_FILTERED}
 
@@ -296,6 +297,68 @@ def pairwise_point_in_polygon(points: GeoSeries, polygons: GeoSeries, method="ex
         int(poly.part_offset.numel()), _lib.ptr(poly.ring_offset), int(poly.ring_offset.numel()),
         _lib.ptr(poly.x), _lib.ptr(poly.y), int(poly.x.numel()), _dtype_code(pts.x),
         _METHODS[method], alloc.ref, _lib.stream_ptr(), _lib.ptr(out)), lib)
+    return out
+
+
+def _point_linestring_args(points, linestrings):
+    """C-ABI arguments shared by the pairwise point-linestring calls."""
+    if points.kind == MULTIPOINT:
+        mp = points.multipoints
+        pgo, px, py = mp.geometry_offset, mp.x, mp.y
+    else:
+        pgo, px, py = None, points.points.x, points.points.y
+    ls = linestrings.lines
+    n = len(points)
+    args = (_lib.ptr(pgo) if pgo is not None else None,
+            int(pgo.numel()) if pgo is not None else 0, _lib.ptr(px), _lib.ptr(py),
+            int(px.numel()), _lib.ptr(ls.geometry_offset), int(ls.geometry_offset.numel()),
+            _lib.ptr(ls.part_offset), int(ls.part_offset.numel()), _lib.ptr(ls.x),
+            _lib.ptr(ls.y), int(ls.x.numel()), _dtype_code(px))
+    return n, px, args
+
+
+def pairwise_point_linestring_distance(points: GeoSeries, linestrings: GeoSeries,
+                                       method="exact"):
+    """Distance of (multi)point i to (multi)linestring i (distance.py:317):
+    the smallest distance between any of its points and any segment."""
+    if not contains_only_points_or_multipoints(points):
+        raise ValueError("`points` array must contain only points")
+    if not contains_only_linestrings(linestrings):
+        raise ValueError("`linestrings` array must contain only linestrings")
+    lib = _lib.load()
+    n, px, args = _point_linestring_args(points, linestrings)
+    out = torch.empty(n, dtype=px.dtype, device=px.device)
+    _lib.check(lib.cspt_pairwise_point_linestring_distance(
+        *args, _METHODS[method], _lib.stream_ptr(), _lib.ptr(out)), lib)
+    return out
+
+
+def pairwise_point_linestring_nearest_points(points: GeoSeries, linestrings: GeoSeries,
+                                             method="exact"):
+    """Nearest points between (multi)point i and (multi)linestring i
+    (nearest_points.py:16-124): a Table with point_geometry_id (0 for
+    single points), linestring_geometry_id, segment_id and geometry (the
+    nearest points on the linestrings, a point GeoSeries)."""
+    if not contains_only_points_or_multipoints(points):
+        raise ValueError("`points` must contain only point geometries.")
+    if not contains_only_linestrings(linestrings):
+        raise ValueError("`linestrings` must contain only linestring geometries.")
+    lib = _lib.load()
+    n, px, args = _point_linestring_args(points, linestrings)
+    dev = px.device
+    opt = torch.zeros(n, dtype=torch.int32, device=dev)
+    ols = torch.empty(n, dtype=torch.int32, device=dev)
+    oseg = torch.empty(n, dtype=torch.int32, device=dev)
+    oxy = torch.empty(2 * n, dtype=px.dtype, device=dev)
+    _lib.check(lib.cspt_pairwise_point_linestring_nearest_points(
+        *args, _METHODS[method], _lib.stream_ptr(),
+        _lib.ptr(opt) if points.kind == MULTIPOINT else None, _lib.ptr(ols), _lib.ptr(oseg),
+        _lib.ptr(oxy)), lib)
+    out = Table()
+    out["point_geometry_id"] = opt
+    out["linestring_geometry_id"] = ols
+    out["segment_id"] = oseg
+    out["geometry"] = GeoSeries.from_points_xy(oxy)
     return out
 
 

@@ -56,9 +56,30 @@ void quadtree_contains_properly(void const* x, void const* y, size_t n, uint32_t
                                 cspt_dtype dtype, cspt_method method, cspt_allocator const* mr,
                                 void* stream, uint32_t** out_point, uint32_t** out_part,
                                 uint32_t** out_geom, size_t* out_n);
+void pairwise_point_linestring(size_t n, uint32_t const* pgo, size_t npgo, void const* x,
+                               void const* y, size_t np, uint32_t const* lgo, size_t nlgo,
+                               uint32_t const* lpo, size_t nlpo, void const* lx, void const* ly,
+                               size_t nv, cspt_dtype dtype, cspt_method method,
+                               Allocator const& alloc, void* od, int32_t* opt, int32_t* ols,
+                               int32_t* oseg, void* oxy, uint64_t* out_refined);
 
 namespace {
 thread_local std::string t_last_error;
+
+// Pairs of a pairwise (multi)point - (multi)linestring call: multipoints
+// count geometry offsets, single points count points; multilinestrings
+// count geometry offsets, single linestrings count part offsets.
+struct PlPairs {
+  size_t points, linestrings;
+};
+PlPairs pl_pairs(uint32_t const* pgo, size_t npgo, size_t np, uint32_t const* lgo, size_t nlgo,
+                 size_t nlpo)
+{
+  PlPairs r;
+  r.points      = pgo ? (npgo > 0 ? npgo - 1 : 0) : np;
+  r.linestrings = lgo ? (nlgo > 0 ? nlgo - 1 : 0) : (nlpo > 0 ? nlpo - 1 : 0);
+  return r;
+}
 thread_local uint64_t t_last_refined = 0;
 
 void check_dtype(cspt_dtype dtype)
@@ -455,6 +476,74 @@ cspt_status cspt_quadtree_contains_properly(
                                poly_x, poly_y, num_poly_vertices, dtype, method, mr, stream,
                                out_point_index, out_part_index, out_geometry_index,
                                out_num_pairs);
+  });
+}
+
+cspt_status cspt_pairwise_point_linestring_distance(
+  const uint32_t* point_geometry_offsets, size_t num_point_geometry_offsets, const void* x,
+  const void* y, size_t num_points, const uint32_t* linestring_geometry_offsets,
+  size_t num_linestring_geometry_offsets, const uint32_t* linestring_part_offsets,
+  size_t num_linestring_part_offsets, const void* ls_x, const void* ls_y,
+  size_t num_ls_vertices, cspt_dtype dtype, cspt_method method, void* stream,
+  void* out_distance)
+{
+  return guarded([&] {
+    t_last_refined = 0;
+    check_dtype(dtype);
+    CSPT_EXPECTS(method == CSPT_METHOD_EXACT || method == CSPT_METHOD_FILTERED,
+                 "unknown distance method");
+    PlPairs const pr = pl_pairs(point_geometry_offsets, num_point_geometry_offsets, num_points,
+                                linestring_geometry_offsets, num_linestring_geometry_offsets,
+                                num_linestring_part_offsets);
+    // point_linestring_distance.cu:92-93
+    CSPT_EXPECTS(pr.points == pr.linestrings,
+                 "Inputs should have the same number of geometries.");
+    if (pr.points == 0) return;
+    CSPT_EXPECTS(out_distance, "output pointers must not be null");
+    Allocator alloc(nullptr, as_stream(stream));
+    uint64_t refined = 0;
+    pairwise_point_linestring(pr.points, point_geometry_offsets, num_point_geometry_offsets, x,
+                              y, num_points, linestring_geometry_offsets,
+                              num_linestring_geometry_offsets, linestring_part_offsets,
+                              num_linestring_part_offsets, ls_x, ls_y, num_ls_vertices, dtype,
+                              method, alloc, out_distance, nullptr, nullptr, nullptr, nullptr,
+                              &refined);
+    t_last_refined = refined;
+  });
+}
+
+cspt_status cspt_pairwise_point_linestring_nearest_points(
+  const uint32_t* point_geometry_offsets, size_t num_point_geometry_offsets, const void* x,
+  const void* y, size_t num_points, const uint32_t* linestring_geometry_offsets,
+  size_t num_linestring_geometry_offsets, const uint32_t* linestring_part_offsets,
+  size_t num_linestring_part_offsets, const void* ls_x, const void* ls_y,
+  size_t num_ls_vertices, cspt_dtype dtype, cspt_method method, void* stream,
+  int32_t* out_point_geometry_id, int32_t* out_linestring_geometry_id, int32_t* out_segment_id,
+  void* out_nearest_xy)
+{
+  return guarded([&] {
+    t_last_refined = 0;
+    check_dtype(dtype);
+    CSPT_EXPECTS(method == CSPT_METHOD_EXACT || method == CSPT_METHOD_FILTERED,
+                 "unknown distance method");
+    PlPairs const pr = pl_pairs(point_geometry_offsets, num_point_geometry_offsets, num_points,
+                                linestring_geometry_offsets, num_linestring_geometry_offsets,
+                                num_linestring_part_offsets);
+    // point_linestring_nearest_points.cu:225-236
+    CSPT_EXPECTS(pr.points == pr.linestrings,
+                 "Mismatch number of (multi)points and (multi)linestrings.");
+    if (pr.points == 0) return;
+    CSPT_EXPECTS(out_segment_id && out_nearest_xy, "output pointers must not be null");
+    Allocator alloc(nullptr, as_stream(stream));
+    uint64_t refined = 0;
+    pairwise_point_linestring(pr.points, point_geometry_offsets, num_point_geometry_offsets, x,
+                              y, num_points, linestring_geometry_offsets,
+                              num_linestring_geometry_offsets, linestring_part_offsets,
+                              num_linestring_part_offsets, ls_x, ls_y, num_ls_vertices, dtype,
+                              method, alloc, nullptr, out_point_geometry_id,
+                              out_linestring_geometry_id, out_segment_id, out_nearest_xy,
+                              &refined);
+    t_last_refined = refined;
   });
 }
 

@@ -5,8 +5,8 @@ cuDF container of GeoArrow columns.  The join functions only read
 `points.points.{x,y}`, `polygons.polygons.{part_offset,ring_offset,x,y}`
 and `linestrings.lines.{part_offset,geometry_offset,x,y}`, so this stand-in
 stores exactly those GeoArrow buffers as torch CUDA tensors and offers the
-reference's `from_points_xy`, `from_linestrings_xy` and `from_polygons_xy`
-constructors.  Results are returned as `Table`, an ordered mapping of column
+reference's `from_points_xy`, `from_multipoints_xy`, `from_linestrings_xy`
+and `from_polygons_xy` constructors.  Results are returned as `Table`, an ordered mapping of column
 name to tensor in place of cudf.DataFrame.
 """
 
@@ -15,7 +15,7 @@ from collections import OrderedDict
 import numpy as np
 import torch
 
-POINT, LINESTRING, POLYGON = "point", "linestring", "polygon"
+POINT, MULTIPOINT, LINESTRING, POLYGON = "point", "multipoint", "linestring", "polygon"
 
 
 def as_device_tensor(a, dtype=None, device=None):
@@ -67,6 +67,12 @@ class GeoSeries:
         return self._coords
 
     @property
+    def multipoints(self):
+        if self.kind != MULTIPOINT:
+            raise ValueError("GeoSeries must contain only multipoints.")
+        return self._coords
+
+    @property
     def lines(self):
         if self.kind != LINESTRING:
             raise ValueError("GeoSeries must contain only linestrings.")
@@ -89,6 +95,12 @@ class GeoSeries:
         return cls(POINT, c, int(c.x.numel()))
 
     @classmethod
+    def from_multipoints_xy(cls, multipoints_xy, geometry_offset):
+        x, y = _xy_split(multipoints_xy)
+        c = _Coords(x, y, geometry_offset=geometry_offset)
+        return cls(MULTIPOINT, c, int(c.geometry_offset.numel()) - 1)
+
+    @classmethod
     def from_linestrings_xy(cls, linestrings_xy, part_offset, geometry_offset):
         x, y = _xy_split(linestrings_xy)
         c = _Coords(x, y, part_offset=part_offset, geometry_offset=geometry_offset)
@@ -104,6 +116,10 @@ class GeoSeries:
 
 def contains_only_points(gs):
     return isinstance(gs, GeoSeries) and gs.kind == POINT
+
+
+def contains_only_points_or_multipoints(gs):
+    return isinstance(gs, GeoSeries) and gs.kind in (POINT, MULTIPOINT)
 
 
 def contains_only_linestrings(gs):
@@ -130,4 +146,4 @@ class Table(OrderedDict):
         return len(self)
 
     def to_numpy(self):
-        return {k: v.cpu().numpy() for k, v in self.items()}
+        return {k: v.cpu().numpy() for k, v in self.items() if isinstance(v, torch.Tensor)}

@@ -263,6 +263,142 @@ cspt_status cspt_quadtree_contains_properly(
   void* stream, uint32_t** out_point_index, uint32_t** out_part_index,
   uint32_t** out_geometry_index, size_t* out_num_pairs);
 
+/*
+ * Replaces cuspatial::pairwise_point_linestring_distance
+ * (cpp/include/cuspatial/distance.hpp:167-170;
+ * cpp/src/distance/point_linestring_distance.cu:80-110).
+ * Pair i: multipoint i (points [point_geometry_offsets[i], [i+1]) or, with
+ * point_geometry_offsets NULL, point i) against multilinestring i (parts
+ * [linestring_geometry_offsets[i], [i+1]) or, NULL, part i; part j has the
+ * vertices [linestring_part_offsets[j], [j+1])).  Writes one distance per
+ * pair (dtype of the coordinates) to the caller's device array.
+ */
+cspt_status cspt_pairwise_point_linestring_distance(
+  const uint32_t* point_geometry_offsets, size_t num_point_geometry_offsets, const void* x,
+  const void* y, size_t num_points, const uint32_t* linestring_geometry_offsets,
+  size_t num_linestring_geometry_offsets, const uint32_t* linestring_part_offsets,
+  size_t num_linestring_part_offsets, const void* ls_x, const void* ls_y,
+  size_t num_ls_vertices, cspt_dtype dtype, cspt_method method, void* stream,
+  void* out_distance);
+
+/*
+ * Replaces cuspatial::pairwise_point_linestring_nearest_points
+ * (cpp/include/cuspatial/nearest_points.hpp:36-51 and :150-160;
+ * cpp/src/nearest_points/point_linestring_nearest_points.cu:210-245).
+ * Same inputs as cspt_pairwise_point_linestring_distance.  Per pair: the
+ * point's index within its multipoint, the linestring's index within its
+ * multilinestring, the segment's index within its linestring and the
+ * nearest point (x, y interleaved).  out_point_geometry_id and
+ * out_linestring_geometry_id may be NULL.  Pairs without a segment get
+ * 0, 0, 0, (0, 0) (the reference leaves them unset).
+ */
+cspt_status cspt_pairwise_point_linestring_nearest_points(
+  const uint32_t* point_geometry_offsets, size_t num_point_geometry_offsets, const void* x,
+  const void* y, size_t num_points, const uint32_t* linestring_geometry_offsets,
+  size_t num_linestring_geometry_offsets, const uint32_t* linestring_part_offsets,
+  size_t num_linestring_part_offsets, const void* ls_x, const void* ls_y,
+  size_t num_ls_vertices, cspt_dtype dtype, cspt_method method, void* stream,
+  int32_t* out_point_geometry_id, int32_t* out_linestring_geometry_id, int32_t* out_segment_id,
+  void* out_nearest_xy);
+
+/* ------------------------------------------------------------------------
+ * GeoArrow ingestion (python/cuspatial/cuspatial/io/pygeoarrow.py:9-70 and
+ * core/_column/geocolumn.py): a geometry array handed over through the
+ * Arrow C data interface becomes device columns with this library's offset
+ * layout (geometry -> part -> ring -> point, x and y apart).  Accepted:
+ *   - the reference's dense union of points / multipoints / linestrings /
+ *     polygons (one type per column; points as list<double> of length 2);
+ *   - native GeoArrow: points as fixed_size_list<double or float>[2] or
+ *     struct<x, y>, nested in (large) lists, the type from the
+ *     "ARROW:extension:name" metadata (geoarrow.point ... geoarrow.
+ *     multipolygon) or from `kind`.
+ * The Arrow buffers must be in host memory; no nulls.
+ * ------------------------------------------------------------------------ */
+#ifndef ARROW_C_DATA_INTERFACE
+#define ARROW_C_DATA_INTERFACE
+#define ARROW_FLAG_DICTIONARY_ORDERED 1
+#define ARROW_FLAG_NULLABLE 2
+#define ARROW_FLAG_MAP_KEYS_SORTED 4
+struct ArrowSchema {
+  const char* format;
+  const char* name;
+  const char* metadata;
+  int64_t flags;
+  int64_t n_children;
+  struct ArrowSchema** children;
+  struct ArrowSchema* dictionary;
+  void (*release)(struct ArrowSchema*);
+  void* private_data;
+};
+struct ArrowArray {
+  int64_t length;
+  int64_t null_count;
+  int64_t offset;
+  int64_t n_buffers;
+  int64_t n_children;
+  const void** buffers;
+  struct ArrowArray** children;
+  struct ArrowArray* dictionary;
+  void (*release)(struct ArrowArray*);
+  void* private_data;
+};
+#endif
+
+/* Geometry kinds, in the order of the reference's union children.
+ * LINESTRING and POLYGON columns carry multi-geometries too (geometry
+ * offsets over parts). */
+enum {
+  CSPT_GEOM_POINT      = 0,
+  CSPT_GEOM_MULTIPOINT = 1,
+  CSPT_GEOM_LINESTRING = 2,
+  CSPT_GEOM_POLYGON    = 3
+};
+
+typedef struct {
+  int kind;
+  int multi;        /* 1: multi-geometries (an extra list level) */
+  int interleaved;  /* 1: xy interleaved in the Arrow buffer */
+  cspt_dtype dtype;
+  size_t num_geometries;
+  size_t num_geometry_offsets, num_part_offsets, num_ring_offsets, num_points;
+} cspt_geoarrow_layout;
+
+/* Device columns: geometry_offsets (multipoint -> points, multilinestring
+ * -> parts, multipolygon -> polygons; 0..n for single linestrings and
+ * polygons, NULL for points), part_offsets (linestring -> points, polygon ->
+ * rings), ring_offsets (ring -> points, polygons only), x, y. */
+typedef struct {
+  int kind;
+  cspt_dtype dtype;
+  size_t num_geometries;
+  uint32_t* geometry_offsets;
+  size_t num_geometry_offsets;
+  uint32_t* part_offsets;
+  size_t num_part_offsets;
+  uint32_t* ring_offsets;
+  size_t num_ring_offsets;
+  void* x;
+  void* y;
+  size_t num_points;
+} cspt_geometry_column;
+
+/* Layout and sizes of a GeoArrow array (host only, no device work).
+ * kind: a CSPT_GEOM_* value, or -1 to take it from the union or metadata. */
+cspt_status cspt_geoarrow_describe(const struct ArrowSchema* schema,
+                                   const struct ArrowArray* array, int kind,
+                                   cspt_geoarrow_layout* out);
+
+/* Copies a GeoArrow array to device columns allocated with mr (one
+ * host->device copy per buffer; interleaved coordinates are split on the
+ * device).  Synchronises the stream.  The caller keeps ownership of the
+ * Arrow structures (they are not released). */
+cspt_status cspt_geoarrow_import(const struct ArrowSchema* schema, const struct ArrowArray* array,
+                                 int kind, const cspt_allocator* mr, void* stream,
+                                 cspt_geometry_column* out);
+
+/* Releases the device columns of cspt_geoarrow_import (same allocator). */
+void cspt_geometry_column_free(const cspt_allocator* mr, cspt_geometry_column* col, void* stream);
+
 /* ------------------------------------------------------------------------
  * Batched point-in-polygon join (no counterpart in the reference, which
  * joins one point set with one polygon set per call).

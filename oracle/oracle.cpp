@@ -603,6 +603,121 @@ void quadtree_point_to_nearest_linestring(uint32_t const* pair_ls, uint32_t cons
   }
 }
 
+// detail/utility/linestring.cuh:56-75 — squared distance from c to segment
+// ab and the nearest point on it.  The reference's build contracts each dot
+// product x1*x2 + y1*y2 into fma(x1, x2, y1*y2) and a + t*ab into
+// fma(t, ab, a); the oracle writes those fmas out.
+template <typename T>
+T segment_nearest(T cx, T cy, T ax, T ay, T bx, T by, T& nx, T& ny)
+{
+  T const abx = bx - ax, aby = by - ay;
+  T const acx = cx - ax, acy = cy - ay;
+  T const l2  = std::fma(abx, abx, aby * aby);
+  if (float_equal(l2, T{0})) {
+    nx = ax;
+    ny = ay;
+    return std::fma(acx, acx, acy * acy);
+  }
+  T const r   = std::fma(acx, abx, acy * aby);
+  T const bcx = cx - bx, bcy = cy - by;
+  if (r <= 0 || r >= l2) {
+    T const dac = std::fma(acx, acx, acy * acy);
+    T const dbc = std::fma(bcx, bcx, bcy * bcy);
+    if (dac < dbc) {
+      nx = ax;
+      ny = ay;
+      return dac;
+    }
+    nx = bx;
+    ny = by;
+    return dbc;
+  }
+  T const t   = r / l2;
+  T const px  = std::fma(t, abx, ax);
+  T const py  = std::fma(t, aby, ay);
+  T const pcx = cx - px, pcy = cy - py;
+  nx          = px;
+  ny          = py;
+  return std::fma(pcx, pcx, pcy * pcy);
+}
+
+// detail/kernel/pairwise_distance.cuh:94-131 with
+// detail/distance/point_linestring_distance.cuh:37-60: per segment the
+// smallest squared distance over the multipoint (device min = fmin, from
+// T max), its square root, and the smallest of those over the segments
+// (from T max).  pgo / lgo: geometry offsets (null: one point / one
+// linestring per pair); lpo: linestring part offsets.
+template <typename T>
+void pairwise_point_linestring_distance(size_t n, uint32_t const* pgo, T const* x, T const* y,
+                                        uint32_t const* lgo, uint32_t const* lpo, size_t nparts,
+                                        T const* lx, T const* ly, T* out)
+{
+  T const big = std::numeric_limits<T>::max();
+  for (size_t g = 0; g < n; ++g) {
+    size_t const p0 = pgo ? pgo[g] : g, p1 = pgo ? pgo[g + 1] : g + 1;
+    // parts named beyond the last part offset do not exist (the reference
+    // maps each vertex to its part, pairwise_distance.cuh:115-121)
+    size_t const l1 = std::min<size_t>(lgo ? lgo[g + 1] : g + 1, nparts);
+    size_t const l0 = std::min<size_t>(lgo ? lgo[g] : g, l1);
+    T d = big;
+    for (size_t part = l0; part < l1; ++part) {
+      for (size_t v = lpo[part]; v + 1 < lpo[part + 1]; ++v) {
+        T m = big;
+        for (size_t p = p0; p < p1; ++p) {
+          T nx, ny;
+          m = std::fmin(m, segment_nearest<T>(x[p], y[p], lx[v], ly[v], lx[v + 1], ly[v + 1],
+                                              nx, ny));
+        }
+        d = std::fmin(d, std::sqrt(m));
+      }
+    }
+    out[g] = d;
+  }
+}
+
+// detail/point_linestring_nearest_points.cuh:55-110: the first strictly
+// smaller squared distance over (point, part, segment) in order; ids local
+// to the pair.  Pairs without a segment keep (0, 0, 0, (0, 0)).
+template <typename T>
+void pairwise_point_linestring_nearest_points(size_t n, uint32_t const* pgo, T const* x,
+                                              T const* y, uint32_t const* lgo,
+                                              uint32_t const* lpo, size_t nparts, T const* lx,
+                                              T const* ly, int32_t* opt, int32_t* ols,
+                                              int32_t* oseg, T* oxy)
+{
+  for (size_t g = 0; g < n; ++g) {
+    size_t const p0 = pgo ? pgo[g] : g, p1 = pgo ? pgo[g + 1] : g + 1;
+    size_t const l1 = std::min<size_t>(lgo ? lgo[g + 1] : g + 1, nparts);
+    size_t const l0 = std::min<size_t>(lgo ? lgo[g] : g, l1);
+    T best           = std::numeric_limits<T>::max();
+    int32_t bp = 0, bl = 0, bs = 0;
+    T bx = 0, by = 0;
+    for (size_t p = p0; p < p1; ++p) {
+      for (size_t part = l0; part < l1; ++part) {
+        size_t const s0 = lpo[part];
+        for (size_t v = s0; v + 1 < lpo[part + 1]; ++v) {
+          T nx, ny;
+          T const d =
+            segment_nearest<T>(x[p], y[p], lx[v], ly[v], lx[v + 1], ly[v + 1], nx, ny);
+          if (d < best) {
+            best = d;
+            bp   = static_cast<int32_t>(p - p0);
+            bl   = static_cast<int32_t>(part - l0);
+            bs   = static_cast<int32_t>(v - s0);
+            bx   = nx;
+            by   = ny;
+          }
+        }
+      }
+    }
+    opt[g]         = bp;
+    ols[g]         = bl;
+    oseg[g]        = bs;
+    oxy[2 * g]     = bx;
+    oxy[2 * g + 1] = by;
+  }
+}
+
 template <typename T>
 void* dup_vec(std::vector<T> const& v)
 {
@@ -816,6 +931,30 @@ int oracle_point_in_polygon(void const* x, void const* y, size_t n, uint32_t con
       static_cast<uint8_t*>(out)[i] = static_cast<uint8_t>(mask);
     else
       static_cast<int32_t*>(out)[i] = mask;
+  }
+  return 0;
+}
+
+int oracle_pairwise_point_linestring(size_t n, uint32_t const* pgo, void const* x,
+                                     void const* y, uint32_t const* lgo, uint32_t const* lpo,
+                                     size_t nparts, void const* lx, void const* ly, int dtype,
+                                     void* out_dist, int32_t* opt, int32_t* ols, int32_t* oseg,
+                                     void* oxy)
+{
+  if (dtype == 1) {
+    auto X = static_cast<double const*>(x), Y = static_cast<double const*>(y);
+    auto LX = static_cast<double const*>(lx), LY = static_cast<double const*>(ly);
+    pairwise_point_linestring_distance<double>(n, pgo, X, Y, lgo, lpo, nparts, LX, LY,
+                                               static_cast<double*>(out_dist));
+    pairwise_point_linestring_nearest_points<double>(n, pgo, X, Y, lgo, lpo, nparts, LX, LY,
+                                                     opt, ols, oseg, static_cast<double*>(oxy));
+  } else {
+    auto X = static_cast<float const*>(x), Y = static_cast<float const*>(y);
+    auto LX = static_cast<float const*>(lx), LY = static_cast<float const*>(ly);
+    pairwise_point_linestring_distance<float>(n, pgo, X, Y, lgo, lpo, nparts, LX, LY,
+                                              static_cast<float*>(out_dist));
+    pairwise_point_linestring_nearest_points<float>(n, pgo, X, Y, lgo, lpo, nparts, LX, LY,
+                                                    opt, ols, oseg, static_cast<float*>(oxy));
   }
   return 0;
 }

@@ -58,6 +58,8 @@ def _load():
         ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_sz)]
     lib.oracle_is_point_in_polygon.argtypes = [
         ctypes.c_double, ctypes.c_double, _vp, ctypes.c_int64, ctypes.c_int64, _vp, _vp]
+    lib.oracle_pairwise_point_linestring.argtypes = [
+        _sz, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp]
     lib.oracle_point_in_polygon.argtypes = [
         _vp, _vp, _sz, _vp, _sz, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp]
     lib.oracle_quadtree_point_to_nearest_linestring.argtypes = [
@@ -213,6 +215,35 @@ def point_in_polygon(x, y, poly_offsets, ring_offsets, px, py, pairwise=False):
     lib.oracle_point_in_polygon(_ptr(x), _ptr(y), x.size, _ptr(po), npoly, _ptr(ro), _ptr(px),
                                 _ptr(py), _dtype_code(x), int(bool(pairwise)), _ptr(out))
     return out
+
+
+def pairwise_point_linestring(x, y, part_offsets, lx, ly, point_geometry_offsets=None,
+                              linestring_geometry_offsets=None):
+    """Pairwise point-linestring distance and nearest points: a dict with
+    distance, point_geometry_id, linestring_geometry_id, segment_id and the
+    nearest points' x, y."""
+    lib = _load()
+    x = np.ascontiguousarray(x)
+    y = np.ascontiguousarray(y, dtype=x.dtype)
+    lx = np.ascontiguousarray(lx, dtype=x.dtype)
+    ly = np.ascontiguousarray(ly, dtype=x.dtype)
+    lpo = np.ascontiguousarray(part_offsets, dtype=np.uint32)
+    pgo = (None if point_geometry_offsets is None
+           else np.ascontiguousarray(point_geometry_offsets, dtype=np.uint32))
+    lgo = (None if linestring_geometry_offsets is None
+           else np.ascontiguousarray(linestring_geometry_offsets, dtype=np.uint32))
+    n = (pgo.size - 1) if pgo is not None else x.size
+    dist = np.zeros(n, dtype=x.dtype)
+    opt = np.zeros(n, np.int32)
+    ols = np.zeros(n, np.int32)
+    oseg = np.zeros(n, np.int32)
+    oxy = np.zeros(2 * n, dtype=x.dtype)
+    lib.oracle_pairwise_point_linestring(n, _ptr(pgo), _ptr(x), _ptr(y), _ptr(lgo), _ptr(lpo),
+                                         max(lpo.size - 1, 0), _ptr(lx), _ptr(ly),
+                                         _dtype_code(x), _ptr(dist),
+                                         _ptr(opt), _ptr(ols), _ptr(oseg), _ptr(oxy))
+    return dict(distance=dist, point_geometry_id=opt, linestring_geometry_id=ols,
+                segment_id=oseg, x=oxy[0::2].copy(), y=oxy[1::2].copy())
 
 
 def quadtree_point_to_nearest_linestring(pairs, tree, point_indices, x, y, ls_offsets, lx, ly):

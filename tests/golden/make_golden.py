@@ -14,6 +14,8 @@ Sources:
   cpp/tests/join/quadtree_point_to_nearest_linestring_test_small.cu
   cpp/tests/point_in_polygon/point_in_polygon_test.cu           (boundary rule)
   python/cuspatial/cuspatial/tests/spatial/bounding/test_linestring_bounding_boxes.py
+  cpp/tests/distance/point_linestring_distance_test.cu          (pairwise distance)
+  cpp/tests/nearest_points/point_linestring_nearest_points_test.cu
 """
 
 import json
@@ -266,6 +268,133 @@ def linestring_bbox_kat(root):
                 expansion_radius=radius, minx=minx, miny=miny, maxx=maxx, maxy=maxy)
 
 
+def cpp_expr(tok):
+    """A number or the tests' std::sqrt(T{a}) [/ b] expressions."""
+    tok = " ".join(tok.split())
+    m = re.fullmatch(r"std::sqrt\(T\{([-+0-9.eE]+)\}\)(?:\s*/\s*([-+0-9.eE]+))?", tok)
+    if m:
+        v = parse_number(m.group(1)) ** 0.5
+        return v / parse_number(m.group(2)) if m.group(2) else v
+    return parse_number(tok)
+
+
+def braces_after(body, pattern):
+    """The brace list that follows the first match of `pattern` (None if absent)."""
+    m = re.search(pattern, body, re.S)
+    if not m:
+        return None
+    return parse_braces(body, body.index("{", m.end() - 1))[0]
+
+
+def expr_list_after(body, pattern):
+    m = re.search(pattern, body, re.S)
+    if not m:
+        return None
+    start = body.index("{", m.end() - 1)
+    depth, i = 0, start
+    while True:
+        if body[i] == "{":
+            depth += 1
+        elif body[i] == "}":
+            depth -= 1
+            if depth == 0:
+                break
+        i += 1
+    inner = body[start + 1:i]
+    parts, depth, tok = [], 0, ""
+    for c in inner:
+        if c in "({":
+            depth += 1
+        elif c in ")}":
+            depth -= 1
+        if c == "," and depth == 0:
+            parts.append(tok)
+            tok = ""
+        else:
+            tok += c
+    if tok.strip():
+        parts.append(tok)
+    return [cpp_expr(t) for t in parts]
+
+
+def point_linestring_distance_kats(root):
+    rel = "cpp/tests/distance/point_linestring_distance_test.cu"
+    text = strip_comments(open(os.path.join(root, rel)).read())
+    cases = []
+    for name, body in test_bodies(text, "PairwisePointLinestringDistanceTest").items():
+        c = dict(name=name)
+        if name == "ManyPairsFromIteratorsSingleComponent":
+            # built from counting iterators in the test: linestring i has the
+            # vertices (3i, 1), (3i+1, 1), (3i+2, 1); point i is (3i, 0)
+            n = 100
+            c.update(x=[3.0 * i for i in range(n)], y=[0.0] * n,
+                     point_geometry_offsets=None, linestring_geometry_offsets=None,
+                     part_offsets=[3 * i for i in range(n + 1)],
+                     lx=[float(i) for i in range(3 * n)], ly=[1.0] * (3 * n),
+                     expected=[1.0] * n)
+            cases.append(c)
+            continue
+        if "d_points_x" in body:
+            px = braces_after(body, r"d_points_x\s*=\s*rmm::device_vector<T>\(\s*std::vector<T>")
+            py = braces_after(body, r"d_points_y\s*=\s*rmm::device_vector<T>\(\s*std::vector<T>")
+            lx = braces_after(body, r"d_linestring_points_x\s*=\s*rmm::device_vector<T>\(\s*std::vector<T>")
+            ly = braces_after(body, r"d_linestring_points_y\s*=\s*rmm::device_vector<T>\(\s*std::vector<T>")
+            n = len(px)
+            c.update(x=px, y=py, point_geometry_offsets=None, linestring_geometry_offsets=None,
+                     part_offsets=[3 * i for i in range(n + 1)], lx=lx, ly=ly,
+                     expected=expr_list_after(body, r"expect\s*=\s*std::vector<T>"))
+            cases.append(c)
+            continue
+        pts = braces_after(body, r"CartVec points")
+        lpts = braces_after(body, r"CartVec linestring_points")
+        c.update(x=[float(p[0]) for p in pts], y=[float(p[1]) for p in pts],
+                 point_geometry_offsets=braces_after(body, r"point_geometry_offsets"),
+                 linestring_geometry_offsets=braces_after(body, r"linestring_geometry_offsets"),
+                 part_offsets=braces_after(body, r"linestring_part_offsets"),
+                 lx=[float(p[0]) for p in lpts], ly=[float(p[1]) for p in lpts],
+                 expected=expr_list_after(body, r"expect\(std::vector<T>"))
+        if c["expected"] is None:
+            c["expected"] = []
+        cases.append(c)
+    return dict(source=rel, note="expected distances; the reference compares them "
+                "with CUSPATIAL_EXPECT_VECTORS_EQUIVALENT (float tolerance)", cases=cases)
+
+
+def nearest_points_kats(root):
+    rel = "cpp/tests/nearest_points/point_linestring_nearest_points_test.cu"
+    text = strip_comments(open(os.path.join(root, rel)).read())
+    cases = []
+    for name, body in test_bodies(text, "PairwisePointLinestringNearestPointsTest").items():
+        n = int(re.search(r"num_pairs\s*=\s*(\d+)", body).group(1))
+        pts = braces_after(body, r"\bpoints(?:_it)?\s*=\s*rmm::device_vector<vec_2d<T>>\(\s*CartVec")
+        lpts = braces_after(body, r"\blinestring_points(?:_it)?\s*=\s*rmm::device_vector<vec_2d<T>>\(\s*CartVec")
+        pgo = braces_after(body, r"points_geometry_offsets\s*=\s*rmm::device_vector<int32_t>\(\s*std::vector<int>")
+        lgo = braces_after(body, r"linestring_geometry_offsets\s*=\s*rmm::device_vector<int32_t>\(\s*std::vector<int>")
+        lpo = braces_after(body, r"linestring_part_offsets\s*=\s*rmm::device_vector<int32_t>\(\s*std::vector<int32_t>")
+
+        def ids(var):
+            m = re.search(r"EXPECT_EQ\((?:thrust::host_vector<int32_t>\()?%s\)?\s*,\s*"
+                          r"std::vector<int32_t>\(?" % var, body)
+            if not m:
+                return None
+            return parse_braces(body, body.index("{", m.end() - 1))[0]
+
+        coords = braces_after(body, r"expected_coordinate\s*=\s*CartVec")
+        if coords is None:
+            coords = braces_after(body, r"CUSPATIAL_EXPECT_VECTORS_EQUIVALENT\(\s*neartest_point_coordinate\s*,\s*CartVec")
+        cases.append(dict(
+            name=name, num_pairs=n, x=[float(p[0]) for p in pts], y=[float(p[1]) for p in pts],
+            point_geometry_offsets=pgo, linestring_geometry_offsets=lgo, part_offsets=lpo,
+            lx=[float(p[0]) for p in lpts], ly=[float(p[1]) for p in lpts],
+            point_geometry_id=ids("nearest_point_id"),
+            linestring_geometry_id=ids(r"nearest_linestring_(?:linestring_|parts_)?id"),
+            segment_id=ids(r"nearest_(?:linestring_)?segment_id"),
+            nearest_x=[float(p[0]) for p in (coords or [])],
+            nearest_y=[float(p[1]) for p in (coords or [])]))
+    return dict(source=rel, note="ids exact; coordinates compared with float tolerance in "
+                "the reference", cases=cases)
+
+
 def main():
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     here = os.path.dirname(os.path.abspath(__file__))
@@ -275,6 +404,8 @@ def main():
         "quadtree_point_to_nearest_linestring_small.json": nearest_small_kat(root),
         "point_in_polygon.json": point_in_polygon_kats(root),
         "linestring_bounding_boxes_small.json": linestring_bbox_kat(root),
+        "point_linestring_distance.json": point_linestring_distance_kats(root),
+        "point_linestring_nearest_points.json": nearest_points_kats(root),
     }
     for name, data in outputs.items():
         with open(os.path.join(here, name), "w") as f:

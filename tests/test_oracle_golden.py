@@ -133,3 +133,47 @@ def test_polygon_bounding_boxes_skip_empty_polygon():
     assert bb["minx"][:2].tolist() == [0, 10]
     assert bb["maxy"][:2].tolist() == [7, 17]
     assert np.isnan(bb["minx"][2])
+
+
+def _ulps(a, b):
+    """Distance in units in the last place between same-dtype arrays."""
+    a = np.asarray(a)
+    b = np.asarray(b, dtype=a.dtype)
+    it = np.int64 if a.dtype == np.float64 else np.int32
+    ia = a.view(it).astype(np.int64)
+    ib = b.view(it).astype(np.int64)
+    top = np.int64(np.iinfo(it).min)
+    ia = np.where(ia < 0, top - ia, ia)
+    ib = np.where(ib < 0, top - ib, ib)
+    return np.abs(ia - ib)
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+def test_pairwise_point_linestring_distance_kats(golden, dtype):
+    # cpp/tests/distance/point_linestring_distance_test.cu:44-456; the
+    # reference compares with gtest's 4-ULP float equality
+    for c in golden("point_linestring_distance.json")["cases"]:
+        r = O.pairwise_point_linestring(np.array(c["x"], dtype), np.array(c["y"], dtype),
+                                        c["part_offsets"], np.array(c["lx"], dtype),
+                                        np.array(c["ly"], dtype), c["point_geometry_offsets"],
+                                        c["linestring_geometry_offsets"])
+        want = np.array(c["expected"], dtype)
+        assert len(r["distance"]) == len(want), c["name"]
+        assert np.all(_ulps(r["distance"], want) <= 4), (c["name"], r["distance"], want)
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+def test_pairwise_point_linestring_nearest_points_kats(golden, dtype):
+    # cpp/tests/nearest_points/point_linestring_nearest_points_test.cu:43-420
+    for c in golden("point_linestring_nearest_points.json")["cases"]:
+        n = c["num_pairs"]
+        r = O.pairwise_point_linestring(np.array(c["x"], dtype), np.array(c["y"], dtype),
+                                        c["part_offsets"], np.array(c["lx"], dtype),
+                                        np.array(c["ly"], dtype), c["point_geometry_offsets"],
+                                        c["linestring_geometry_offsets"])
+        assert len(r["segment_id"]) == n
+        for k in ("point_geometry_id", "linestring_geometry_id", "segment_id"):
+            if c[k] is not None:
+                assert r[k].tolist() == c[k], (c["name"], k)
+        for k, ck in (("x", "nearest_x"), ("y", "nearest_y")):
+            assert np.all(_ulps(r[k], np.array(c[ck], dtype)) <= 4), (c["name"], k)
