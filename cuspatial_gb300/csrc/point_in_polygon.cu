@@ -7,12 +7,13 @@
 // (pip_functor and the pairwise transform) and detail/algorithm/
 // is_point_in_polygon.cuh:45-100 (the per-pair test).
 //
-// Bitmask form: the polygons go into the slab index (polygon_index.cuh) and
-// one thread takes one point through all of them; the index limits each test
-// to the edges of the point's slab.  With float64 input and the filtered
-// method the point is placed once on the index's anchor grid (bit
-// arithmetic, no float64 instruction) and the float32 filter decides each
-// polygon, as in the quadtree join.
+// Bitmask form: the polygons go into the slab index (polygon_index.cuh), which
+// limits each test to the edges of the point's slab; each lane holds one
+// polygon's index fields in registers and the lanes of a warp cover
+// (point, polygon) combinations.  With float64 input and the filtered method
+// each point is placed once on the index's anchor grid (bit arithmetic, no
+// float64 instruction) and the float32 filter decides each polygon, as in the
+// quadtree join.
 //
 // Pairwise form: every polygon is used once, so no index is built; a group
 // of G lanes (1, 4, 8 or 32, from the mean polygon size) walks the polygon's
@@ -73,20 +74,35 @@ __device__ inline bool grid_split(double v, int k, long long& q, float& u)
   return true;
 }
 
-// Bitmask form, one thread per point: bit p of out[i] = point i inside
-// polygon p (pip_functor, detail/point_in_polygon.cuh:41-66).
+// Bitmask form (pip_functor, detail/point_in_polygon.cuh:41-66): bit p of
+// out[i] = point i inside polygon p.  With at most 31 polygons every lane
+// keeps one polygon's index fields in registers for the whole kernel: with
+// P = 2^lp >= the polygon count, lane = (slot s, polygon p) with
+// p = lane % P and s = lane / P, so a warp tests 32 / P points at a time
+// against all polygons; a ballot then holds each point's mask in P bits.
+// Points are read (and masks written) 32 at a time, one per lane, and passed
+// to the testing lanes by shuffles.
 template <typename T, bool Filtered>
 __global__ void __launch_bounds__(kPointsBlock)
   points_pip_kernel(T const* __restrict__ x, T const* __restrict__ y, size_t n,
-                    PolygonIndexView<T> ix, int32_t* __restrict__ out,
+                    PolygonIndexView<T> ix, uint32_t lp, int32_t* __restrict__ out,
                     unsigned long long* __restrict__ refined)
 {
-  uint32_t const np    = static_cast<uint32_t>(ix.num_polygons);
-  size_t const stride  = static_cast<size_t>(gridDim.x) * blockDim.x;
+  int const lane       = threadIdx.x & 31;
+  uint32_t const P     = 1u << lp;
+  uint32_t const S     = 32u >> lp;
+  uint32_t const p     = static_cast<uint32_t>(lane) & (P - 1u);
+  uint32_t const slot  = static_cast<uint32_t>(lane) >> lp;
+  unsigned const pbits = P == 32u ? 0xFFFFFFFFu : ((1u << P) - 1u);
+  bool const has_poly  = p < ix.num_polygons;
   uint32_t nref        = 0;
-  int gk               = 0;
-  float gf             = 0.0f;
-  bool gok             = false;
+  // the lane's polygon
+  float4 box    = make_float4(0.f, 0.f, 0.f, 0.f);
+  float mp = 0.0f, invh = 0.0f, gf = 0.0f;
+  uint32_t ns = 1, slab0 = 0, vb = 0, ve = 0;
+  long long aix = 0, aiy = 0;
+  bool exact_poly = true, gok = false;
+  int gk          = 0;
   if constexpr (Filtered) {
     double const g = *ix.grid;
     gf             = static_cast<float>(g);
@@ -94,47 +110,81 @@ __global__ void __launch_bounds__(kPointsBlock)
     gk = static_cast<int>((static_cast<unsigned long long>(__double_as_longlong(g)) >> 52) &
                           0x7FFull) -
          1023;
-  }
-  for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
-       i += stride) {
-    T const px   = x[i];
-    T const py   = y[i];
-    int32_t mask = 0;
-    if constexpr (Filtered) {
-      long long qx = 0, qy = 0;
-      float ux = 0.0f, uy = 0.0f;
-      bool const framed = gok && grid_split(px, gk, qx, ux) && grid_split(py, gk, qy, uy);
-      float const mlf   = fmaxf(fabsf(ux), fabsf(uy));
-      for (uint32_t p = 0; p < np; ++p) {
-        long long const dix = ix.anchor_ix[p] - qx;
-        long long const diy = ix.anchor_iy[p] - qy;
-        bool const exact    = !framed || ix.exact_only[p] || dix <= -16777216LL ||
-                           dix >= 16777216LL || diy <= -16777216LL || diy >= 16777216LL;
-        bool hit;
-        if (exact) {
-          ++nref;
-          hit = pip_exact<double>(px, py, ix, p);
-        } else {
-          // anchor offset in grid steps: exact in float32 below 2^24 steps
-          float const dx = static_cast<float>(static_cast<int>(dix)) * gf;
-          float const dy = static_cast<float>(static_cast<int>(diy)) * gf;
-          hit            = filtered_test<false>(
-            ix, p, ux - dx, uy - dy, ix.max_offset[p], mlf, ix.box32[p], ix.inv_slab_h32[p],
-            0.0f, ix.num_slabs[p], ix.slab_base[p], ix.vert_begin[p], ix.vert_end[p],
-            [&](double& ox, double& oy) {
-              ox = px;
-              oy = py;
-            },
-            nref);
-        }
-        mask |= hit ? (1 << p) : 0;
-      }
-    } else {
-      for (uint32_t p = 0; p < np; ++p) mask |= pip_exact<T>(px, py, ix, p) ? (1 << p) : 0;
+    if (has_poly) {
+      box        = ix.box32[p];
+      mp         = ix.max_offset[p];
+      invh       = ix.inv_slab_h32[p];
+      ns         = ix.num_slabs[p];
+      slab0      = ix.slab_base[p];
+      vb         = ix.vert_begin[p];
+      ve         = ix.vert_end[p];
+      aix        = ix.anchor_ix[p];
+      aiy        = ix.anchor_iy[p];
+      exact_poly = ix.exact_only[p] != 0;
     }
-    out[i] = mask;
   }
-  if (Filtered && refined && nref) atomicAdd(refined, static_cast<unsigned long long>(nref));
+  size_t const warp   = (blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5;
+  size_t const nwarps = (static_cast<size_t>(gridDim.x) * blockDim.x) >> 5;
+  for (size_t base = warp * 32; base < n; base += nwarps * 32) {
+    size_t const i = base + static_cast<size_t>(lane);
+    T px = T{0}, py = T{0};
+    if (i < n) {
+      px = x[i];
+      py = y[i];
+    }
+    long long qx = 0, qy = 0;
+    float ux = 0.0f, uy = 0.0f;
+    bool framed = false;
+    if constexpr (Filtered)
+      framed = gok && grid_split(px, gk, qx, ux) && grid_split(py, gk, qy, uy);
+    int32_t mine = 0;
+    for (uint32_t b = 0; b < P; ++b) {
+      int const src  = static_cast<int>(b * S + slot);  // lane holding the tested point
+      T const tx     = __shfl_sync(0xFFFFFFFFu, px, src);
+      T const ty     = __shfl_sync(0xFFFFFFFFu, py, src);
+      bool const live = has_poly && base + static_cast<size_t>(src) < n;
+      bool hit        = false;
+      if constexpr (Filtered) {
+        long long const tqx = __shfl_sync(0xFFFFFFFFu, qx, src);
+        long long const tqy = __shfl_sync(0xFFFFFFFFu, qy, src);
+        float const tux     = __shfl_sync(0xFFFFFFFFu, ux, src);
+        float const tuy     = __shfl_sync(0xFFFFFFFFu, uy, src);
+        bool const tfr      = __shfl_sync(0xFFFFFFFFu, static_cast<int>(framed), src) != 0;
+        if (live) {
+          long long const dix = aix - tqx;
+          long long const diy = aiy - tqy;
+          bool const exact    = !tfr || exact_poly || dix <= -16777216LL || dix >= 16777216LL ||
+                             diy <= -16777216LL || diy >= 16777216LL;
+          if (exact) {
+            ++nref;
+            hit = pip_exact<double>(tx, ty, ix, p);
+          } else {
+            // anchor offset in grid steps: exact in float32 below 2^24 steps
+            float const dx = static_cast<float>(static_cast<int>(dix)) * gf;
+            float const dy = static_cast<float>(static_cast<int>(diy)) * gf;
+            hit            = filtered_test<false>(
+              ix, p, tux - dx, tuy - dy, mp, fmaxf(fabsf(tux), fabsf(tuy)), box, invh, 0.0f, ns,
+              slab0, vb, ve,
+              [&](double& ox, double& oy) {
+                ox = tx;
+                oy = ty;
+              },
+              nref);
+          }
+        }
+      } else {
+        if (live) hit = pip_exact<T>(tx, ty, ix, p);
+      }
+      unsigned const bal = __ballot_sync(0xFFFFFFFFu, hit);
+      uint32_t const own = static_cast<uint32_t>(lane) - b * S;  // this lane's point slot
+      if (own < S) mine = static_cast<int32_t>((bal >> (own * P)) & pbits);
+    }
+    if (i < n) out[i] = mine;
+  }
+  if (Filtered && refined) {
+    for (int o = 16; o > 0; o >>= 1) nref += __shfl_xor_sync(0xFFFFFFFFu, nref, o);
+    if (lane == 0 && nref) atomicAdd(refined, static_cast<unsigned long long>(nref));
+  }
 }
 
 __device__ inline bool same_bits(double a, double b)
@@ -304,6 +354,14 @@ unsigned points_grid(size_t n)
   return grid_for(n, kPointsBlock, static_cast<unsigned>(num_sms()) * 8u);
 }
 
+// log2 of the lanes per point: the smallest power of two >= the polygons
+uint32_t lanes_log2(size_t npoly)
+{
+  uint32_t lp = 0;
+  while ((size_t{1} << lp) < npoly) ++lp;
+  return lp;
+}
+
 template <typename T>
 void bitmask(T const* x, T const* y, size_t n, uint32_t const* po, size_t npo, uint32_t const* ro,
              size_t nro, T const* vx, T const* vy, size_t nv, bool filtered, Allocator const& alloc,
@@ -311,18 +369,19 @@ void bitmask(T const* x, T const* y, size_t n, uint32_t const* po, size_t npo, u
 {
   cudaStream_t const s = alloc.stream();
   PolygonIndex<T> index(po, npo, ro, nro, vx, vy, nv, filtered, alloc);
+  uint32_t const lp = lanes_log2(npo - 1);
   Buffer<unsigned long long> refined(alloc, 1);
   CSPT_CUDA_TRY(cudaMemsetAsync(refined.data(), 0, sizeof(unsigned long long), s));
   {
     KernelTimer timer("points_pip", s);
     if (filtered) {
       if constexpr (std::is_same<T, double>::value) {
-        points_pip_kernel<double, true>
-          <<<points_grid(n), kPointsBlock, 0, s>>>(x, y, n, index.view(), out, refined.data());
+        points_pip_kernel<double, true><<<points_grid(n), kPointsBlock, 0, s>>>(
+          x, y, n, index.view(), lp, out, refined.data());
       }
     } else {
       points_pip_kernel<T, false>
-        <<<points_grid(n), kPointsBlock, 0, s>>>(x, y, n, index.view(), out, nullptr);
+        <<<points_grid(n), kPointsBlock, 0, s>>>(x, y, n, index.view(), lp, out, nullptr);
     }
     CSPT_CHECK_LAUNCH();
   }
