@@ -13,6 +13,7 @@
 // coordinates); each offset level is rebased to start at 0 on the host
 // (sliced arrays) and copied, the coordinates are copied once as they are
 // and split into x / y by a kernel when interleaved.
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -194,31 +195,51 @@ uint32_t* to_device(std::vector<uint32_t> const& h, Allocator const& alloc)
   return d;
 }
 
-}  // namespace
+// The whole parse: the geometry kind, the rebased offsets of every level
+// and where the points' coordinates are.
+struct Parsed {
+  cspt_geoarrow_layout layout{};
+  std::vector<uint32_t> geom, part, ring;
+  PointLayout points;
+};
 
-void geoarrow_describe(ArrowSchema const* schema, ArrowArray const* array, int kind_hint,
-                       cspt_geoarrow_layout* out)
+Parsed parse(ArrowSchema const* schema, ArrowArray const* array, int kind)
 {
+  Parsed r;
   ArrowSchema const* s = schema;
   ArrowArray const* a  = array;
   int64_t start = 0, len = a->length;
-  int kind = kind_hint;
   // the reference's dense union of four children (pygeoarrow.py:22-31)
   if (starts_with(s->format, "+ud:")) {
     CSPT_EXPECTS(s->n_children == 4, "the geometry union has four children");
-    int8_t const* types    = static_cast<int8_t const*>(a->buffers[1]);
-    int32_t const* offsets = static_cast<int32_t const*>(a->buffers[2]);
-    int8_t t               = len > 0 ? types[a->offset] : 0;
-    int32_t o0             = len > 0 ? offsets[a->offset] : 0;
+    // unions carry no validity buffer: type ids and value offsets (a
+    // leading validity slot is tolerated)
+    CSPT_EXPECTS(a->n_buffers == 2 || a->n_buffers == 3, "a dense union has two buffers");
+    int const b0           = a->n_buffers == 3 ? 1 : 0;
+    int8_t const* types    = static_cast<int8_t const*>(a->buffers[b0]);
+    int32_t const* offsets = static_cast<int32_t const*>(a->buffers[b0 + 1]);
+    int8_t const t         = len > 0 ? types[a->offset] : 0;
+    int32_t const o0       = len > 0 ? offsets[a->offset] : 0;
     for (int64_t i = 0; i < len; ++i) {
       if (types[a->offset + i] != t || offsets[a->offset + i] != o0 + i)
         throw Error{CSPT_UNSUPPORTED,
                     "mixed geometry types in one column are not supported; split the column by "
                     "type"};
     }
-    kind  = t;  // 0 points, 1 multipoints, 2 (multi)linestrings, 3 (multi)polygons
-    s     = s->children[t];
-    a     = a->children[t];
+    // type ids to children: the codes listed after "+ud:" (0,1,2,3 in the
+    // reference's union)
+    int child = -1, idx = 0;
+    for (char const* c = s->format + 4; *c; ++idx) {
+      char* end      = nullptr;
+      int const code = static_cast<int>(std::strtol(c, &end, 10));
+      if (end == c) break;  // not a number: stop
+      if (code == t) child = idx;
+      c = *end == ',' ? end + 1 : end;
+    }
+    CSPT_EXPECTS(child >= 0 && child < 4, "unknown union child");
+    kind  = child;  // 0 points, 1 multipoints, 2 (multi)linestrings, 3 (multi)polygons
+    s     = s->children[child];
+    a     = a->children[child];
     start = o0;
   } else if (kind < 0) {
     std::string const ext = extension_name(s->metadata);
@@ -236,67 +257,21 @@ void geoarrow_describe(ArrowSchema const* schema, ArrowArray const* array, int k
   }
   CSPT_EXPECTS(kind >= CSPT_GEOM_POINT && kind <= CSPT_GEOM_POLYGON, "unknown geometry kind");
   int const depth = list_depth(s);
-  // geometry levels each kind has above its points; one more = multi
+  // list levels each kind has above its points; one more = multi
   int const base = kind == CSPT_GEOM_POINT ? 0 : kind == CSPT_GEOM_POLYGON ? 2 : 1;
   CSPT_EXPECTS(depth == base || (depth == base + 1 && kind != CSPT_GEOM_POINT &&
                                  kind != CSPT_GEOM_MULTIPOINT),
                "list nesting does not match the geometry type");
   bool const multi = depth > base;
-  *out             = cspt_geoarrow_layout{};
-  out->kind        = kind;
-  out->num_geometries = static_cast<size_t>(len);
-  out->multi       = multi ? 1 : 0;
-  // walk the levels: counts only
-  for (int lvl = 0; lvl < depth; ++lvl) {
-    Level const l = list_level(s, a, start, len);
-    size_t* slot  = lvl == 0 && (multi || kind == CSPT_GEOM_MULTIPOINT) ? &out->num_geometry_offsets
-                    : (kind == CSPT_GEOM_POLYGON && lvl == depth - 1) ? &out->num_ring_offsets
-                                                                       : &out->num_part_offsets;
-    *slot = l.offsets.size();
-    s     = s->children[0];
-    a     = a->children[0];
-    start = l.child_start;
-    len   = l.child_len;
-  }
-  if ((kind == CSPT_GEOM_LINESTRING || kind == CSPT_GEOM_POLYGON) && !multi)
-    out->num_geometry_offsets = out->num_geometries + 1;
-  PointLayout const p = point_level(s, a, start, len);
-  out->dtype          = p.dtype;
-  out->interleaved    = p.interleaved ? 1 : 0;
-  out->num_points     = static_cast<size_t>(len);
-}
-
-void geoarrow_import(ArrowSchema const* schema, ArrowArray const* array, int kind_hint,
-                     cspt_allocator const* mr, cudaStream_t st_, cspt_geometry_column* out)
-{
-  Allocator const alloc(mr, st_);
-  cspt_geoarrow_layout lay;
-  geoarrow_describe(schema, array, kind_hint, &lay);
-  ArrowSchema const* s = schema;
-  ArrowArray const* a  = array;
-  int64_t start = 0, len = a->length;
-  if (starts_with(s->format, "+ud:")) {
-    int8_t const t = len > 0 ? static_cast<int8_t const*>(a->buffers[1])[a->offset] : 0;
-    start          = len > 0 ? static_cast<int32_t const*>(a->buffers[2])[a->offset] : 0;
-    s              = s->children[t];
-    a              = a->children[t];
-  }
-  int const kind  = lay.kind;
-  int const depth = list_depth(s);
-  bool const multi = lay.multi != 0;
-  *out             = cspt_geometry_column{};
-  out->kind        = kind;
-  out->dtype       = lay.dtype;
-  out->num_geometries = lay.num_geometries;
-  std::vector<uint32_t> geom, part, ring;
+  size_t const n   = static_cast<size_t>(len);
   for (int lvl = 0; lvl < depth; ++lvl) {
     Level l = list_level(s, a, start, len);
     if (lvl == 0 && (multi || kind == CSPT_GEOM_MULTIPOINT))
-      geom = std::move(l.offsets);
+      r.geom = std::move(l.offsets);
     else if (kind == CSPT_GEOM_POLYGON && lvl == depth - 1)
-      ring = std::move(l.offsets);
+      r.ring = std::move(l.offsets);
     else
-      part = std::move(l.offsets);
+      r.part = std::move(l.offsets);
     s     = s->children[0];
     a     = a->children[0];
     start = l.child_start;
@@ -304,25 +279,48 @@ void geoarrow_import(ArrowSchema const* schema, ArrowArray const* array, int kin
   }
   // single linestrings / polygons: one part per geometry
   if ((kind == CSPT_GEOM_LINESTRING || kind == CSPT_GEOM_POLYGON) && !multi) {
-    geom.resize(lay.num_geometries + 1);
-    for (size_t i = 0; i <= lay.num_geometries; ++i) geom[i] = static_cast<uint32_t>(i);
+    r.geom.resize(n + 1);
+    for (size_t i = 0; i <= n; ++i) r.geom[i] = static_cast<uint32_t>(i);
   }
-  PointLayout const p = point_level(s, a, start, len);
-  size_t const np     = static_cast<size_t>(len);
+  r.points                          = point_level(s, a, start, len);
+  r.layout.kind                     = kind;
+  r.layout.multi                    = multi ? 1 : 0;
+  r.layout.interleaved              = r.points.interleaved ? 1 : 0;
+  r.layout.dtype                    = r.points.dtype;
+  r.layout.num_geometries           = n;
+  r.layout.num_geometry_offsets     = r.geom.size();
+  r.layout.num_part_offsets         = r.part.size();
+  r.layout.num_ring_offsets         = r.ring.size();
+  r.layout.num_points               = static_cast<size_t>(len);
+  return r;
+}
+
+}  // namespace
+
+void geoarrow_import(ArrowSchema const* schema, ArrowArray const* array, int kind_hint,
+                     cspt_allocator const* mr, cudaStream_t st, cspt_geometry_column* out)
+{
+  Allocator const alloc(mr, st);
+  Parsed const r      = parse(schema, array, kind_hint);
+  PointLayout const& p = r.points;
+  size_t const np     = r.layout.num_points;
   size_t const es     = p.dtype == CSPT_FLOAT64 ? 8 : 4;
-  cudaStream_t const st = alloc.stream();
+  *out                = cspt_geometry_column{};
+  out->kind           = r.layout.kind;
+  out->dtype          = p.dtype;
+  out->num_geometries = r.layout.num_geometries;
   try {
-    if (!geom.empty()) {
-      out->geometry_offsets     = to_device(geom, alloc);
-      out->num_geometry_offsets = geom.size();
+    if (!r.geom.empty()) {
+      out->geometry_offsets     = to_device(r.geom, alloc);
+      out->num_geometry_offsets = r.geom.size();
     }
-    if (!part.empty()) {
-      out->part_offsets     = to_device(part, alloc);
-      out->num_part_offsets = part.size();
+    if (!r.part.empty()) {
+      out->part_offsets     = to_device(r.part, alloc);
+      out->num_part_offsets = r.part.size();
     }
-    if (!ring.empty()) {
-      out->ring_offsets     = to_device(ring, alloc);
-      out->num_ring_offsets = ring.size();
+    if (!r.ring.empty()) {
+      out->ring_offsets     = to_device(r.ring, alloc);
+      out->num_ring_offsets = r.ring.size();
     }
     out->num_points = np;
     out->x          = alloc.allocate(np * es);
@@ -330,22 +328,21 @@ void geoarrow_import(ArrowSchema const* schema, ArrowArray const* array, int kin
     if (np > 0) {
       if (p.interleaved) {
         Buffer<char> xy(alloc, 2 * np * es);
-        CSPT_CUDA_TRY(
-          cudaMemcpyAsync(xy.data(), p.xy, 2 * np * es, cudaMemcpyHostToDevice, st));
+        CSPT_CUDA_TRY(cudaMemcpyAsync(xy.data(), p.xy, 2 * np * es, cudaMemcpyHostToDevice, st));
         split_xy_kernel<<<grid_for(np, kArrowBlock, static_cast<unsigned>(num_sms()) * 8u),
                           kArrowBlock, 0, st>>>(xy.data(), np, es, static_cast<char*>(out->x),
                                                 static_cast<char*>(out->y));
         CSPT_CHECK_LAUNCH();
-        CSPT_CUDA_TRY(cudaStreamSynchronize(st));  // the staging buffer is released here
+        CSPT_CUDA_TRY(cudaStreamSynchronize(st));  // before the staging buffer is released
       } else {
         CSPT_CUDA_TRY(cudaMemcpyAsync(out->x, p.x, np * es, cudaMemcpyHostToDevice, st));
         CSPT_CUDA_TRY(cudaMemcpyAsync(out->y, p.y, np * es, cudaMemcpyHostToDevice, st));
       }
     }
-    // the host vectors above are pageable: the copies have been staged
+    // the offset vectors are pageable host memory owned here
     CSPT_CUDA_TRY(cudaStreamSynchronize(st));
   } catch (...) {
-    cspt_geometry_column_free(mr, out, st_);
+    cspt_geometry_column_free(mr, out, st);
     throw;
   }
 }
@@ -360,7 +357,41 @@ cspt_status cspt_geoarrow_describe(const struct ArrowSchema* schema,
 {
   return cspt::guarded([&] {
     CSPT_EXPECTS(schema && array && out, "arguments must not be null");
-    cspt::geoarrow_describe(schema, array, kind, out);
+    *out = cspt::parse(schema, array, kind).layout;
+  });
+}
+
+cspt_status cspt_geoarrow_read_host(const struct ArrowSchema* schema,
+                                    const struct ArrowArray* array, int kind,
+                                    uint32_t* geometry_offsets, uint32_t* part_offsets,
+                                    uint32_t* ring_offsets, void* x, void* y)
+{
+  return cspt::guarded([&] {
+    CSPT_EXPECTS(schema && array, "arguments must not be null");
+    cspt::Parsed const r = cspt::parse(schema, array, kind);
+    auto put = [](std::vector<uint32_t> const& v, uint32_t* dst) {
+      if (!v.empty()) {
+        CSPT_EXPECTS(dst, "output pointers must not be null");
+        std::memcpy(dst, v.data(), v.size() * 4);
+      }
+    };
+    put(r.geom, geometry_offsets);
+    put(r.part, part_offsets);
+    put(r.ring, ring_offsets);
+    size_t const np = r.layout.num_points;
+    size_t const es = r.points.dtype == CSPT_FLOAT64 ? 8 : 4;
+    if (np == 0) return;
+    CSPT_EXPECTS(x && y, "output pointers must not be null");
+    if (r.points.interleaved) {
+      char const* xy = static_cast<char const*>(r.points.xy);
+      for (size_t i = 0; i < np; ++i) {
+        std::memcpy(static_cast<char*>(x) + i * es, xy + 2 * i * es, es);
+        std::memcpy(static_cast<char*>(y) + i * es, xy + (2 * i + 1) * es, es);
+      }
+    } else {
+      std::memcpy(x, r.points.x, np * es);
+      std::memcpy(y, r.points.y, np * es);
+    }
   });
 }
 

@@ -388,6 +388,13 @@ cspt_status cspt_geoarrow_describe(const struct ArrowSchema* schema,
                                    const struct ArrowArray* array, int kind,
                                    cspt_geoarrow_layout* out);
 
+/* The same columns written to caller host buffers sized by
+ * cspt_geoarrow_describe (no device work; NULL for absent levels). */
+cspt_status cspt_geoarrow_read_host(const struct ArrowSchema* schema,
+                                    const struct ArrowArray* array, int kind,
+                                    uint32_t* geometry_offsets, uint32_t* part_offsets,
+                                    uint32_t* ring_offsets, void* x, void* y);
+
 /* Copies a GeoArrow array to device columns allocated with mr (one
  * host->device copy per buffer; interleaved coordinates are split on the
  * device).  Synchronises the stream.  The caller keeps ownership of the
