@@ -29,6 +29,18 @@ namespace cspt {
 namespace {
 
 constexpr int kPipBlock = 256;
+// the quadrant fast path: edges per warp list, slabs per quadrant
+constexpr uint32_t kFastCap   = 64;
+constexpr uint32_t kFastSlabs = 32;
+
+// The float32 slab of offset y (the lookup of filtered_test).
+__device__ inline uint32_t slab_lookup(float qy, float y0, float invh, uint32_t ns)
+{
+  float const fs = (qy - y0) * invh;
+  uint32_t sj    = 0;
+  if (fs > 0.0f) sj = fs >= static_cast<float>(ns) ? ns - 1 : static_cast<uint32_t>(fs);
+  return sj >= ns ? ns - 1 : sj;
+}
 // resident blocks per SM the registers are sized for (filtered / exact)
 #ifndef CSPT_PIP_MIN_BLOCKS
 #define CSPT_PIP_MIN_BLOCKS 6
@@ -78,6 +90,14 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
                   unsigned long long* __restrict__ next_pair)
 {
   int const lane      = threadIdx.x & 31;
+  int const wid       = threadIdx.x >> 5;
+  // the quadrant fast path's edge lists, per warp
+  __shared__ float2 s_party[kPipBlock / 32][kFastCap];
+  __shared__ uint32_t s_partk[kPipBlock / 32][kFastCap];
+  __shared__ float4 s_full[kPipBlock / 32][kFastCap];
+  __shared__ uint32_t s_fullk[kPipBlock / 32][kFastCap];
+  __shared__ uint8_t s_pbeg[kPipBlock / 32][kFastSlabs + 1];
+  __shared__ uint8_t s_fbeg[kPipBlock / 32][kFastSlabs + 1];
   float const gf      = Filtered ? static_cast<float>(*ix.grid) : 0.0f;
   bool const gok      = gf >= 1.17549435e-38f && gf < 1.0e30f;  // normal float grid step
   uint32_t nref       = 0;
@@ -110,25 +130,206 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
       float const dy = exact ? 0.0f : static_cast<float>(static_cast<int>(diy)) * gf;
       float4 const bx = ix.box32[poly];  // polygon box in its own frame
       float const mp  = ix.max_offset[poly];
+      // the quadrant's points in the polygon's frame lie in this box
+      float const qxmin = lf.uxmin - dx, qxmax = lf.uxmax - dx;
+      float const qymin = lf.uymin - dy, qymax = lf.uymax - dy;
+      float const mall  = fmaxf(fmaxf(mp, lf.m), fmaxf(fmaxf(fabsf(qxmin), fabsf(qxmax)),
+                                                      fmaxf(fabsf(qymin), fabsf(qymax))));
+      float const tol   = 4.76837158203125e-07f * mall;  // 2^-21 M
       // whole quadrant outside the polygon's box (beyond the tolerance)
-      if (!exact) {
-        float const qxmin = lf.uxmin - dx, qxmax = lf.uxmax - dx;
-        float const qymin = lf.uymin - dy, qymax = lf.uymax - dy;
-        float const mall  = fmaxf(fmaxf(mp, lf.m), fmaxf(fmaxf(fabsf(qxmin), fabsf(qxmax)),
-                                                        fmaxf(fabsf(qymin), fabsf(qymax))));
-        float const tol   = 4.76837158203125e-07f * mall;
-        if (qxmax < bx.x - tol || qxmin > bx.z + tol || qymax < bx.y - tol ||
-            qymin > bx.w + tol) {
-          for (uint32_t w = lane; w < nw; w += 32) bits[wb + w] = 0u;
-          if (lane == 0) counts[k] = 0;
-          continue;
-        }
+      if (!exact && (qxmax < bx.x - tol || qxmin > bx.z + tol || qymax < bx.y - tol ||
+                     qymin > bx.w + tol)) {
+        for (uint32_t w = lane; w < nw; w += 32) bits[wb + w] = 0u;
+        if (lane == 0) counts[k] = 0;
+        continue;
       }
       float const invh     = ix.inv_slab_h32[poly];
       float const invw     = Ordered ? ix.inv_bin_w32[poly] : 0.0f;
       uint32_t const ns    = ix.num_slabs[poly];
       uint32_t const slab0 = ix.slab_base[poly];
       uint32_t const vb = ix.vert_begin[poly], ve = ix.vert_end[poly];
+      // Quadrant-level edge classification.  Each point's float32 slab
+      // lookup is monotone in y, so the quadrant's points fall in slabs
+      // j0..j1 and those of slab j in a band of y (the slab's extent widened
+      // by the lookup error, 1/32 slab, and tol, and clipped to the box).
+      // Per slab the warp classifies the slab's edges once against the box
+      // [qxmin, qxmax] x band, with the filter's margins:
+      //   x entirely left of the box, or y entirely above / below the band:
+      //     never toggles, never on the edge;
+      //   x entirely right and y across the whole band: toggles for every
+      //     point of the slab (the crossing is right of the point by more
+      //     than tol and the edge rises by more than 2 tol, so the
+      //     reference's float64 comparison is decided) -> a common parity;
+      //   x entirely right, y partly: the toggle is the y-flags test alone;
+      //   x overlapping the box: the full per-point test.
+      // Exactly vertical edges keep their x-only check (the vertical list).
+      // (the ordered index, used by plans evaluated many times, keeps its
+      // per-bin windows: its launches use small blocks that these per-warp
+      // lists would starve of occupancy)
+      bool fast = false, vcheck = false;
+      uint32_t base = 0, j0 = 0, jspan = 0;
+      if constexpr (!Ordered) {
+        if (!exact && mall * invh <= 16384.0f) {
+          j0                  = slab_lookup(qymin, bx.y, invh, ns);
+          uint32_t const j1   = slab_lookup(qymax, bx.y, invh, ns);
+          jspan               = j1 - j0;
+          if (jspan < kFastSlabs) {
+            fast              = true;
+            float const hs    = invh > 0.0f ? 1.0f / invh : 0.0f;
+            float const dlt   = tol + 0.03125f * hs;
+            unsigned const lt = (1u << lane) - 1u;
+            uint32_t npart = 0, nfull = 0;
+            for (uint32_t j = j0; j <= j1 && fast; ++j) {
+              uint32_t const jj = j - j0;
+              if (lane == 0) {
+                s_pbeg[wid][jj] = static_cast<uint8_t>(npart);
+                s_fbeg[wid][jj] = static_cast<uint8_t>(nfull);
+              }
+              float const ylo = j == 0 ? qymin : fmaxf(qymin, __fmaf_rn(static_cast<float>(j), hs, bx.y) - dlt);
+              float const yhi = j + 1 >= ns ? qymax
+                                            : fminf(qymax, __fmaf_rn(static_cast<float>(j + 1), hs, bx.y) + dlt);
+              uint32_t const sidx = slab0 + j;
+              uint32_t const e0 = ix.slab_start[sidx], e1 = ix.slab_start[sidx + 1];
+              for (uint32_t t0 = e0; t0 < e1; t0 += 32) {
+                uint32_t const kk = t0 + lane;
+                bool const has    = kk < e1;
+                float4 const e    = has ? ix.slab_e32[kk] : make_float4(0.f, 0.f, 0.f, 0.f);
+                float const exmin = fminf(e.x, e.z), exmax = fmaxf(e.x, e.z);
+                float const eymin = fminf(e.y, e.w), eymax = fmaxf(e.y, e.w);
+                int cls = 0;  // 0 none, 1 every point, 2 y-test, 3 full test
+                if (has && !(exmax < qxmin - tol) && !(eymin > yhi + tol || eymax < ylo - tol)) {
+                  if (exmin > qxmax + tol)
+                    cls = (eymin < ylo - tol && eymax > yhi + tol) ? 1 : 2;
+                  else
+                    cls = 3;
+                }
+                if (__popc(__ballot_sync(0xFFFFFFFFu, cls == 1)) & 1) base ^= 1u << jj;
+                unsigned const bp = __ballot_sync(0xFFFFFFFFu, cls == 2);
+                unsigned const bf = __ballot_sync(0xFFFFFFFFu, cls == 3);
+                if (npart + __popc(bp) > kFastCap || nfull + __popc(bf) > kFastCap) {
+                  fast = false;
+                  break;
+                }
+                if (cls == 2) {
+                  uint32_t const slot = npart + __popc(bp & lt);
+                  s_party[wid][slot]  = make_float2(e.y, e.w);
+                  s_partk[wid][slot]  = kk;
+                }
+                if (cls == 3) {
+                  uint32_t const slot = nfull + __popc(bf & lt);
+                  s_full[wid][slot]   = e;
+                  s_fullk[wid][slot]  = kk;
+                }
+                npart += __popc(bp);
+                nfull += __popc(bf);
+              }
+            }
+            if (fast && lane == 0) {
+              s_pbeg[wid][j1 - j0 + 1] = static_cast<uint8_t>(npart);
+              s_fbeg[wid][j1 - j0 + 1] = static_cast<uint8_t>(nfull);
+            }
+            __syncwarp();
+            if (fast && vb < ve) {
+              // a vertical edge within tol of the box's x-range
+              uint32_t lo = vb, hi = ve;
+              float const key = qxmin - tol;
+              while (lo < hi) {
+                uint32_t const mid = (lo + hi) >> 1;
+                if (ix.vert_x32[mid] < key)
+                  lo = mid + 1;
+                else
+                  hi = mid;
+              }
+              vcheck = lo < ve && ix.vert_x32[lo] <= qxmax + tol;
+            }
+          }
+        }
+      }
+      if (fast) {
+        float const eb = __fmaf_rn(7.62939453125e-06f * mall, mall, 7.52316384526264e-37f);
+        for (uint32_t c = 0; c < len; c += 32) {
+          uint64_t const pos = off + c + lane;
+          bool hit           = false;
+          if (c + lane < len && pos < npi) {
+            float2 const uv = u[pos];
+            float const qx = uv.x - dx, qy = uv.y - dy;
+            // in [0, jspan]: the lookup is monotone and qy lies in the box
+            uint32_t const jj = min(slab_lookup(qy, bx.y, invh, ns) - j0, jspan);
+            bool within       = (base >> jj) & 1u;
+            uint32_t const pb = s_pbeg[wid][jj], pe = s_pbeg[wid][jj + 1];
+            uint32_t const fb = s_fbeg[wid][jj], fe = s_fbeg[wid][jj + 1];
+            bool on_edge   = false;
+            bool have64    = false;
+            double px64 = 0.0, py64 = 0.0;
+            auto load = [&] {
+              if (!have64) {
+                uint32_t const pi = point_indices[pos];
+                px64              = x[pi];
+                py64              = y[pi];
+                have64            = true;
+              }
+            };
+            auto exact_at = [&](uint32_t kk) {
+              ++nref;
+              load();
+              uint32_t const v  = ix.slab_edges[kk] & kEntryVertex;
+              uint32_t const pv = ix.prev_vertex[v];
+              return exact_edge<double>(px64, py64, ix.vx[v], ix.vy[v], ix.vx[pv], ix.vy[pv]);
+            };
+            if (vcheck) {
+              uint32_t lo = vb, hi = ve;
+              float const key = qx - tol;
+              while (lo < hi) {
+                uint32_t const mid = (lo + hi) >> 1;
+                if (ix.vert_x32[mid] < key)
+                  lo = mid + 1;
+                else
+                  hi = mid;
+              }
+              if (lo < ve && ix.vert_x32[lo] <= qx + tol) {
+                load();
+                on_edge = sorted_has<double>(ix.vert_x, vb, ve, px64);
+              }
+            }
+            for (uint32_t t = pb; t < pe && !on_edge; ++t) {
+              float2 const yy = s_party[wid][t];
+              float const ya = yy.x - qy, yb = yy.y - qy;
+              if (fabsf(ya) <= tol || fabsf(yb) <= tol) {
+                int const ee = exact_at(s_partk[wid][t]);
+                if (ee == 2) on_edge = true;
+                if (ee == 1) within = !within;
+              } else if ((ya > 0.0f) != (yb > 0.0f)) {
+                within = !within;
+              }
+            }
+            for (uint32_t t = fb; t < fe && !on_edge; ++t) {
+              float4 const e = s_full[wid][t];
+              float const ya = e.y - qy, yb = e.w - qy;
+              bool const y1  = ya > 0.0f;
+              bool const y0  = yb > 0.0f;
+              float const cr = __fmaf_rn(qx - e.x, e.w - e.y, -((e.z - e.x) * (qy - e.y)));
+              bool const undecided =
+                fabsf(ya) <= tol || fabsf(yb) <= tol ||
+                (fabsf(cr) <= eb &&
+                 (y1 != y0 || !(qx < fminf(e.x, e.z) - tol || qx > fmaxf(e.x, e.z) + tol)));
+              if (!undecided) {
+                if (y1 != y0 && ((cr < 0.0f) != y1)) within = !within;
+                continue;
+              }
+              int const ee = exact_at(s_fullk[wid][t]);
+              if (ee == 2) on_edge = true;
+              if (ee == 1) within = !within;
+            }
+            hit = within && !on_edge;
+          }
+          unsigned const w = __ballot_sync(0xFFFFFFFFu, hit);
+          if (lane == 0) bits[wb + (c >> 5)] = w;
+          cnt += __popc(w);
+        }
+        __syncwarp();  // the next pair rewrites this warp's edge lists
+        if (lane == 0) counts[k] = cnt;
+        continue;
+      }
       for (uint32_t c = 0; c < len; c += 32) {
         uint64_t const pos = off + c + lane;
         bool hit           = false;
