@@ -30,8 +30,8 @@ namespace {
 
 constexpr int kPipBlock = 256;
 // the quadrant fast path: edges per warp list, slabs per quadrant
-constexpr uint32_t kFastCap   = 64;
-constexpr uint32_t kFastSlabs = 32;
+constexpr uint32_t kFastCap   = 96;
+constexpr uint32_t kFastSlabs = 31;
 
 // The float32 slab of offset y (the lookup of filtered_test).
 __device__ inline uint32_t slab_lookup(float qy, float y0, float invh, uint32_t ns)
@@ -96,8 +96,12 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
   __shared__ uint32_t s_partk[kPipBlock / 32][kFastCap];
   __shared__ float4 s_full[kPipBlock / 32][kFastCap];
   __shared__ uint32_t s_fullk[kPipBlock / 32][kFastCap];
+  __shared__ uint8_t s_pslab[kPipBlock / 32][kFastCap];
+  __shared__ uint8_t s_fslab[kPipBlock / 32][kFastCap];
   __shared__ uint8_t s_pbeg[kPipBlock / 32][kFastSlabs + 1];
   __shared__ uint8_t s_fbeg[kPipBlock / 32][kFastSlabs + 1];
+  __shared__ uint32_t s_start[kPipBlock / 32][kFastSlabs + 1];
+  __shared__ uint32_t s_base[kPipBlock / 32];
   float const gf      = Filtered ? static_cast<float>(*ix.grid) : 0.0f;
   bool const gok      = gf >= 1.17549435e-38f && gf < 1.0e30f;  // normal float grid step
   uint32_t nref       = 0;
@@ -178,57 +182,92 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
             float const hs    = invh > 0.0f ? 1.0f / invh : 0.0f;
             float const dlt   = tol + 0.03125f * hs;
             unsigned const lt = (1u << lane) - 1u;
+            // the entries of slabs j0..j1 are contiguous: their starts
+            // (jspan + 2 <= 32 values) bound one stream of entries
+            uint32_t const st = lane <= jspan + 1 ? ix.slab_start[slab0 + j0 + lane] : 0u;
+            if (lane <= jspan + 1) s_start[wid][lane] = st;
+            if (lane == 0) s_base[wid] = 0u;
+            uint32_t const E0 = __shfl_sync(0xFFFFFFFFu, st, 0);
+            uint32_t const E1 = __shfl_sync(0xFFFFFFFFu, st, static_cast<int>(jspan + 1));
+            __syncwarp();
             uint32_t npart = 0, nfull = 0;
-            for (uint32_t j = j0; j <= j1 && fast; ++j) {
-              uint32_t const jj = j - j0;
-              if (lane == 0) {
-                s_pbeg[wid][jj] = static_cast<uint8_t>(npart);
-                s_fbeg[wid][jj] = static_cast<uint8_t>(nfull);
+            for (uint32_t t0 = E0; t0 < E1; t0 += 32) {
+              uint32_t const kk = t0 + lane;
+              bool const has    = kk < E1;
+              // the entry's slab: the last start <= kk
+              uint32_t lo = 0, hi = jspan + 1;
+              while (hi - lo > 1) {
+                uint32_t const mid = (lo + hi) >> 1;
+                if (s_start[wid][mid] <= kk)
+                  lo = mid;
+                else
+                  hi = mid;
               }
+              uint32_t const jj = lo, j = j0 + lo;
               float const ylo = j == 0 ? qymin : fmaxf(qymin, __fmaf_rn(static_cast<float>(j), hs, bx.y) - dlt);
               float const yhi = j + 1 >= ns ? qymax
                                             : fminf(qymax, __fmaf_rn(static_cast<float>(j + 1), hs, bx.y) + dlt);
-              uint32_t const sidx = slab0 + j;
-              uint32_t const e0 = ix.slab_start[sidx], e1 = ix.slab_start[sidx + 1];
-              for (uint32_t t0 = e0; t0 < e1; t0 += 32) {
-                uint32_t const kk = t0 + lane;
-                bool const has    = kk < e1;
-                float4 const e    = has ? ix.slab_e32[kk] : make_float4(0.f, 0.f, 0.f, 0.f);
-                float const exmin = fminf(e.x, e.z), exmax = fmaxf(e.x, e.z);
-                float const eymin = fminf(e.y, e.w), eymax = fmaxf(e.y, e.w);
-                int cls = 0;  // 0 none, 1 every point, 2 y-test, 3 full test
-                if (has && !(exmax < qxmin - tol) && !(eymin > yhi + tol || eymax < ylo - tol)) {
-                  if (exmin > qxmax + tol)
-                    cls = (eymin < ylo - tol && eymax > yhi + tol) ? 1 : 2;
-                  else
-                    cls = 3;
-                }
-                if (__popc(__ballot_sync(0xFFFFFFFFu, cls == 1)) & 1) base ^= 1u << jj;
-                unsigned const bp = __ballot_sync(0xFFFFFFFFu, cls == 2);
-                unsigned const bf = __ballot_sync(0xFFFFFFFFu, cls == 3);
-                if (npart + __popc(bp) > kFastCap || nfull + __popc(bf) > kFastCap) {
-                  fast = false;
-                  break;
-                }
-                if (cls == 2) {
-                  uint32_t const slot = npart + __popc(bp & lt);
-                  s_party[wid][slot]  = make_float2(e.y, e.w);
-                  s_partk[wid][slot]  = kk;
-                }
-                if (cls == 3) {
-                  uint32_t const slot = nfull + __popc(bf & lt);
-                  s_full[wid][slot]   = e;
-                  s_fullk[wid][slot]  = kk;
-                }
-                npart += __popc(bp);
-                nfull += __popc(bf);
+              float4 const e    = has ? ix.slab_e32[kk] : make_float4(0.f, 0.f, 0.f, 0.f);
+              float const exmin = fminf(e.x, e.z), exmax = fmaxf(e.x, e.z);
+              float const eymin = fminf(e.y, e.w), eymax = fmaxf(e.y, e.w);
+              int cls = 0;  // 0 none, 1 every point, 2 y-test, 3 full test
+              if (has && !(exmax < qxmin - tol) && !(eymin > yhi + tol || eymax < ylo - tol)) {
+                if (exmin > qxmax + tol)
+                  cls = (eymin < ylo - tol && eymax > yhi + tol) ? 1 : 2;
+                else
+                  cls = 3;
               }
-            }
-            if (fast && lane == 0) {
-              s_pbeg[wid][j1 - j0 + 1] = static_cast<uint8_t>(npart);
-              s_fbeg[wid][j1 - j0 + 1] = static_cast<uint8_t>(nfull);
+              if (cls == 1) atomicXor(&s_base[wid], 1u << jj);
+              unsigned const bp = __ballot_sync(0xFFFFFFFFu, cls == 2);
+              unsigned const bf = __ballot_sync(0xFFFFFFFFu, cls == 3);
+              if (npart + __popc(bp) > kFastCap || nfull + __popc(bf) > kFastCap) {
+                fast = false;
+                break;
+              }
+              // lanes hold increasing entries, so the lists stay in slab order
+              if (cls == 2) {
+                uint32_t const slot = npart + __popc(bp & lt);
+                s_party[wid][slot]  = make_float2(e.y, e.w);
+                s_partk[wid][slot]  = kk;
+                s_pslab[wid][slot]  = static_cast<uint8_t>(jj);
+              }
+              if (cls == 3) {
+                uint32_t const slot = nfull + __popc(bf & lt);
+                s_full[wid][slot]   = e;
+                s_fullk[wid][slot]  = kk;
+                s_fslab[wid][slot]  = static_cast<uint8_t>(jj);
+              }
+              npart += __popc(bp);
+              nfull += __popc(bf);
             }
             __syncwarp();
+            if (fast) {
+              // each slab's list range: lane jj counts the entries of lower
+              // slabs (the lists are sorted by slab)
+              if (lane <= jspan + 1) {
+                uint32_t lo = 0, hi = npart;
+                while (lo < hi) {
+                  uint32_t const mid = (lo + hi) >> 1;
+                  if (s_pslab[wid][mid] < static_cast<uint32_t>(lane))
+                    lo = mid + 1;
+                  else
+                    hi = mid;
+                }
+                s_pbeg[wid][lane] = static_cast<uint8_t>(lo);
+                lo = 0;
+                hi = nfull;
+                while (lo < hi) {
+                  uint32_t const mid = (lo + hi) >> 1;
+                  if (s_fslab[wid][mid] < static_cast<uint32_t>(lane))
+                    lo = mid + 1;
+                  else
+                    hi = mid;
+                }
+                s_fbeg[wid][lane] = static_cast<uint8_t>(lo);
+              }
+              __syncwarp();
+              base = s_base[wid];
+            }
             if (fast && vb < ve) {
               // a vertical edge within tol of the box's x-range
               uint32_t lo = vb, hi = ve;
