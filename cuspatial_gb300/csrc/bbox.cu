@@ -6,6 +6,8 @@
 // so the warp reduces raw coordinates and applies r once.  reduce_by_key emits
 // no row for a geometry without vertices, so rows are placed at the rank of
 // the geometry among non-empty ones; the rows left at the end are NaN.
+#include <climits>
+
 #include "common.cuh"
 #include "scan.cuh"
 
@@ -16,6 +18,16 @@ template <typename T>
 __device__ inline T dmin(T a, T b)
 {
   return fmin(a, b);
+}
+// Order-preserving integer image of a non-NaN double (-0 sorts below +0).
+__device__ inline long long order_key(double v)
+{
+  long long const b = __double_as_longlong(v);
+  return b >= 0 ? b : (b ^ 0x7FFFFFFFFFFFFFFFLL);
+}
+__device__ inline double from_order_key(long long k)
+{
+  return __longlong_as_double(k >= 0 ? k : (k ^ 0x7FFFFFFFFFFFFFFFLL));
 }
 template <typename T>
 __device__ inline T dmax(T a, T b)
@@ -44,20 +56,55 @@ __global__ void bbox_kernel(uint32_t const* __restrict__ vbegin_off,
       ve = vend_off[g];
     }
     if (ve <= vb) continue;
-    T mnx = x[vb], mny = y[vb], mxx = x[vb], mxy = y[vb];
-    for (size_t v = vb + lane; v < ve; v += 32) {
-      T const px = x[v], py = y[v];
-      mnx        = dmin(mnx, px);
-      mny        = dmin(mny, py);
-      mxx        = dmax(mxx, px);
-      mxy        = dmax(mxy, py);
-    }
+    T mnx, mny, mxx, mxy;
+    if constexpr (std::is_same<T, double>::value) {
+      // fmin / fmax (NaN skipped) on an order-preserving integer image: the
+      // integer pipe instead of this part's slow float64 min/max
+      long long k0 = LLONG_MAX, k1 = LLONG_MAX, k2 = LLONG_MIN, k3 = LLONG_MIN;
+      for (size_t v = vb + lane; v < ve; v += 32) {
+        double const px = x[v], py = y[v];
+        if (px == px) {
+          long long const kx = order_key(px);
+          k0                 = min(k0, kx);
+          k2                 = max(k2, kx);
+        }
+        if (py == py) {
+          long long const ky = order_key(py);
+          k1                 = min(k1, ky);
+          k3                 = max(k3, ky);
+        }
+      }
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      mnx = dmin(mnx, __shfl_xor_sync(0xFFFFFFFFu, mnx, off));
-      mny = dmin(mny, __shfl_xor_sync(0xFFFFFFFFu, mny, off));
-      mxx = dmax(mxx, __shfl_xor_sync(0xFFFFFFFFu, mxx, off));
-      mxy = dmax(mxy, __shfl_xor_sync(0xFFFFFFFFu, mxy, off));
+      for (int off = 16; off > 0; off >>= 1) {
+        k0 = min(k0, __shfl_xor_sync(0xFFFFFFFFu, k0, off));
+        k1 = min(k1, __shfl_xor_sync(0xFFFFFFFFu, k1, off));
+        k2 = max(k2, __shfl_xor_sync(0xFFFFFFFFu, k2, off));
+        k3 = max(k3, __shfl_xor_sync(0xFFFFFFFFu, k3, off));
+      }
+      double const nan = std::numeric_limits<double>::quiet_NaN();
+      mnx = k0 == LLONG_MAX ? nan : from_order_key(k0);
+      mny = k1 == LLONG_MAX ? nan : from_order_key(k1);
+      mxx = k2 == LLONG_MIN ? nan : from_order_key(k2);
+      mxy = k3 == LLONG_MIN ? nan : from_order_key(k3);
+    } else {
+      mnx = x[vb];
+      mny = y[vb];
+      mxx = x[vb];
+      mxy = y[vb];
+      for (size_t v = vb + lane; v < ve; v += 32) {
+        T const px = x[v], py = y[v];
+        mnx        = dmin(mnx, px);
+        mny        = dmin(mny, py);
+        mxx        = dmax(mxx, px);
+        mxy        = dmax(mxy, py);
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        mnx = dmin(mnx, __shfl_xor_sync(0xFFFFFFFFu, mnx, off));
+        mny = dmin(mny, __shfl_xor_sync(0xFFFFFFFFu, mny, off));
+        mxx = dmax(mxx, __shfl_xor_sync(0xFFFFFFFFu, mxx, off));
+        mxy = dmax(mxy, __shfl_xor_sync(0xFFFFFFFFu, mxy, off));
+      }
     }
     if (lane == 0) {
       uint32_t const o = row[g];

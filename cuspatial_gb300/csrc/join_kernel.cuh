@@ -72,6 +72,82 @@ __device__ inline int classify(TreeView const& t, uint32_t node, T bminx, T bmin
   return t.internal[node] ? 1 : 0;
 }
 
+// float32 pre-classification of a node for float64 trees.  The reference's
+// corner fl64(fma(k, s 2^sh, v_min)) and the float32 fmaf(k, fl32(s) 2^sh,
+// fl32(v_min)) both lie within u32 (|k s 2^sh| + |v_min| + |corner|) of the
+// exact value, so within eps = 2^-20 M of each other for
+// M = max(|v_min|) + s 2^(max_depth+1); a box side rounded to float32 lies
+// within its own margin eb.  Each of the reference's four comparisons is
+// decided when the float32 values are farther apart than both margins (and
+// the float32 rounding of the compared sums, covered by the factor 2 in
+// eps); otherwise the float64 expression decides.
+struct FloatBox {
+  float x0, y0, x1, y1;      // box sides, rounded to float32
+  float ex0, ey0, ex1, ey1;  // their margins
+  float vx, vy, s, eps;      // tree origin and scale in float32, corner margin
+};
+
+__device__ inline float side_margin(float v)
+{
+  return fmaf(fabsf(v), 4.76837158203125e-07f, 1.17549435e-38f);  // 2^-21 |v|
+}
+
+template <typename T>
+__device__ inline FloatBox float_box(T x0, T y0, T x1, T y1, T vminx, T vminy, T scale,
+                                     int max_depth)
+{
+  FloatBox f;
+  f.x0  = static_cast<float>(x0);
+  f.y0  = static_cast<float>(y0);
+  f.x1  = static_cast<float>(x1);
+  f.y1  = static_cast<float>(y1);
+  f.ex0 = side_margin(f.x0);
+  f.ey0 = side_margin(f.y0);
+  f.ex1 = side_margin(f.x1);
+  f.ey1 = side_margin(f.y1);
+  f.vx  = static_cast<float>(vminx);
+  f.vy  = static_cast<float>(vminy);
+  f.s   = static_cast<float>(scale);
+  float const m = fmaxf(fabsf(f.vx), fabsf(f.vy)) + ldexpf(f.s, max_depth + 1);
+  f.eps = 9.5367431640625e-07f * m;  // 2^-20 M (NaN or inf: nothing is decided)
+  return f;
+}
+
+// 2 disjoint, 1 internal and overlapping, 0 overlapping leaf; -1 undecided
+__device__ inline int classify_float(uint32_t key, int sh, FloatBox const& f)
+{
+  float const kx  = static_cast<float>(gather16(key));
+  float const ky  = static_cast<float>(gather16(key >> 1));
+  float const ls  = ldexpf(f.s, sh);
+  float const ax0 = fmaf(kx, ls, f.vx), ax1 = fmaf(kx + 1.0f, ls, f.vx);
+  float const ay0 = fmaf(ky, ls, f.vy), ay1 = fmaf(ky + 1.0f, ls, f.vy);
+  float const e   = f.eps;
+  // intersection.cuh:123-126: x0 > bmaxx || x1 < bminx || y0 > bmaxy || y1 < bminy
+  if (ax0 - e > f.x1 + f.ex1 || ax1 + e < f.x0 - f.ex0 || ay0 - e > f.y1 + f.ey1 ||
+      ay1 + e < f.y0 - f.ey0)
+    return 2;
+  if (ax0 + e < f.x1 - f.ex1 && ax1 - e > f.x0 + f.ex0 && ay0 + e < f.y1 - f.ey1 &&
+      ay1 - e > f.y0 + f.ey0)
+    return 1;  // overlapping: internal or leaf decided by the caller
+  return -1;
+}
+
+template <typename T>
+__device__ inline int classify_filtered(TreeView const& t, uint32_t node, FloatBox const& f,
+                                        T bminx, T bminy, T bmaxx, T bmaxy, T vminx, T vminy,
+                                        T scale, int max_depth)
+{
+  if constexpr (std::is_same<T, double>::value) {
+    uint32_t const key = t.key[node];
+    int const sh       = max_depth - 1 - t.level[node];
+    if (sh < 0) return 2;
+    int const c = classify_float(key, sh, f);
+    if (c == 2) return 2;
+    if (c == 1) return t.internal[node] ? 1 : 0;
+  }
+  return classify<T>(t, node, bminx, bminy, bmaxx, bmaxy, vminx, vminy, scale, max_depth);
+}
+
 // Walks the tree for box b; calls emit(node) for every intersecting leaf.
 // Returns false when the private stack would overflow (malformed tree).
 template <typename T, typename Emit>
@@ -132,6 +208,8 @@ __global__ void __launch_bounds__(kJoinWarps * 32)
        b += nwarps) {
     T const x0 = bminx[b], y0 = bminy[b], x1 = bmaxx[b], y1 = bmaxy[b];
     BoxTree<T> const bt = trees(b);
+    FloatBox const fbox = float_box<T>(x0, y0, x1, y1, bt.vminx, bt.vminy, bt.scale,
+                                       bt.max_depth);
     uint32_t const L0   = bt.L0;
     uint32_t found      = 0;
     uint32_t p     = Write ? pos[b] : 0u;
@@ -166,7 +244,8 @@ __global__ void __launch_bounds__(kJoinWarps * 32)
         if (node >= bt.nq) {
           bad = true;
         } else {
-          c = classify<T>(t, g, x0, y0, x1, y1, bt.vminx, bt.vminy, bt.scale, bt.max_depth);
+          c = classify_filtered<T>(t, g, fbox, x0, y0, x1, y1, bt.vminx, bt.vminy, bt.scale,
+                                   bt.max_depth);
         }
       }
       unsigned const leaves = __ballot_sync(0xFFFFFFFFu, c == 0);

@@ -22,10 +22,16 @@ constexpr int kMaxSlabs = 4096;
 // about (1 + 1/density) * sum|rise| / height edges (the edges crossing it plus
 // those ending inside it) and the index holds (1 + density) entries per edge.
 // Denser slabs shorten every candidate's edge walk at the cost of index
-// memory and build time; measured on the 100k-polygon, 8-512-vertex star
-// set, density 4 minimises build + float32 evaluation and density 8 the
-// float64-only evaluation.
-constexpr double kSlabDensityFloat32 = 4.0;
+// memory and build time.  Measured on the 100k-polygon, 8-512-vertex star
+// set (build + evaluation): density 2 for the one-shot float32 index, whose
+// pair kernel classifies a quadrant's slab entries once (1: 12.90 ms,
+// 2: 12.51, 3: 12.71, 4: 13.29); 4 for the ordered index, whose per-point
+// windows gain from shorter slabs; 8 for the float64-only evaluation.
+#ifndef CSPT_SLAB_DENSITY32
+#define CSPT_SLAB_DENSITY32 2.0
+#endif
+constexpr double kSlabDensityFloat32 = CSPT_SLAB_DENSITY32;
+constexpr double kSlabDensityOrdered = 4.0;
 constexpr double kSlabDensityFloat64 = 8.0;
 __device__ inline uint32_t choose_slabs(uint32_t nv, double height, double sum_rise,
                                         double density)
@@ -506,16 +512,6 @@ __global__ void __launch_bounds__(kIdxBlock)
 // than kSortSlab entries get an empty crossing set (every edge is tested).
 constexpr int kSortSlab = 64;
 
-__device__ inline uint32_t warp_min_u32(uint32_t v)
-{
-  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
-  return v;
-}
-__device__ inline uint32_t warp_max_u32(uint32_t v)
-{
-  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
-  return v;
-}
 
 // One warp per slab; lane l holds entries l and l + 32 (kSortSlab = 64).
 __global__ void __launch_bounds__(kIdxBlock)
@@ -732,7 +728,9 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
     index_count_kernel<T><<<grd, kIdxBlock, 0, s>>>(
       po, ro, vx, vy, np, pminx_.data(), pminy_.data(), pmaxx_.data(), pmaxy_.data(),
       invh_.data(), nslab_.data(), nent.data(), nvert.data(), exact_.data(), prev_.data(),
-      spans.data(), yslab.data(), build_float32 ? kSlabDensityFloat32 : kSlabDensityFloat64);
+      spans.data(), yslab.data(),
+      build_float32 ? (order_slabs ? kSlabDensityOrdered : kSlabDensityFloat32)
+                    : kSlabDensityFloat64);
     CSPT_CHECK_LAUNCH();
   }
   grid_kernel<T><<<1, 1024, 0, s>>>(pminx_.data(), pminy_.data(), pmaxx_.data(), pmaxy_.data(),
