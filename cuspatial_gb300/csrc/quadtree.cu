@@ -261,14 +261,20 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
 
   Buffer<uint32_t> keys(alloc, n), keys_alt(alloc, n);
   Buffer<uint32_t> idx(alloc, n), idx_alt(alloc, n);
-  morton_keys_kernel<T><<<grd, blk, 0, s>>>(x, y, n, minx, miny, maxx, maxy, scale,
-                                            T{1} / scale, d, keys.data());
-  CSPT_CHECK_LAUNCH();
+  {
+    KernelTimer kt("quadtree_keys", s);
+    morton_keys_kernel<T><<<grd, blk, 0, s>>>(x, y, n, minx, miny, maxx, maxy, scale,
+                                              T{1} / scale, d, keys.data());
+    CSPT_CHECK_LAUNCH();
+  }
   // cells reach 2^d + 2, so the key needs 2(d+1) bits (2(d+2) below d = 2)
   int const key_bits = d >= 2 ? 2 * d + 2 : 2 * d + 4;
-  bool const alt     = radix_sort_pairs<uint32_t>(keys.data(), idx.data(), keys_alt.data(),
-                                              idx_alt.data(), n, 0, key_bits > 32 ? 32 : key_bits,
-                                              true, alloc);
+  bool alt;
+  {
+    KernelTimer kt("quadtree_sort", s);
+    alt = radix_sort_pairs<uint32_t>(keys.data(), idx.data(), keys_alt.data(), idx_alt.data(), n,
+                                     0, key_bits > 32 ? 32 : key_bits, true, alloc);
+  }
   Buffer<uint32_t>& skeys = alt ? keys_alt : keys;
   Buffer<uint32_t>& sidx  = alt ? idx_alt : idx;
   (alt ? keys : keys_alt).reset();
