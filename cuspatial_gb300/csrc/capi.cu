@@ -104,6 +104,41 @@ int num_sms()
   return sms;
 }
 
+cudaStream_t side_stream()
+{
+  struct Streams {
+    std::vector<cudaStream_t> by_device;
+    ~Streams()
+    {
+      for (cudaStream_t st : by_device)
+        if (st) (void)cudaStreamDestroy(st);
+    }
+  };
+  thread_local Streams t;
+  int dev = 0;
+  CSPT_CUDA_TRY(cudaGetDevice(&dev));
+  if (static_cast<size_t>(dev) >= t.by_device.size()) t.by_device.resize(dev + 1, nullptr);
+  if (!t.by_device[dev])
+    CSPT_CUDA_TRY(cudaStreamCreateWithFlags(&t.by_device[dev], cudaStreamNonBlocking));
+  return t.by_device[dev];
+}
+
+void StreamJoin::join()
+{
+  if (!side_) return;
+  cudaStream_t const side = side_;
+  side_                   = nullptr;
+  cudaEvent_t e           = nullptr;
+  if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess &&
+      cudaEventRecord(e, side) == cudaSuccess && cudaStreamWaitEvent(main_, e, 0) == cudaSuccess) {
+    (void)cudaEventDestroy(e);
+    return;
+  }
+  (void)cudaGetLastError();
+  if (e) (void)cudaEventDestroy(e);
+  (void)cudaStreamSynchronize(side);  // the host waits instead
+}
+
 uint64_t last_refined() { return t_last_refined; }
 
 namespace {

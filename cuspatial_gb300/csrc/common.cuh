@@ -203,6 +203,27 @@ inline unsigned grid_for(size_t n, unsigned block, unsigned cap = 1u << 20)
 
 int num_sms();
 
+// A second stream of the calling thread on the current device, for work that
+// overlaps the caller's stream inside one call (created on first use;
+// non-blocking with respect to the legacy default stream).
+cudaStream_t side_stream();
+
+// Makes `main` wait for everything enqueued on `side` so far, at join() or
+// when it goes out of scope (also while an exception unwinds), so that
+// buffers released on `main` afterwards are no longer in use on `side`.
+class StreamJoin {
+ public:
+  StreamJoin(cudaStream_t main, cudaStream_t side) : main_(main), side_(side) {}
+  ~StreamJoin() { join(); }
+  StreamJoin(StreamJoin const&)            = delete;
+  StreamJoin& operator=(StreamJoin const&) = delete;
+  void join();
+
+ private:
+  cudaStream_t main_;
+  cudaStream_t side_;
+};
+
 // ---------------------------------------------------------------------------
 // device helpers
 // ---------------------------------------------------------------------------

@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(256)
   uint32_t const ng   = *ngroups_p;
   double const g      = *gridp;
   double const ginv   = 1.0 / g;  // g is a power of two: v * ginv == v / g while 1/g is finite
-  bool const gi       = isfinite(ginv);
+  bool const ginv_ok  = isfinite(ginv);
   for (size_t gi = (blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5; gi < ng;
        gi += nwarps) {
     uint32_t const quad = pair_quad[group_start[gi]];
@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(256)
       x0                = x[i0];
       y0                = y[i0];
     }
-    double rx = rint(gi ? x0 * ginv : x0 / g), ry = rint(gi ? y0 * ginv : y0 / g);
+    double rx = rint(ginv_ok ? x0 * ginv : x0 / g), ry = rint(ginv_ok ? y0 * ginv : y0 / g);
     if (!(fabs(rx) < 4.0e18)) rx = 0.0;  // also NaN
     if (!(fabs(ry) < 4.0e18)) ry = 0.0;
     double const ax = rx * g, ay = ry * g;

@@ -41,6 +41,15 @@ __device__ inline uint32_t slab_lookup(float qy, float y0, float invh, uint32_t 
   if (fs > 0.0f) sj = fs >= static_cast<float>(ns) ? ns - 1 : static_cast<uint32_t>(fs);
   return sj >= ns ? ns - 1 : sj;
 }
+// Blocks of 256 threads per SM for the leaf frames (the index fill that runs
+// beside them takes what the frames leave; 2-8 measured within 1%).
+#ifndef CSPT_LEAF_BLOCKS_PER_SM
+#define CSPT_LEAF_BLOCKS_PER_SM 8
+#endif
+inline unsigned leaf_frame_grid(size_t npairs)
+{
+  return grid_for(npairs * 32, 256, static_cast<unsigned>(num_sms()) * CSPT_LEAF_BLOCKS_PER_SM);
+}
 // resident blocks per SM the registers are sized for (filtered / exact)
 #ifndef CSPT_PIP_MIN_BLOCKS
 #define CSPT_PIP_MIN_BLOCKS 6
@@ -171,7 +180,7 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
       // per-bin windows: its launches use small blocks that these per-warp
       // lists would starve of occupancy)
       bool fast = false, vcheck = false;
-      uint32_t base = 0, j0 = 0, jspan = 0;
+      uint32_t base = 0, j0 = 0, jspan = 0, npart_all = 0;
       if constexpr (!Ordered) {
         if (!exact && mall * invh <= 16384.0f) {
           j0                  = slab_lookup(qymin, bx.y, invh, ns);
@@ -266,7 +275,8 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
                 s_fbeg[wid][lane] = static_cast<uint8_t>(lo);
               }
               __syncwarp();
-              base = s_base[wid];
+              base      = s_base[wid];
+              npart_all = npart + nfull;
             }
             if (fast && vb < ve) {
               // a vertical edge within tol of the box's x-range
@@ -282,6 +292,24 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
               vcheck = lo < ve && ix.vert_x32[lo] <= qxmax + tol;
             }
           }
+        }
+      }
+      if (fast && npart_all == 0 && !vcheck) {
+        uint32_t const mask = (2u << jspan) - 1u;
+        if ((base & mask) == 0u || (base & mask) == mask) {
+          // no edge reaches the quadrant's band: every point has the slabs'
+          // common parity, the words are written without reading a point
+          bool const all      = (base & mask) != 0u;
+          uint64_t const vmax = off >= npi ? 0 : (npi - off < len ? npi - off : len);
+          for (uint32_t w = lane; w < nw; w += 32) {
+            uint64_t const b0 = static_cast<uint64_t>(w) * 32u;
+            uint32_t word     = 0u;
+            if (all && vmax > b0) word = vmax - b0 >= 32 ? 0xFFFFFFFFu : (1u << (vmax - b0)) - 1u;
+            bits[wb + w] = word;
+          }
+          __syncwarp();
+          if (lane == 0) counts[k] = all ? static_cast<uint32_t>(vmax) : 0u;
+          continue;
         }
       }
       if (fast) {
@@ -491,7 +519,6 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
 {
   cudaStream_t const s = alloc.stream();
   bool const filtered  = method == CSPT_METHOD_FILTERED && std::is_same<T, double>::value;
-  PolygonIndex<T> index(po, npo, ro, nro, vx, vy, nv, filtered, alloc);
   uint32_t const* qlen = tree->length;
   uint32_t const* qoff = tree->offset;
 
@@ -510,33 +537,49 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
   CSPT_CUDA_TRY(cudaMemsetAsync(refined.data(), 0, 2 * sizeof(unsigned long long), s));
   unsigned const blk = 256;
   unsigned const grd = grid_for(npairs * 32, blk, 152u * 8u * 4u);
+  // filtered: groups of consecutive pairs sharing a quadrant, each pair's
+  // group, and the leaf frames (float32 point offsets from the quadrant's
+  // anchor), which need only the index's anchor grid
+  Buffer<uint32_t> gstart, pgroup;
+  Buffer<float2> u;
+  Buffer<LeafFrame> frames;
+  if (filtered) {
+    gstart       = Buffer<uint32_t>(alloc, npairs + 1);
+    pgroup       = Buffer<uint32_t>(alloc, npairs);
+    uint32_t* gs = gstart.data();
+    uint32_t* pg = pgroup.data();
+    scan_apply<uint32_t>(
+      [pair_quad] __device__(size_t k) {
+        return (k == 0 || pair_quad[k] != pair_quad[k - 1]) ? 1u : 0u;
+      },
+      [gs, pg] __device__(size_t k, uint32_t e, uint32_t f) {
+        if (f) gs[e] = static_cast<uint32_t>(k);
+        pg[k] = e + f - 1u;
+      },
+      npairs, gs + npairs, alloc);
+    u      = Buffer<float2>(alloc, npi);
+    frames = Buffer<LeafFrame>(alloc, npairs);
+  }
+  // The leaf frames (a gather of the points, bound by HBM) run on a second
+  // stream while the index writes its slab entries: the sizing pass below
+  // synchronises the stream, so everything above is complete when the frames
+  // start, and `join` (destroyed before the index and the buffers above, also
+  // on an exception) orders the rest of the call after them.
+  PolygonIndex<T> index(po, npo, ro, nro, vx, vy, nv, filtered, alloc, false, filtered);
+  cudaStream_t const side = filtered ? side_stream() : nullptr;
+  StreamJoin join(s, side);
   if constexpr (std::is_same<T, double>::value) {
-    Buffer<uint32_t> gstart, pgroup;
-    Buffer<float2> u;
-    Buffer<LeafFrame> frames;
     if (filtered) {
-      // groups of consecutive pairs sharing a quadrant, and each pair's group
-      gstart = Buffer<uint32_t>(alloc, npairs + 1);
-      pgroup = Buffer<uint32_t>(alloc, npairs);
-      uint32_t* gs = gstart.data();
-      uint32_t* pg = pgroup.data();
-      scan_apply<uint32_t>(
-        [pair_quad] __device__(size_t k) {
-          return (k == 0 || pair_quad[k] != pair_quad[k - 1]) ? 1u : 0u;
-        },
-        [gs, pg] __device__(size_t k, uint32_t e, uint32_t f) {
-          if (f) gs[e] = static_cast<uint32_t>(k);
-          pg[k] = e + f - 1u;
-        },
-        npairs, gs + npairs, alloc);
-      u      = Buffer<float2>(alloc, npi);
-      frames = Buffer<LeafFrame>(alloc, npairs);
-      KernelTimer timer("leaf_frames", s);
-      leaf_frame_kernel<<<grd, blk, 0, s>>>(gs, gs + npairs, pair_quad, qlen, qoff, point_indices,
-                                            npi, x, y, index.view().grid, u.data(),
-                                            frames.data());
+      KernelTimer timer("leaf_frames", side);
+      leaf_frame_kernel<<<leaf_frame_grid(npairs), blk, 0, side>>>(
+        gstart.data(), gstart.data() + npairs, pair_quad, qlen, qoff, point_indices, npi, x, y,
+        index.grid(), u.data(), frames.data());
       CSPT_CHECK_LAUNCH();
     }
+  }
+  index.fill();
+  join.join();
+  if constexpr (std::is_same<T, double>::value) {
     KernelTimer timer("pip_bits", s);
     if (filtered)
       pip_pair_kernel<true>

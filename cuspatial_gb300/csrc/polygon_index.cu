@@ -689,9 +689,21 @@ __global__ void vert_end_kernel(uint32_t const* __restrict__ vbeg,
 }  // namespace
 
 template <typename T>
+struct PolygonIndex<T>::Sizing {
+  uint32_t const *po, *ro;
+  T const *vx, *vy;
+  size_t np, nslabs_total, nentries, nvertical;
+  bool build_float32, order_slabs;
+  unsigned grd;
+  Buffer<uint32_t> ebase, nvert, spans;
+  Buffer<float> yslab;
+  Allocator const* alloc;  // the caller's: the index's buffers keep pointing to it
+};
+
+template <typename T>
 PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro, size_t nro,
                               T const* vx, T const* vy, size_t nv, bool build_float32,
-                              Allocator const& alloc, bool order_slabs)
+                              Allocator const& alloc, bool order_slabs, bool defer_fill)
 {
   (void)nro;
   cudaStream_t const s = alloc.stream();
@@ -756,7 +768,30 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
   CSPT_CUDA_TRY(cudaStreamSynchronize(s));
   CSPT_EXPECTS(wtot[0] < (1ull << 32) && wtot[1] < (1ull << 32),
                "polygon set too large for the slab index (2^32 slab entries)");
-  size_t const nslabs_total = tot[0], nentries = tot[1], nvertical = tot[2];
+  sizing_.reset(new Sizing{po, ro, vx, vy, np, tot[0], tot[1], tot[2], build_float32, order_slabs,
+                           grd, std::move(ebase), std::move(nvert), std::move(spans),
+                           std::move(yslab), &alloc});
+  if (!defer_fill) fill();
+}
+
+template <typename T>
+PolygonIndex<T>::~PolygonIndex() = default;
+
+template <typename T>
+void PolygonIndex<T>::fill()
+{
+  if (!sizing_) return;
+  std::unique_ptr<Sizing> const z = std::move(sizing_);
+  Allocator const& alloc = *z->alloc;
+  cudaStream_t const s   = alloc.stream();
+  KernelTimer timer("polygon_index", s);
+  uint32_t const *po = z->po, *ro = z->ro;
+  T const *vx = z->vx, *vy = z->vy;
+  size_t const np = z->np, nslabs_total = z->nslabs_total, nentries = z->nentries,
+               nvertical = z->nvertical;
+  size_t const nv          = prev_.size();
+  bool const build_float32 = z->build_float32;
+  unsigned const grd       = z->grd;
   slab_start_ = Buffer<uint32_t>(alloc, nslabs_total + 1);
   slab_edges_ = Buffer<uint32_t>(alloc, nentries);
   if (build_float32) slab_e32_ = Buffer<float4>(alloc, nentries);
@@ -768,19 +803,19 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
   if (np > 0) {
     index_fill_kernel<T><<<grd, kIdxBlock, 0, s>>>(
       po, ro, vx, vy, np, pminx_.data(), pminy_.data(), pmaxx_.data(), pmaxy_.data(),
-      invh_.data(), nslab_.data(), slab_base_.data(), ebase.data(), vbeg_.data(), grid_.data(),
+      invh_.data(), nslab_.data(), slab_base_.data(), z->ebase.data(), vbeg_.data(), grid_.data(),
       build_float32, ax_.data(), ay_.data(), aix_.data(), aiy_.data(), box32_.data(),
-      invh32_.data(), maxoff_.data(), prev_.data(), spans.data(), edge32_.data(),
+      invh32_.data(), maxoff_.data(), prev_.data(), z->spans.data(), edge32_.data(),
       slab_start_.data(),
       slab_edges_.data(), slab_e32_.data(), vert_x_.data(), vert_x32_.data(), vxy32.data(),
-      yslab.data());
+      z->yslab.data());
     CSPT_CHECK_LAUNCH();
-    vert_end_kernel<<<grid_for(np, 256, 152u * 16u), 256, 0, s>>>(vbeg_.data(), nvert.data(),
+    vert_end_kernel<<<grid_for(np, 256, 152u * 16u), 256, 0, s>>>(vbeg_.data(), z->nvert.data(),
                                                                   np, vend_.data());
     CSPT_CHECK_LAUNCH();
   }
   vxy32.reset();
-  bool const ordered = build_float32 && order_slabs;
+  bool const ordered = build_float32 && z->order_slabs;
   slab_nfull_ = Buffer<uint32_t>(alloc, ordered ? nslabs_total : 0);
   slab_bins_  = Buffer<uint32_t>(alloc, ordered ? nslabs_total * kSlabBins : 0);
   invw32_     = Buffer<float>(alloc, ordered ? np : 0);
@@ -795,7 +830,7 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
     slab_edges_ = std::move(edges2);
     slab_e32_   = std::move(e32b);
   }
-  yslab.reset();
+  z->yslab.reset();
   v_ = PolygonIndexView<T>{po,
                            ro,
                            vx,

@@ -38,6 +38,8 @@
 // exact in float64 and, when below 2^24 grid steps, in float32.
 #pragma once
 
+#include <memory>
+
 #include "common.cuh"
 
 namespace cspt {
@@ -100,13 +102,25 @@ class PolygonIndex {
   // build the per-(slab, x-bin) windows.  It costs a pass over all slab
   // entries and pays off where the index is evaluated many times (batched
   // plans, resident polygon sets).
+  // defer_fill: return once the per-polygon boxes, slab counts and the anchor
+  // grid are on the device and the sizes are known (the call synchronises
+  // the stream for them); fill() then writes the slab entries.  Work that
+  // needs only grid() can run on another stream meanwhile.
   PolygonIndex(uint32_t const* poly_offsets, size_t num_poly_offsets,
                uint32_t const* ring_offsets, size_t num_ring_offsets, T const* vx, T const* vy,
                size_t num_vertices, bool build_float32, Allocator const& alloc,
-               bool order_slabs = false);
+               bool order_slabs = false, bool defer_fill = false);
+  ~PolygonIndex();
+  PolygonIndex(PolygonIndex const&)            = delete;
+  PolygonIndex& operator=(PolygonIndex const&) = delete;
+  void fill();
+  // device scalar: the anchor grid step (valid before fill())
+  T const* grid() const { return grid_.data(); }
   PolygonIndexView<T> view() const { return v_; }
 
  private:
+  struct Sizing;  // state carried from the sizing pass to fill()
+  std::unique_ptr<Sizing> sizing_;
   Buffer<T> pminx_, pminy_, pmaxx_, pmaxy_, ax_, ay_, invh_, vert_x_, grid_;
   Buffer<float> maxoff_, vert_x32_, invh32_;
   Buffer<long long> aix_, aiy_;
