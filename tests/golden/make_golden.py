@@ -16,8 +16,15 @@ Sources:
   python/cuspatial/cuspatial/tests/spatial/bounding/test_linestring_bounding_boxes.py
   cpp/tests/distance/point_linestring_distance_test.cu          (pairwise distance)
   cpp/tests/nearest_points/point_linestring_nearest_points_test.cu
+  python/cuspatial/cuspatial/tests/spatial/indexing/test_indexing.py
+  python/cuspatial/cuspatial/tests/spatial/join/test_spatial_join.py
+  python/cuspatial/cuspatial/tests/spatial/join/test_point_in_polygon.py
+
+The Python tests are parsed with the ast module and followed by a small
+evaluator (python_test_kats below); they are not imported or executed either.
 """
 
+import ast
 import json
 import os
 import re
@@ -395,6 +402,200 @@ def nearest_points_kats(root):
                 "the reference", cases=cases)
 
 
+# ---------------------------------------------------------------------------
+# The reference's Python tests.  Each test body is parsed (ast) and followed by
+# a small evaluator over the forms these tests use: literals, cudf.Series and
+# DataFrame become lists and dicts, GeoSeries constructors become geometry
+# records, every cuspatial.* call becomes an op record over its evaluated
+# arguments, and cudf.testing.assert_frame_equal pairs an op record (the
+# value under test) with its expected frame.  Tests parametrised by dtype are
+# followed once per dtype.  Anything outside those forms skips the test, and
+# the skipped tests are listed in the fixture.
+# ---------------------------------------------------------------------------
+_NP_NAMES = {"np.float32": "float32", "np.float64": "float64", "np.uint32": "uint32",
+             "np.uint8": "uint8", "np.bool_": "bool", "np.int8": "int8"}
+
+
+def _dotted(node):
+    if isinstance(node, ast.Name):
+        return node.id
+    if isinstance(node, ast.Attribute):
+        base = _dotted(node.value)
+        return base + "." + node.attr if base else None
+    return None
+
+
+class _Unsupported(Exception):
+    pass
+
+
+class _Eval:
+    def __init__(self, env, helpers):
+        self.env = dict(env)
+        self.helpers = helpers
+        self.checks = []
+
+    def ev(self, n):
+        if isinstance(n, ast.Constant):
+            return n.value
+        if isinstance(n, (ast.List, ast.Tuple)):
+            out = []
+            for e in n.elts:
+                if isinstance(e, ast.Starred):
+                    out.extend(self.ev(e.value))
+                else:
+                    out.append(self.ev(e))
+            return out
+        if isinstance(n, ast.Dict):
+            return {self.ev(k): self.ev(v) for k, v in zip(n.keys, n.values)}
+        if isinstance(n, ast.UnaryOp) and isinstance(n.op, ast.USub):
+            return -self.ev(n.operand)
+        if isinstance(n, ast.Compare) and len(n.ops) == 1 and isinstance(n.ops[0], ast.Eq):
+            return self.ev(n.left) == self.ev(n.comparators[0])
+        if isinstance(n, ast.Name):
+            if n.id in self.env:
+                return self.env[n.id]
+            raise _Unsupported("name " + n.id)
+        if isinstance(n, ast.Attribute) and _dotted(n) in _NP_NAMES:
+            return _NP_NAMES[_dotted(n)]
+        if isinstance(n, ast.Call):
+            return self.call(n)
+        raise _Unsupported(type(n).__name__)
+
+    def call(self, n):
+        f = n.func
+        if isinstance(f, ast.Attribute) and f.attr == "astype":
+            return self.ev(f.value)
+        if isinstance(f, ast.Attribute) and f.attr == "interleave_columns":
+            df = self.ev(f.value)
+            out = []
+            for a, b in zip(df["x"], df["y"]):
+                out += [a, b]
+            return out
+        name = _dotted(f)
+        args = []
+        for a in n.args:
+            if isinstance(a, ast.Starred):
+                args.extend(self.ev(a.value))
+            else:
+                args.append(self.ev(a))
+        kw = {k.arg: self.ev(k.value) for k in n.keywords}
+        if name == "cudf.Series":
+            return list(args[0]) if args else []
+        if name == "cudf.DataFrame":
+            return dict(args[0]) if args else {}
+        if name == "Point":
+            return [args[0], args[1]]
+        if name == "len":
+            return len(args[0])
+        if name in ("cp.arange", "np.arange"):
+            return list(range(args[0]))
+        if name == "cuspatial.GeoSeries":
+            if not args[0]:
+                return {"geometry": "empty"}
+            return {"geometry": "points", "xy": [c for p in args[0] for c in p]}
+        if name == "cuspatial.GeoSeries.from_points_xy":
+            return {"geometry": "points", "xy": args[0]}
+        if name == "cuspatial.GeoSeries.from_polygons_xy":
+            return {"geometry": "polygons", "xy": args[0], "ring_offset": args[1],
+                    "part_offset": args[2], "geometry_offset": args[3]}
+        if name == "cuspatial.GeoSeries.from_linestrings_xy":
+            return {"geometry": "linestrings", "xy": args[0], "part_offset": args[1],
+                    "geometry_offset": args[2]}
+        if name == "cudf.testing.assert_frame_equal":
+            self.checks.append((args[0], args[1]))
+            return None
+        if name and name.startswith("cuspatial."):
+            return {"op": name.split(".", 1)[1], "args": args}
+        if name in self.helpers:
+            fdef = self.helpers[name]
+            saved = dict(self.env)
+            for p, v in zip([a.arg for a in fdef.args.args], args):
+                self.env[p] = v
+            self.env.update(kw)
+            self.run(fdef.body)
+            self.env = saved
+            return None
+        raise _Unsupported("call " + str(name))
+
+    def run(self, body):
+        for st in body:
+            if isinstance(st, ast.Assign):
+                v = self.ev(st.value)
+                for t in st.targets:
+                    self.assign(t, v)
+            elif isinstance(st, ast.Expr):
+                if not isinstance(st.value, ast.Constant):  # docstrings
+                    self.ev(st.value)
+            elif isinstance(st, ast.If):
+                self.run(st.body if self.ev(st.test) else st.orelse)
+            else:
+                raise _Unsupported(type(st).__name__)
+
+    def assign(self, t, v):
+        if isinstance(t, ast.Name):
+            self.env[t.id] = v
+        elif isinstance(t, ast.Tuple) and isinstance(v, dict) and "op" in v:
+            for i, e in enumerate(t.elts):  # an op returning a pair
+                self.env[e.id] = dict(v, out=i)
+        elif isinstance(t, ast.Subscript):
+            self.ev(t.value)[self.ev(t.slice)] = v
+        else:
+            raise _Unsupported("assignment")
+
+
+def _dtype_params(fdef):
+    for d in fdef.decorator_list:
+        if (isinstance(d, ast.Call) and _dotted(d.func) == "pytest.mark.parametrize" and
+                isinstance(d.args[0], ast.Constant) and d.args[0].value == "dtype"):
+            return [_NP_NAMES.get(_dotted(e), getattr(e, "value", None)) for e in d.args[1].elts]
+    return None
+
+
+def python_test_kats(root):
+    files = ["python/cuspatial/cuspatial/tests/spatial/indexing/test_indexing.py",
+             "python/cuspatial/cuspatial/tests/spatial/join/test_spatial_join.py",
+             "python/cuspatial/cuspatial/tests/spatial/join/test_point_in_polygon.py"]
+    cases, skipped = [], []
+    for rel in files:
+        tree = ast.parse(open(os.path.join(root, rel)).read())
+        env, helpers, tests = {}, {}, []
+        for st in tree.body:
+            if isinstance(st, ast.Assign):
+                try:
+                    v = _Eval(env, helpers).ev(st.value)
+                except _Unsupported:
+                    continue
+                for t in st.targets:
+                    if isinstance(t, ast.Name):
+                        env[t.id] = v
+            elif isinstance(st, ast.FunctionDef):
+                if st.name.startswith("test_"):
+                    tests.append(st)
+                else:
+                    helpers[st.name] = st
+        for fdef in tests:
+            dtypes = _dtype_params(fdef) or [None]
+            for dt in dtypes:
+                e = _Eval(env, helpers)
+                if dt is not None:
+                    e.env["dtype"] = dt
+                try:
+                    e.run(fdef.body)
+                except (_Unsupported, KeyError, IndexError, TypeError) as exc:
+                    skipped.append(dict(source=rel, test=fdef.name, reason=str(exc)))
+                    break
+                for actual, expected in e.checks:
+                    if isinstance(expected, dict) and "op" in expected:
+                        actual, expected = expected, actual
+                    cases.append(dict(source="%s:%d" % (rel, fdef.lineno), test=fdef.name,
+                                      dtype=dt or "float64", actual=actual,
+                                      expected={str(k): v for k, v in expected.items()}))
+    return dict(note="each case: an op record (the value under test, built from the "
+                     "reference's Python API calls) and the frame the test expects",
+                cases=cases, skipped=skipped)
+
+
 def main():
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     here = os.path.dirname(os.path.abspath(__file__))
@@ -406,6 +607,7 @@ def main():
         "linestring_bounding_boxes_small.json": linestring_bbox_kat(root),
         "point_linestring_distance.json": point_linestring_distance_kats(root),
         "point_linestring_nearest_points.json": nearest_points_kats(root),
+        "python_tests.json": python_test_kats(root),
     }
     for name, data in outputs.items():
         with open(os.path.join(here, name), "w") as f:
