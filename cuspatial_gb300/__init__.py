@@ -8,17 +8,18 @@ the pairwise point-linestring distance and nearest points;
 they run hand-written CUDA kernels in libcuspatial_gb300.so through its C ABI.
 """
 
-from .api import (join_quadtree_and_bounding_boxes, last_refined_count,
+from .api import (HostRowsTooFew, join_quadtree_and_bounding_boxes, last_refined_count,
                   linestring_bounding_boxes, pairwise_point_in_polygon,
                   pairwise_point_linestring_distance, pairwise_point_linestring_nearest_points,
                   point_in_polygon, point_in_polygon_bitmask, polygon_bounding_boxes,
                   quadtree_on_points, quadtree_point_in_polygon,
-                  quadtree_point_to_nearest_linestring)
+                  quadtree_point_in_polygon_host, quadtree_point_to_nearest_linestring)
 from .contains import contains_properly, polygons_contains_properly
 from .geoseries import GeoSeries, Table
 
 __all__ = [
     "GeoSeries",
+    "HostRowsTooFew",
     "Table",
     "contains_properly",
     "join_quadtree_and_bounding_boxes",
@@ -33,5 +34,6 @@ __all__ = [
     "polygons_contains_properly",
     "quadtree_on_points",
     "quadtree_point_in_polygon",
+    "quadtree_point_in_polygon_host",
     "quadtree_point_to_nearest_linestring",
 ]

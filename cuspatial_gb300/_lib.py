@@ -105,6 +105,10 @@ def _declare(lib):
         _vp, _vp, _sz, ctypes.POINTER(CsptQuadtree), _vp, _sz, _vp, _vp, _sz, _vp, _sz, _vp, _sz,
         _vp, _vp, _sz, ctypes.c_int, ctypes.c_int, ctypes.POINTER(CsptAllocator), _vp,
         ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_sz)]
+    lib.cspt_quadtree_point_in_polygon_host.argtypes = [
+        _vp, _vp, _sz, ctypes.POINTER(CsptQuadtree), _vp, _sz, _vp, _vp, _sz, _vp, _sz, _vp, _sz,
+        _vp, _vp, _sz, ctypes.c_int, ctypes.c_int, ctypes.POINTER(CsptAllocator), _vp, _vp, _vp,
+        _sz, ctypes.POINTER(_sz)]
     lib.cspt_quadtree_point_to_nearest_linestring.argtypes = [
         _vp, _vp, _sz, ctypes.POINTER(CsptQuadtree), _vp, _sz, _vp, _vp, _sz, _vp, _sz, _vp, _vp,
         _sz, ctypes.c_int, ctypes.c_int, ctypes.POINTER(CsptAllocator), _vp, _vp, _vp, _vp,
@@ -160,7 +164,8 @@ def _declare(lib):
         getattr(lib, name).restype = ctypes.c_int
     for name in ("cspt_quadtree_on_points", "cspt_polygon_bounding_boxes",
                  "cspt_linestring_bounding_boxes", "cspt_join_quadtree_and_bounding_boxes",
-                 "cspt_quadtree_point_in_polygon", "cspt_quadtree_point_to_nearest_linestring"):
+                 "cspt_quadtree_point_in_polygon", "cspt_quadtree_point_in_polygon_host",
+                 "cspt_quadtree_point_to_nearest_linestring"):
         getattr(lib, name).restype = ctypes.c_int
     return lib
 

@@ -193,6 +193,59 @@ def quadtree_point_in_polygon(poly_quad_pairs, quadtree, point_indices, points: 
     return out
 
 
+class HostRowsTooFew(RuntimeError):
+    """The host arrays given to quadtree_point_in_polygon_host hold fewer rows
+    than the result; `rows` is the result's row count."""
+
+    def __init__(self, msg, rows):
+        super().__init__(msg)
+        self.rows = rows
+
+
+def quadtree_point_in_polygon_host(poly_quad_pairs, quadtree, point_indices, points: GeoSeries,
+                                   polygons: GeoSeries, polygon_index_out, point_index_out,
+                                   method="exact"):
+    """quadtree_point_in_polygon with the rows written into host tensors.
+
+    polygon_index_out and point_index_out are int32 CPU tensors of equal
+    length (page-locked, for the device-to-host copies to overlap the
+    evaluation, which runs in chunks of pairs).  Returns the number of rows
+    written, in the order of quadtree_point_in_polygon.  Raises HostRowsTooFew
+    (with the row count) when the tensors are too short.
+    """
+    if not contains_only_points(points):
+        raise ValueError("`point` Geoseries must contains only point geometries.")
+    if not contains_only_polygons(polygons):
+        raise ValueError("`polygons` Geoseries must contains only polygons geometries.")
+    for t in (polygon_index_out, point_index_out):
+        if t.device.type != "cpu" or t.dtype != torch.int32 or not t.is_contiguous():
+            raise ValueError("host outputs must be contiguous int32 CPU tensors")
+    cap = min(int(polygon_index_out.numel()), int(point_index_out.numel()))
+    lib = _lib.load()
+    st, keep = _tree_struct(quadtree)
+    pp = as_device_tensor(poly_quad_pairs["bbox_offset"] if "bbox_offset" in poly_quad_pairs
+                          else poly_quad_pairs["polygon_index"], dtype=torch.int32)
+    pq = as_device_tensor(poly_quad_pairs["quad_offset"], dtype=torch.int32)
+    pi = as_device_tensor(point_indices, dtype=torch.int32)
+    pts = points.points
+    poly = polygons.polygons
+    alloc = _lib.TorchAllocator(pts.x.device)
+    nn = ctypes.c_size_t()
+    status = lib.cspt_quadtree_point_in_polygon_host(
+        _lib.ptr(pp), _lib.ptr(pq), int(pp.numel()), ctypes.byref(st), _lib.ptr(pi),
+        int(pi.numel()), _lib.ptr(pts.x), _lib.ptr(pts.y), int(pts.x.numel()),
+        _lib.ptr(poly.part_offset), int(poly.part_offset.numel()), _lib.ptr(poly.ring_offset),
+        int(poly.ring_offset.numel()), _lib.ptr(poly.x), _lib.ptr(poly.y), int(poly.x.numel()),
+        _dtype_code(pts.x), _METHODS[method], alloc.ref, _lib.stream_ptr(),
+        polygon_index_out.data_ptr() if cap else None, point_index_out.data_ptr() if cap else None,
+        cap, ctypes.byref(nn))
+    del keep
+    if status != _lib.OK and int(nn.value) > cap:
+        raise HostRowsTooFew(lib.cspt_last_error_message().decode(), int(nn.value))
+    _lib.check(status, lib)
+    return int(nn.value)
+
+
 def quadtree_point_to_nearest_linestring(linestring_quad_pairs, quadtree, point_indices,
                                          points: GeoSeries, linestrings: GeoSeries,
                                          method="exact"):

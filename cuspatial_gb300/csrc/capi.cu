@@ -33,7 +33,7 @@ void quadtree_point_in_polygon(uint32_t const* pair_poly, uint32_t const* pair_q
                                size_t nro, void const* vx, void const* vy, size_t nv,
                                cspt_dtype dtype, cspt_method method, Allocator const& alloc,
                                uint32_t** out_poly, uint32_t** out_point, size_t* out_n,
-                               uint64_t* out_refined);
+                               uint64_t* out_refined, HostRows const* host = nullptr);
 void quadtree_point_to_nearest_linestring(uint32_t const* pair_ls, uint32_t const* pair_quad,
                                           size_t npairs, cspt_quadtree const* tree,
                                           uint32_t const* point_indices, size_t npi,
@@ -121,6 +121,16 @@ cudaStream_t side_stream()
   if (!t.by_device[dev])
     CSPT_CUDA_TRY(cudaStreamCreateWithFlags(&t.by_device[dev], cudaStreamNonBlocking));
   return t.by_device[dev];
+}
+
+void stream_wait(cudaStream_t waiter, cudaStream_t on)
+{
+  cudaEvent_t e = nullptr;
+  CSPT_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  cudaError_t err = cudaEventRecord(e, on);
+  if (err == cudaSuccess) err = cudaStreamWaitEvent(waiter, e, 0);
+  (void)cudaEventDestroy(e);
+  CSPT_CUDA_TRY(err);
 }
 
 void StreamJoin::join()
@@ -384,6 +394,46 @@ cspt_status cspt_quadtree_point_in_polygon(
                               ring_offsets, num_ring_offsets, poly_x, poly_y, num_poly_vertices,
                               dtype, method, alloc, out_polygon_index, out_point_index,
                               out_num_pairs, &refined);
+    t_last_refined = refined;
+  });
+}
+
+cspt_status cspt_quadtree_point_in_polygon_host(
+  const uint32_t* pair_polygon, const uint32_t* pair_quad, size_t num_pairs,
+  const cspt_quadtree* tree, const uint32_t* point_indices, size_t num_point_indices,
+  const void* x, const void* y, size_t num_points, const uint32_t* poly_offsets,
+  size_t num_poly_offsets, const uint32_t* ring_offsets, size_t num_ring_offsets,
+  const void* poly_x, const void* poly_y, size_t num_poly_vertices, cspt_dtype dtype,
+  cspt_method method, const cspt_allocator* mr, void* stream, uint32_t* host_polygon_index,
+  uint32_t* host_point_index, size_t host_capacity, size_t* out_num_pairs)
+{
+  return guarded([&] {
+    CSPT_EXPECTS(out_num_pairs, "output pointers must not be null");
+    *out_num_pairs = 0;
+    t_last_refined = 0;
+    CSPT_EXPECTS(tree, "a quadtree table must have 5 columns");
+    check_dtype(dtype);
+    // quadtree_point_in_polygon.cu:154-169
+    CSPT_EXPECTS(num_point_indices == num_points,
+                 "number of points must be the same for both x and y columns");
+    CSPT_EXPECTS(method == CSPT_METHOD_EXACT || method == CSPT_METHOD_FILTERED,
+                 "unknown point-in-polygon method");
+    CSPT_EXPECTS(host_capacity == 0 || (host_polygon_index && host_point_index),
+                 "host output arrays must not be null");
+    // :171-178
+    if (num_pairs == 0 || tree->num_nodes == 0 || num_point_indices == 0 ||
+        num_poly_offsets == 0)
+      return;
+    CSPT_EXPECTS(num_ring_offsets > 0,
+                 "Polygon ring offsets must contain at least one (1) value");
+    Allocator alloc(mr, as_stream(stream));
+    uint64_t refined = 0;
+    HostRows const host{host_polygon_index, host_point_index, host_capacity};
+    quadtree_point_in_polygon(pair_polygon, pair_quad, num_pairs, tree, point_indices,
+                              num_point_indices, x, y, poly_offsets, num_poly_offsets,
+                              ring_offsets, num_ring_offsets, poly_x, poly_y, num_poly_vertices,
+                              dtype, method, alloc, nullptr, nullptr, out_num_pairs, &refined,
+                              &host);
     t_last_refined = refined;
   });
 }

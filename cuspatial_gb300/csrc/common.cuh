@@ -208,6 +208,16 @@ int num_sms();
 // non-blocking with respect to the legacy default stream).
 cudaStream_t side_stream();
 
+// Makes `waiter` wait for everything enqueued on `on` so far.
+void stream_wait(cudaStream_t waiter, cudaStream_t on);
+
+// Caller's host arrays for result rows written to host memory.
+struct HostRows {
+  uint32_t* polygon_index;
+  uint32_t* point_index;
+  size_t capacity;  // rows each array holds
+};
+
 // Makes `main` wait for everything enqueued on `side` so far, at join() or
 // when it goes out of scope (also while an exception unwinds), so that
 // buffers released on `main` afterwards are no longer in use on `side`.

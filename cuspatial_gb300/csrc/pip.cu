@@ -29,6 +29,8 @@ namespace cspt {
 namespace {
 
 constexpr int kPipBlock = 256;
+// chunks of pairs when the rows go to host memory (copies overlap the next chunk)
+constexpr size_t kHostChunks = 8;
 // the quadrant fast path: edges per warp list, slabs per quadrant
 constexpr uint32_t kFastCap   = 96;
 constexpr uint32_t kFastSlabs = 31;
@@ -515,7 +517,8 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
          cspt_quadtree const* tree, uint32_t const* point_indices, size_t npi, T const* x,
          T const* y, uint32_t const* po, size_t npo, uint32_t const* ro, size_t nro,
          T const* vx, T const* vy, size_t nv, cspt_method method, Allocator const& alloc,
-         uint32_t** out_poly, uint32_t** out_point, size_t* out_n, uint64_t* out_refined)
+         uint32_t** out_poly, uint32_t** out_point, size_t* out_n, uint64_t* out_refined,
+         HostRows const* host)
 {
   cudaStream_t const s = alloc.stream();
   bool const filtered  = method == CSPT_METHOD_FILTERED && std::is_same<T, double>::value;
@@ -536,7 +539,6 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
   Buffer<unsigned long long> refined(alloc, 2);  // [0] refined candidates, [1] next pair
   CSPT_CUDA_TRY(cudaMemsetAsync(refined.data(), 0, 2 * sizeof(unsigned long long), s));
   unsigned const blk = 256;
-  unsigned const grd = grid_for(npairs * 32, blk, 152u * 8u * 4u);
   // filtered: groups of consecutive pairs sharing a quadrant, each pair's
   // group, and the leaf frames (float32 point offsets from the quadrant's
   // anchor), which need only the index's anchor grid
@@ -579,48 +581,98 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
   }
   index.fill();
   join.join();
-  if constexpr (std::is_same<T, double>::value) {
+  // hit bitmask and per-pair counts of pairs [k0, k0 + n) (the pair
+  // arrays are offset; word offsets and group ids stay absolute)
+  auto evaluate = [&](size_t k0, size_t n) {
     KernelTimer timer("pip_bits", s);
-    if (filtered)
-      pip_pair_kernel<true>
-        <<<pair_grid(pip_pair_kernel<true>, kPipBlock, npairs), kPipBlock, 0, s>>>(
-          pair_poly, pair_quad, pgroup.data(), npairs, qlen, qoff, point_indices, npi, x, y,
-          u.data(), frames.data(), index.view(), word_off.data(), bits.data(), counts.data(),
-          refined.data(), refined.data() + 1);
-    else
-      pip_pair_kernel<false>
-        <<<pair_grid(pip_pair_kernel<false>, kPipBlock, npairs), kPipBlock, 0, s>>>(
-          pair_poly, pair_quad, nullptr, npairs, qlen, qoff, point_indices, npi, x, y, nullptr,
-          nullptr, index.view(), word_off.data(), bits.data(), counts.data(), nullptr,
-          refined.data() + 1);
+    if constexpr (std::is_same<T, double>::value) {
+      CSPT_CUDA_TRY(cudaMemsetAsync(refined.data() + 1, 0, sizeof(unsigned long long), s));
+      if (filtered)
+        pip_pair_kernel<true><<<pair_grid(pip_pair_kernel<true>, kPipBlock, n), kPipBlock, 0, s>>>(
+          pair_poly + k0, pair_quad + k0, pgroup.data() + k0, n, qlen, qoff, point_indices, npi,
+          x, y, u.data(), frames.data(), index.view(), word_off.data() + k0, bits.data(),
+          counts.data() + k0, refined.data(), refined.data() + 1);
+      else
+        pip_pair_kernel<false>
+          <<<pair_grid(pip_pair_kernel<false>, kPipBlock, n), kPipBlock, 0, s>>>(
+            pair_poly + k0, pair_quad + k0, nullptr, n, qlen, qoff, point_indices, npi, x, y,
+            nullptr, nullptr, index.view(), word_off.data() + k0, bits.data(), counts.data() + k0,
+            nullptr, refined.data() + 1);
+    } else {
+      pip_pair_kernel_f32<<<grid_for(n * 32, blk, 152u * 8u * 4u), blk, 0, s>>>(
+        pair_poly + k0, pair_quad + k0, n, qlen, qoff, point_indices, npi, x, y, index.view(),
+        word_off.data() + k0, bits.data(), counts.data() + k0);
+    }
     CSPT_CHECK_LAUNCH();
-  } else {
-    KernelTimer timer("pip_bits", s);
-    pip_pair_kernel_f32<<<grd, blk, 0, s>>>(pair_poly, pair_quad, npairs, qlen, qoff,
-                                            point_indices, npi, x, y, index.view(),
-                                            word_off.data(), bits.data(), counts.data());
-    CSPT_CHECK_LAUNCH();
-  }
-  Buffer<uint64_t> out_off(alloc, npairs + 1);
-  uint64_t* oo        = out_off.data();
-  uint32_t const* cnt = counts.data();
-  scan_apply<uint64_t>([cnt] __device__(size_t k) { return static_cast<uint64_t>(cnt[k]); },
-                       [oo] __device__(size_t k, uint64_t e, uint64_t) { oo[k] = e; }, npairs,
-                       oo + npairs, alloc);
-  size_t const m = read_back(oo + npairs, s);
-  if (out_refined) *out_refined = filtered ? read_back(refined.data(), s) : 0;
-  *out_n = m;
-  if (m == 0) return;
-  Buffer<uint32_t> op(alloc, m), oq(alloc, m);
-  {
+  };
+  // row offsets of pairs [k0, k0 + n) from their counts; returns the rows
+  auto row_offsets = [&](size_t k0, size_t n, Buffer<uint64_t>& out_off) {
+    out_off             = Buffer<uint64_t>(alloc, n + 1);
+    uint64_t* oo        = out_off.data();
+    uint32_t const* cnt = counts.data() + k0;
+    scan_apply<uint64_t>([cnt] __device__(size_t k) { return static_cast<uint64_t>(cnt[k]); },
+                         [oo] __device__(size_t k, uint64_t e, uint64_t) { oo[k] = e; }, n,
+                         oo + n, alloc);
+    return static_cast<size_t>(read_back(oo + n, s));
+  };
+  auto expand = [&](size_t k0, size_t n, Buffer<uint64_t> const& out_off, uint32_t* op,
+                    uint32_t* oq, size_t m) {
     KernelTimer timer("pip_expand", s);
-    pip_expand_kernel<<<grd, blk, 0, s>>>(pair_poly, pair_quad, npairs, qlen, qoff,
-                                          word_off.data(), bits.data(), out_off.data(),
-                                          op.data(), oq.data(), m);
+    pip_expand_kernel<<<grid_for(n * 32, blk, 152u * 8u * 4u), blk, 0, s>>>(
+      pair_poly + k0, pair_quad + k0, n, qlen, qoff, word_off.data() + k0, bits.data(),
+      out_off.data(), op, oq, m);
     CSPT_CHECK_LAUNCH();
+  };
+
+  if (!host) {
+    evaluate(0, npairs);
+    Buffer<uint64_t> out_off;
+    size_t const m = row_offsets(0, npairs, out_off);
+    if (out_refined) *out_refined = filtered ? read_back(refined.data(), s) : 0;
+    *out_n = m;
+    if (m == 0) return;
+    Buffer<uint32_t> op(alloc, m), oq(alloc, m);
+    expand(0, npairs, out_off, op.data(), oq.data(), m);
+    *out_poly  = op.release();
+    *out_point = oq.release();
+    return;
   }
-  *out_poly  = op.release();
-  *out_point = oq.release();
+
+  // Host output: the pairs are evaluated in chunks, and each chunk's rows are
+  // copied to the host on a second stream while the next chunk is evaluated.
+  // The staged rows stay allocated until `copies` has joined.
+  std::vector<Buffer<uint32_t>> staged;
+  cudaStream_t const copy = side_stream();
+  StreamJoin copies(s, copy);
+  size_t const nchunks = std::max<size_t>(1, std::min<size_t>(kHostChunks, npairs >> 14));
+  size_t rows          = 0;
+  for (size_t c = 0; c < nchunks; ++c) {
+    size_t const k0 = npairs * c / nchunks, n = npairs * (c + 1) / nchunks - k0;
+    evaluate(k0, n);
+    Buffer<uint64_t> out_off;
+    size_t const m = row_offsets(k0, n, out_off);
+    if (m > 0) {
+      Buffer<uint32_t> op(alloc, m), oq(alloc, m);
+      expand(k0, n, out_off, op.data(), oq.data(), m);
+      if (rows + m <= host->capacity) {
+        stream_wait(copy, s);
+        CSPT_CUDA_TRY(cudaMemcpyAsync(host->polygon_index + rows, op.data(), m * 4,
+                                      cudaMemcpyDeviceToHost, copy));
+        CSPT_CUDA_TRY(cudaMemcpyAsync(host->point_index + rows, oq.data(), m * 4,
+                                      cudaMemcpyDeviceToHost, copy));
+      }
+      staged.push_back(std::move(op));
+      staged.push_back(std::move(oq));
+    }
+    rows += m;
+  }
+  copies.join();
+  if (out_refined) *out_refined = filtered ? read_back(refined.data(), s) : 0;
+  CSPT_CUDA_TRY(cudaStreamSynchronize(s));
+  *out_n = rows;
+  CSPT_EXPECTS(rows <= host->capacity,
+               "the host buffers hold " + std::to_string(host->capacity) +
+                 " rows; the result has " + std::to_string(rows));
 }
 
 }  // namespace
@@ -808,18 +860,18 @@ void quadtree_point_in_polygon(uint32_t const* pair_poly, uint32_t const* pair_q
                                size_t nro, void const* vx, void const* vy, size_t nv,
                                cspt_dtype dtype, cspt_method method, Allocator const& alloc,
                                uint32_t** out_poly, uint32_t** out_point, size_t* out_n,
-                               uint64_t* out_refined)
+                               uint64_t* out_refined, HostRows const* host)
 {
   if (dtype == CSPT_FLOAT64)
     run<double>(pair_poly, pair_quad, npairs, tree, point_indices, npi,
                 static_cast<double const*>(x), static_cast<double const*>(y), po, npo, ro, nro,
                 static_cast<double const*>(vx), static_cast<double const*>(vy), nv, method, alloc,
-                out_poly, out_point, out_n, out_refined);
+                out_poly, out_point, out_n, out_refined, host);
   else
     run<float>(pair_poly, pair_quad, npairs, tree, point_indices, npi,
                static_cast<float const*>(x), static_cast<float const*>(y), po, npo, ro, nro,
                static_cast<float const*>(vx), static_cast<float const*>(vy), nv, method, alloc,
-               out_poly, out_point, out_n, out_refined);
+               out_poly, out_point, out_n, out_refined, host);
 }
 
 }  // namespace cspt

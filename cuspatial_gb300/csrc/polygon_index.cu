@@ -351,27 +351,45 @@ __global__ void __launch_bounds__(kIdxBlock)
 }
 
 // The anchor grid: 2^(e-22) where 2^e bounds every finite polygon coordinate.
+// The largest magnitude is taken on the bit patterns (sign cleared,
+// non-finite skipped), which order as the magnitudes: integer work only, so
+// the FP64 pipe of the one SM this runs on stays out of the loop.
 template <typename T>
 __global__ void __launch_bounds__(1024)
   grid_kernel(T const* __restrict__ pminx, T const* __restrict__ pminy,
               T const* __restrict__ pmaxx, T const* __restrict__ pmaxy, size_t np, T* grid)
 {
-  __shared__ T part[32];
-  T m = 0;
+  using U             = typename uint_of<T>::type;
+  constexpr U kMag    = ~(U{1} << (8 * sizeof(U) - 1));
+  constexpr U kExpAll = sizeof(T) == 8 ? U(0x7FF0000000000000ull) : U(0x7F800000u);
+  __shared__ U part[32];
+  U m = 0;
   for (size_t p = threadIdx.x; p < np; p += blockDim.x) {
     T const v[4] = {pminx[p], pminy[p], pmaxx[p], pmaxy[p]};
-    for (T a : v)
-      if (isfinite(a)) m = fmax(m, fabs(a));
+    for (T a : v) {
+      U b;
+      memcpy(&b, &a, sizeof(T));
+      b &= kMag;
+      if ((b & kExpAll) != kExpAll && b > m) m = b;
+    }
   }
-  for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xFFFFFFFFu, m, off));
+  for (int off = 16; off > 0; off >>= 1) {
+    U const o = __shfl_xor_sync(0xFFFFFFFFu, m, off);
+    m         = o > m ? o : m;
+  }
   if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x < 32) {
-    m = part[threadIdx.x];
-    for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xFFFFFFFFu, m, off));
+    m = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : U{0};
+    for (int off = 16; off > 0; off >>= 1) {
+      U const o = __shfl_xor_sync(0xFFFFFFFFu, m, off);
+      m         = o > m ? o : m;
+    }
     if (threadIdx.x == 0) {
+      T mv;
+      memcpy(&mv, &m, sizeof(T));
       int e = 0;
-      frexp(m > T{0} ? m : T{1}, &e);  // m < 2^e
+      frexp(mv > T{0} ? mv : T{1}, &e);  // mv < 2^e
       *grid = ldexp(T{1}, e - 22);
     }
   }

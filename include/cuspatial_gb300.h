@@ -194,6 +194,27 @@ cspt_status cspt_quadtree_point_in_polygon(
   uint32_t** out_point_index, size_t* out_num_pairs);
 
 /*
+ * cspt_quadtree_point_in_polygon with the rows written to host memory, for a
+ * caller whose results go to the host (the reference's column API followed by
+ * a device-to-host copy of both columns).  Rows go to host_polygon_index and
+ * host_point_index (host_capacity rows each), in the same order.  The pairs
+ * are evaluated in chunks and each chunk's rows are copied while the next is
+ * evaluated, so with page-locked host arrays the copies overlap the
+ * evaluation.  Returns once the rows are in host memory.  *out_num_pairs
+ * receives the row count; when it exceeds host_capacity the call returns
+ * CSPT_INVALID_ARGUMENT (the message gives both counts) and the arrays hold
+ * no complete result.
+ */
+cspt_status cspt_quadtree_point_in_polygon_host(
+  const uint32_t* pair_polygon, const uint32_t* pair_quad, size_t num_pairs,
+  const cspt_quadtree* tree, const uint32_t* point_indices, size_t num_point_indices,
+  const void* x, const void* y, size_t num_points, const uint32_t* poly_offsets,
+  size_t num_poly_offsets, const uint32_t* ring_offsets, size_t num_ring_offsets,
+  const void* poly_x, const void* poly_y, size_t num_poly_vertices, cspt_dtype dtype,
+  cspt_method method, const cspt_allocator* mr, void* stream, uint32_t* host_polygon_index,
+  uint32_t* host_point_index, size_t host_capacity, size_t* out_num_pairs);
+
+/*
  * Replaces cuspatial::quadtree_point_to_nearest_linestring
  * (cpp/include/cuspatial/spatial_join.hpp:166-175;
  * cpp/src/join/quadtree_point_to_nearest_linestring.cu:142-187).

@@ -425,3 +425,44 @@ def test_nearest_linestring_adversarial(method):
     np.testing.assert_array_equal(u32(r["point_index"]), orr["point_index"])
     np.testing.assert_array_equal(u32(r["linestring_index"]), orr["linestring_index"])
     np.testing.assert_array_equal(to_np(r["distance"]), orr["distance"])
+
+
+@pytest.mark.parametrize("method", METHODS)
+def test_host_rows(method):
+    # quadtree_point_in_polygon_host: 149,909 pairs evaluated in 8 chunks, rows
+    # copied to page-locked and to pageable host tensors; the same rows as the
+    # oracle, in the same order
+    w = D.precision_at_scale(n_points=2_000_000, n_polygons=20_000, extent=4000.0,
+                             max_vertices=64)
+    pi, t, bb, j, r = _run_pipeline(w, np.float64, method)
+    assert int(j["bbox_offset"].numel()) > 8 << 14
+    pts, polys = gpu_points(w), gpu_polygons(w.polygons)
+    m = int(r["polygon_index"].numel())
+    P = w.polygons
+    opi, ot = oracle_tree(w, np.float64)
+    oj = O.join_quadtree_and_bounding_boxes(ot, O.polygon_bounding_boxes(
+        P.part_offset, P.ring_offset, P.x, P.y), w.x_min, w.x_max, w.y_min, w.y_max, w.scale,
+        w.max_depth)
+    orr = O.quadtree_point_in_polygon(oj, ot, opi, w.x, w.y, P.part_offset, P.ring_offset,
+                                      P.x, P.y)
+    for pinned in (True, False):
+        hp = torch.full((m + 5,), -1, dtype=torch.int32, pin_memory=pinned)
+        hq = torch.full((m + 5,), -1, dtype=torch.int32, pin_memory=pinned)
+        n = cs.quadtree_point_in_polygon_host(j, t, pi, pts, polys, hp, hq, method=method)
+        assert n == m == len(orr["polygon_index"])
+        np.testing.assert_array_equal(hp[:n].numpy().view(np.uint32), orr["polygon_index"])
+        np.testing.assert_array_equal(hq[:n].numpy().view(np.uint32), orr["point_index"])
+        assert hp[n:].tolist() == [-1] * 5
+    # too few rows: the count comes back with the error
+    small = torch.empty(m - 1, dtype=torch.int32)
+    with pytest.raises(cs.HostRowsTooFew) as e:
+        cs.quadtree_point_in_polygon_host(j, t, pi, pts, polys, small, small.clone(),
+                                          method=method)
+    assert e.value.rows == m and str(m) in str(e.value)
+    # no pairs: nothing is written
+    none = {"bbox_offset": j["bbox_offset"][:0], "quad_offset": j["quad_offset"][:0]}
+    assert cs.quadtree_point_in_polygon_host(none, t, pi, pts, polys, small, small.clone(),
+                                             method=method) == 0
+    with pytest.raises(ValueError):
+        cs.quadtree_point_in_polygon_host(j, t, pi, pts, polys, small.cuda(), small,
+                                          method=method)
