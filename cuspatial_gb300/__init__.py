@@ -12,7 +12,7 @@ from .api import (HostRowsTooFew, join_quadtree_and_bounding_boxes, last_refined
                   linestring_bounding_boxes, pairwise_point_in_polygon,
                   pairwise_point_linestring_distance, pairwise_point_linestring_nearest_points,
                   point_in_polygon, point_in_polygon_bitmask, polygon_bounding_boxes,
-                  quadtree_on_points, quadtree_point_in_polygon,
+                  quadtree_on_points, quadtree_on_points_host, quadtree_point_in_polygon,
                   quadtree_point_in_polygon_host, quadtree_point_to_nearest_linestring)
 from .contains import contains_properly, polygons_contains_properly
 from .geoseries import GeoSeries, Table
@@ -33,6 +33,7 @@ __all__ = [
     "polygon_bounding_boxes",
     "polygons_contains_properly",
     "quadtree_on_points",
+    "quadtree_on_points_host",
     "quadtree_point_in_polygon",
     "quadtree_point_in_polygon_host",
     "quadtree_point_to_nearest_linestring",

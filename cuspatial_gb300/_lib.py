@@ -92,6 +92,10 @@ def _declare(lib):
         _vp, _vp, _sz, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
         ctypes.c_double, ctypes.c_double, ctypes.c_int8, ctypes.c_int32,
         ctypes.POINTER(CsptAllocator), _vp, ctypes.POINTER(_vp), ctypes.POINTER(CsptQuadtree)]
+    lib.cspt_quadtree_on_points_host.argtypes = [
+        _vp, _vp, _sz, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+        ctypes.c_double, ctypes.c_double, ctypes.c_int8, ctypes.c_int32, _vp, _vp,
+        ctypes.POINTER(CsptAllocator), _vp, ctypes.POINTER(_vp), ctypes.POINTER(CsptQuadtree)]
     lib.cspt_polygon_bounding_boxes.argtypes = [
         _vp, _sz, _vp, _sz, _vp, _vp, _sz, ctypes.c_int, ctypes.c_double, _vp, _vp, _vp, _vp, _vp]
     lib.cspt_linestring_bounding_boxes.argtypes = [
@@ -162,7 +166,8 @@ def _declare(lib):
     for name in ("cspt_batched_pip_plan", "cspt_batched_pip_run", "cspt_batched_pip_get_info",
                  "cspt_batched_pip_refined_count"):
         getattr(lib, name).restype = ctypes.c_int
-    for name in ("cspt_quadtree_on_points", "cspt_polygon_bounding_boxes",
+    for name in ("cspt_quadtree_on_points", "cspt_quadtree_on_points_host",
+                 "cspt_polygon_bounding_boxes",
                  "cspt_linestring_bounding_boxes", "cspt_join_quadtree_and_bounding_boxes",
                  "cspt_quadtree_point_in_polygon", "cspt_quadtree_point_in_polygon_host",
                  "cspt_quadtree_point_to_nearest_linestring"):

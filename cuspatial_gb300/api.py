@@ -70,7 +70,10 @@ def quadtree_on_points(points: GeoSeries, x_min, x_max, y_min, y_max, scale, max
         _lib.ptr(xs), _lib.ptr(ys), int(xs.numel()), _dtype_code(xs), float(x_min), float(x_max),
         float(y_min), float(y_max), float(max(scale, min_scale)), int(max_depth), int(max_size),
         alloc.ref, _lib.stream_ptr(), ctypes.byref(pi), ctypes.byref(tree)), lib)
-    n = int(xs.numel())
+    return _adopt_tree(alloc, pi, tree, int(xs.numel()))
+
+
+def _adopt_tree(alloc, pi, tree, n):
     q = int(tree.num_nodes)
     point_indices = alloc.adopt(pi.value, n, torch.int32)
     qt = Table()
@@ -80,6 +83,42 @@ def quadtree_on_points(points: GeoSeries, x_min, x_max, y_min, y_max, scale, max
     qt["length"] = alloc.adopt(tree.length, q, torch.int32)
     qt["offset"] = alloc.adopt(tree.offset, q, torch.int32)
     return point_indices, qt
+
+
+def quadtree_on_points_host(x, y, x_min, x_max, y_min, y_max, scale, max_depth, max_size):
+    """quadtree_on_points for points in host memory.
+
+    x and y are CPU tensors of one floating type (page-locked, for the copy to
+    the device to overlap the Morton keys of the chunks already copied).
+    Returns (points, point_indices, quadtree): points is a GeoSeries over the
+    device copies of x and y, for the calls that follow.
+    """
+    for t in (x, y):
+        if t.device.type != "cpu" or not t.is_contiguous():
+            raise ValueError("x and y must be contiguous CPU tensors")
+    if x.dtype != y.dtype or x.dtype not in (torch.float32, torch.float64):
+        raise TypeError("Only floating-point types are supported")
+    if x.numel() != y.numel():
+        raise RuntimeError("x and y columns must have the same length")
+    lib = _lib.load()
+    x_min, x_max, y_min, y_max = (min(x_min, x_max), max(x_min, x_max), min(y_min, y_max),
+                                  max(y_min, y_max))
+    min_scale = max(x_max - x_min, y_max - y_min) / ((1 << max_depth) + 2)
+    if scale < min_scale:
+        warnings.warn("scale {} is less than required minimum ".format(scale) +
+                      "scale {}. Clamping to minimum scale".format(min_scale))
+    dx = torch.empty(x.numel(), dtype=x.dtype, device="cuda")
+    dy = torch.empty(y.numel(), dtype=y.dtype, device="cuda")
+    alloc = _lib.TorchAllocator(dx.device)
+    pi = ctypes.c_void_p()
+    tree = _lib.CsptQuadtree()
+    _lib.check(lib.cspt_quadtree_on_points_host(
+        x.data_ptr() if x.numel() else None, y.data_ptr() if y.numel() else None,
+        int(x.numel()), _dtype_code(x), float(x_min), float(x_max), float(y_min), float(y_max),
+        float(max(scale, min_scale)), int(max_depth), int(max_size), _lib.ptr(dx), _lib.ptr(dy),
+        alloc.ref, _lib.stream_ptr(), ctypes.byref(pi), ctypes.byref(tree)), lib)
+    point_indices, qt = _adopt_tree(alloc, pi, tree, int(x.numel()))
+    return GeoSeries.from_points(dx, dy), point_indices, qt
 
 
 def _empty_boxes(dtype):

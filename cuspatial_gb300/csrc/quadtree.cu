@@ -231,10 +231,20 @@ __global__ void internal_offset_kernel(uint8_t const* __restrict__ internal,
   }
 }
 
+// Host input: the points are copied from host memory (hx, hy) into the
+// caller's device arrays (x, y) in chunks on a second stream, and the Morton
+// keys of each chunk are computed as soon as its copy has landed.
+template <typename T>
+struct HostInput {
+  T const* hx;
+  T const* hy;
+};
+constexpr size_t kHostChunks = 8;
+
 template <typename T>
 void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d, double y2d,
            double scaled, int max_depth_in, int32_t max_size_in, Allocator const& alloc,
-           uint32_t** out_point_indices, cspt_quadtree* out)
+           uint32_t** out_point_indices, cspt_quadtree* out, HostInput<T> const* host = nullptr)
 {
   cudaStream_t const s = alloc.stream();
   *out                 = cspt_quadtree{nullptr, nullptr, nullptr, nullptr, nullptr, 0};
@@ -261,11 +271,29 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
 
   Buffer<uint32_t> keys(alloc, n), keys_alt(alloc, n);
   Buffer<uint32_t> idx(alloc, n), idx_alt(alloc, n);
-  {
+  if (!host) {
     KernelTimer kt("quadtree_keys", s);
     morton_keys_kernel<T><<<grd, blk, 0, s>>>(x, y, n, minx, miny, maxx, maxy, scale,
                                               T{1} / scale, d, keys.data());
     CSPT_CHECK_LAUNCH();
+  } else {
+    cudaStream_t const copy = side_stream();
+    StreamJoin copies(s, copy);  // before `keys` is released, also on an exception
+    stream_wait(copy, s);        // the destinations may come from work on s
+    size_t const nch = std::max<size_t>(1, std::min<size_t>(kHostChunks, n >> 20));
+    for (size_t c = 0; c < nch; ++c) {
+      size_t const i0 = n * c / nch, m = n * (c + 1) / nch - i0;
+      // x and y are the caller's device destinations in this mode
+      CSPT_CUDA_TRY(cudaMemcpyAsync(const_cast<T*>(x) + i0, host->hx + i0, m * sizeof(T),
+                                    cudaMemcpyHostToDevice, copy));
+      CSPT_CUDA_TRY(cudaMemcpyAsync(const_cast<T*>(y) + i0, host->hy + i0, m * sizeof(T),
+                                    cudaMemcpyHostToDevice, copy));
+      stream_wait(s, copy);
+      morton_keys_kernel<T><<<grid_for(m, blk, 152u * 16u), blk, 0, s>>>(
+        x + i0, y + i0, m, minx, miny, maxx, maxy, scale, T{1} / scale, d, keys.data() + i0);
+      CSPT_CHECK_LAUNCH();
+    }
+    copies.join();
   }
   // cells reach 2^d + 2, so the key needs 2(d+1) bits (2(d+2) below d = 2)
   int const key_bits = d >= 2 ? 2 * d + 2 : 2 * d + 4;
@@ -434,14 +462,19 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
 void quadtree_on_points(void const* x, void const* y, size_t n, cspt_dtype dtype, double x_min,
                         double x_max, double y_min, double y_max, double scale, int max_depth,
                         int32_t max_size, Allocator const& alloc, uint32_t** out_point_indices,
-                        cspt_quadtree* out_tree)
+                        cspt_quadtree* out_tree, void const* host_x, void const* host_y)
 {
   if (dtype == CSPT_FLOAT64) {
+    HostInput<double> const h{static_cast<double const*>(host_x),
+                              static_cast<double const*>(host_y)};
     build<double>(static_cast<double const*>(x), static_cast<double const*>(y), n, x_min, x_max,
-                  y_min, y_max, scale, max_depth, max_size, alloc, out_point_indices, out_tree);
+                  y_min, y_max, scale, max_depth, max_size, alloc, out_point_indices, out_tree,
+                  host_x ? &h : nullptr);
   } else {
+    HostInput<float> const h{static_cast<float const*>(host_x), static_cast<float const*>(host_y)};
     build<float>(static_cast<float const*>(x), static_cast<float const*>(y), n, x_min, x_max,
-                 y_min, y_max, scale, max_depth, max_size, alloc, out_point_indices, out_tree);
+                 y_min, y_max, scale, max_depth, max_size, alloc, out_point_indices, out_tree,
+                 host_x ? &h : nullptr);
   }
 }
 

@@ -114,6 +114,21 @@ cspt_status cspt_quadtree_on_points(const void* x, const void* y, size_t num_poi
                                     uint32_t** out_point_indices, cspt_quadtree* out_tree);
 
 /*
+ * cspt_quadtree_on_points for points in host memory: the points are copied
+ * into the caller's device arrays device_x / device_y (num_points elements
+ * each, for the calls that follow) in chunks, and the Morton keys of each
+ * chunk are computed while the next chunk is copied, so with page-locked host
+ * arrays the copy overlaps the key computation.  Outputs as
+ * cspt_quadtree_on_points.
+ */
+cspt_status cspt_quadtree_on_points_host(const void* host_x, const void* host_y,
+                                         size_t num_points, cspt_dtype dtype, double x_min,
+                                         double x_max, double y_min, double y_max, double scale,
+                                         int8_t max_depth, int32_t max_size, void* device_x,
+                                         void* device_y, const cspt_allocator* mr, void* stream,
+                                         uint32_t** out_point_indices, cspt_quadtree* out_tree);
+
+/*
  * Replaces cuspatial::polygon_bounding_boxes
  * (cpp/include/cuspatial/bounding_boxes.hpp:79-85;
  * cpp/src/bounding_boxes/polygon_bounding_boxes.cu:132-159).

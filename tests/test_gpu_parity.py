@@ -466,3 +466,31 @@ def test_host_rows(method):
     with pytest.raises(ValueError):
         cs.quadtree_point_in_polygon_host(j, t, pi, pts, polys, small.cuda(), small,
                                           method=method)
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+def test_quadtree_from_host(dtype):
+    # quadtree_on_points_host: 9M points copied in 8 chunks (page-locked and
+    # pageable), 1000 points in one chunk, and none; the same tree and
+    # permutation as quadtree_on_points on the device copy, and the device
+    # copy equals the input
+    for n, pinned in ((9_000_000, True), (9_000_000, False), (1000, True), (0, True)):
+        rng = np.random.default_rng(n + int(pinned))
+        x = torch.from_numpy(rng.normal(500, 150, n).astype(dtype))
+        y = torch.from_numpy(rng.normal(500, 150, n).astype(dtype))
+        if pinned:
+            x, y = x.pin_memory(), y.pin_memory()
+        args = (0.0, 1000.0, 0.0, 1000.0, 1000.0 / (1 << 12), 12, 64)
+        pts, pi, t = cs.quadtree_on_points_host(x, y, *args)
+        assert torch.equal(pts.points.x.cpu(), x) and torch.equal(pts.points.y.cpu(), y)
+        pi2, t2 = cs.quadtree_on_points(cs.GeoSeries.from_points(x.cuda(), y.cuda()), *args)
+        assert torch.equal(pi, pi2)
+        for k in t2:
+            assert torch.equal(t[k], t2[k]), k
+        if n:
+            assert int(t["key"].numel()) > 0
+    with pytest.raises(ValueError):
+        cs.quadtree_on_points_host(x.cuda(), y, *args)
+    with pytest.raises(TypeError):
+        cs.quadtree_on_points_host(torch.zeros(3, dtype=torch.int32),
+                                   torch.zeros(3, dtype=torch.int32), *args)
