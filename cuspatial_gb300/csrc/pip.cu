@@ -30,7 +30,10 @@ namespace {
 
 constexpr int kPipBlock = 256;
 // chunks of pairs when the rows go to host memory (copies overlap the next chunk)
-constexpr size_t kHostChunks = 8;
+#ifndef CSPT_HOST_CHUNKS
+#define CSPT_HOST_CHUNKS 8
+#endif
+constexpr size_t kHostChunks = CSPT_HOST_CHUNKS;
 // the quadrant fast path: edges per warp list, slabs per quadrant
 constexpr uint32_t kFastCap   = 96;
 constexpr uint32_t kFastSlabs = 31;

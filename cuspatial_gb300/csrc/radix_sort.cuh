@@ -14,7 +14,10 @@ namespace cspt {
 
 constexpr int kSortBlock = 256;  // one thread per 8-bit digit in the scatter
 constexpr int kSortWarps = kSortBlock / 32;
-constexpr int kSortRound = 8;  // rounds of 32 items per warp
+#ifndef CSPT_SORT_ROUND
+#define CSPT_SORT_ROUND 8
+#endif
+constexpr int kSortRound = CSPT_SORT_ROUND;  // rounds of 32 items per warp
 constexpr int kSortTile  = kSortBlock * kSortRound;
 constexpr unsigned kNoDigit = 0xFFFFu;
 
