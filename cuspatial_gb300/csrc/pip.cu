@@ -647,10 +647,18 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
   std::vector<Buffer<uint32_t>> staged;
   cudaStream_t const copy = side_stream();
   StreamJoin copies(s, copy);
+  // Chunk sizes fall off linearly (weights chunks, chunks - 1, ..., 1), so
+  // the copy of the last chunk, the only one nothing overlaps, is the
+  // shortest.
   size_t const nchunks = std::max<size_t>(1, std::min<size_t>(kHostChunks, npairs >> 14));
-  size_t rows          = 0;
+  size_t const wsum    = nchunks * (nchunks + 1) / 2;
+  auto const chunk_end = [&](size_t c) {  // pairs in chunks 0..c-1
+    size_t const w = c * nchunks - c * (c - 1) / 2;  // sum of the first c weights
+    return c == nchunks ? npairs : static_cast<size_t>(static_cast<double>(npairs) * w / wsum);
+  };
+  size_t rows = 0;
   for (size_t c = 0; c < nchunks; ++c) {
-    size_t const k0 = npairs * c / nchunks, n = npairs * (c + 1) / nchunks - k0;
+    size_t const k0 = chunk_end(c), n = chunk_end(c + 1) - k0;
     evaluate(k0, n);
     Buffer<uint64_t> out_off;
     size_t const m = row_offsets(k0, n, out_off);
