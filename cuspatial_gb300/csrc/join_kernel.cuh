@@ -182,6 +182,15 @@ __device__ inline bool walk(TreeView const& t, BoxTree<T> const& bt, T bminx, T 
 constexpr int kJoinWarps = 4;       // warps per block
 constexpr int kWarpStack = 2048;    // stack entries per warp (shared memory)
 
+// Where the count pass appends each (node, box) it finds, in any order, while
+// fewer than `cap` have been found (`n` counts them all, also past cap).
+struct JoinAppend {
+  uint32_t* node;
+  uint32_t* box;
+  unsigned long long* n;
+  size_t cap;
+};
+
 // One warp per box.  Each round pops up to 32 entries (node << 4 | depth)
 // from the warp's shared stack, one per lane, classifies them, counts or
 // writes the leaves with a ballot, and pushes the children of internal nodes
@@ -196,7 +205,7 @@ __global__ void __launch_bounds__(kJoinWarps * 32)
                    uint32_t* __restrict__ maxkey,
                    uint32_t const* __restrict__ pos, uint32_t* __restrict__ okey,
                    uint32_t* __restrict__ onode, uint32_t* __restrict__ obox,
-                   int* __restrict__ error)
+                   int* __restrict__ error, JoinAppend app = JoinAppend{nullptr, nullptr, nullptr, 0})
 {
   __shared__ uint32_t stack_s[kJoinWarps][kWarpStack];
   uint32_t* stack      = stack_s[threadIdx.x >> 5];
@@ -249,6 +258,18 @@ __global__ void __launch_bounds__(kJoinWarps * 32)
         }
       }
       unsigned const leaves = __ballot_sync(0xFFFFFFFFu, c == 0);
+      if (!Write && app.n && leaves) {
+        unsigned long long at = 0;
+        if (lane == 0) at = atomicAdd(app.n, static_cast<unsigned long long>(__popc(leaves)));
+        at = __shfl_sync(0xFFFFFFFFu, at, 0);
+        if (c == 0) {
+          unsigned long long const d = at + __popc(leaves & lt);
+          if (d < app.cap) {
+            app.node[d] = g;
+            app.box[d]  = static_cast<uint32_t>(b);
+          }
+        }
+      }
       if (c == 0) {
         uint32_t const key = bt.pt_base + t.offset[g];
         if (Write) {
@@ -283,7 +304,10 @@ __global__ void __launch_bounds__(kJoinWarps * 32)
       continue;
     }
     if (overflow) {
-      // rare: restart the box serially on lane 0
+      // rare: restart the box serially on lane 0.  The box's pairs appended
+      // so far would repeat, so the appended set is given up (its count is
+      // pushed past any capacity) and the write pass runs instead.
+      if (!Write && app.n && lane == 0) atomicAdd(app.n, 1ull << 62);
       if (lane == 0) {
         uint32_t q = Write ? pos[b] : 0u;
         found      = 0;
