@@ -34,8 +34,10 @@ constexpr int kPipBlock = 256;
 #define CSPT_HOST_CHUNKS 8
 #endif
 constexpr size_t kHostChunks = CSPT_HOST_CHUNKS;
-// the quadrant fast path: edges per warp list, slabs per quadrant
-constexpr uint32_t kFastCap   = 96;
+// the quadrant fast path: list entries per warp (the y-only list grows up
+// from the start of the pool, the full list down from its end), slabs per
+// quadrant
+constexpr uint32_t kFastPool  = 160;
 constexpr uint32_t kFastSlabs = 31;
 
 // The float32 slab of offset y (the lookup of filtered_test).
@@ -105,13 +107,11 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
 {
   int const lane      = threadIdx.x & 31;
   int const wid       = threadIdx.x >> 5;
-  // the quadrant fast path's edge lists, per warp
-  __shared__ float2 s_party[kPipBlock / 32][kFastCap];
-  __shared__ uint32_t s_partk[kPipBlock / 32][kFastCap];
-  __shared__ float4 s_full[kPipBlock / 32][kFastCap];
-  __shared__ uint32_t s_fullk[kPipBlock / 32][kFastCap];
-  __shared__ uint8_t s_pslab[kPipBlock / 32][kFastCap];
-  __shared__ uint8_t s_fslab[kPipBlock / 32][kFastCap];
+  // the quadrant fast path's edge lists, per warp: entry (the edge, or the
+  // y-only list's two y values), its slab entry index and its slab
+  __shared__ float4 s_pool[kPipBlock / 32][kFastPool];
+  __shared__ uint32_t s_poolk[kPipBlock / 32][kFastPool];
+  __shared__ uint8_t s_pools[kPipBlock / 32][kFastPool];
   __shared__ uint8_t s_pbeg[kPipBlock / 32][kFastSlabs + 1];
   __shared__ uint8_t s_fbeg[kPipBlock / 32][kFastSlabs + 1];
   __shared__ uint32_t s_start[kPipBlock / 32][kFastSlabs + 1];
@@ -234,22 +234,23 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
               if (cls == 1) atomicXor(&s_base[wid], 1u << jj);
               unsigned const bp = __ballot_sync(0xFFFFFFFFu, cls == 2);
               unsigned const bf = __ballot_sync(0xFFFFFFFFu, cls == 3);
-              if (npart + __popc(bp) > kFastCap || nfull + __popc(bf) > kFastCap) {
+              if (npart + nfull + __popc(bp) + __popc(bf) > kFastPool) {
                 fast = false;
                 break;
               }
               // lanes hold increasing entries, so the lists stay in slab order
+              // (the full list's i-th entry sits at kFastPool - 1 - i)
               if (cls == 2) {
                 uint32_t const slot = npart + __popc(bp & lt);
-                s_party[wid][slot]  = make_float2(e.y, e.w);
-                s_partk[wid][slot]  = kk;
-                s_pslab[wid][slot]  = static_cast<uint8_t>(jj);
+                s_pool[wid][slot]   = make_float4(e.y, e.w, 0.0f, 0.0f);
+                s_poolk[wid][slot]  = kk;
+                s_pools[wid][slot]  = static_cast<uint8_t>(jj);
               }
               if (cls == 3) {
-                uint32_t const slot = nfull + __popc(bf & lt);
-                s_full[wid][slot]   = e;
-                s_fullk[wid][slot]  = kk;
-                s_fslab[wid][slot]  = static_cast<uint8_t>(jj);
+                uint32_t const slot = kFastPool - 1u - (nfull + __popc(bf & lt));
+                s_pool[wid][slot]   = e;
+                s_poolk[wid][slot]  = kk;
+                s_pools[wid][slot]  = static_cast<uint8_t>(jj);
               }
               npart += __popc(bp);
               nfull += __popc(bf);
@@ -262,7 +263,7 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
                 uint32_t lo = 0, hi = npart;
                 while (lo < hi) {
                   uint32_t const mid = (lo + hi) >> 1;
-                  if (s_pslab[wid][mid] < static_cast<uint32_t>(lane))
+                  if (s_pools[wid][mid] < static_cast<uint32_t>(lane))
                     lo = mid + 1;
                   else
                     hi = mid;
@@ -272,7 +273,7 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
                 hi = nfull;
                 while (lo < hi) {
                   uint32_t const mid = (lo + hi) >> 1;
-                  if (s_fslab[wid][mid] < static_cast<uint32_t>(lane))
+                  if (s_pools[wid][kFastPool - 1u - mid] < static_cast<uint32_t>(lane))
                     lo = mid + 1;
                   else
                     hi = mid;
@@ -364,10 +365,10 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
               }
             }
             for (uint32_t t = pb; t < pe && !on_edge; ++t) {
-              float2 const yy = s_party[wid][t];
+              float2 const yy = *reinterpret_cast<float2 const*>(&s_pool[wid][t]);
               float const ya = yy.x - qy, yb = yy.y - qy;
               if (fabsf(ya) <= tol || fabsf(yb) <= tol) {
-                int const ee = exact_at(s_partk[wid][t]);
+                int const ee = exact_at(s_poolk[wid][t]);
                 if (ee == 2) on_edge = true;
                 if (ee == 1) within = !within;
               } else if ((ya > 0.0f) != (yb > 0.0f)) {
@@ -375,7 +376,7 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
               }
             }
             for (uint32_t t = fb; t < fe && !on_edge; ++t) {
-              float4 const e = s_full[wid][t];
+              float4 const e = s_pool[wid][kFastPool - 1u - t];
               float const ya = e.y - qy, yb = e.w - qy;
               bool const y1  = ya > 0.0f;
               bool const y0  = yb > 0.0f;
@@ -388,7 +389,7 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
                 if (y1 != y0 && ((cr < 0.0f) != y1)) within = !within;
                 continue;
               }
-              int const ee = exact_at(s_fullk[wid][t]);
+              int const ee = exact_at(s_poolk[wid][kFastPool - 1u - t]);
               if (ee == 2) on_edge = true;
               if (ee == 1) within = !within;
             }
