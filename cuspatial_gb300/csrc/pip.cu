@@ -37,7 +37,10 @@ constexpr size_t kHostChunks = CSPT_HOST_CHUNKS;
 // the quadrant fast path: list entries per warp (the y-only list grows up
 // from the start of the pool, the full list down from its end), slabs per
 // quadrant
-constexpr uint32_t kFastPool  = 160;
+#ifndef CSPT_FAST_POOL
+#define CSPT_FAST_POOL 128
+#endif
+constexpr uint32_t kFastPool  = CSPT_FAST_POOL;
 constexpr uint32_t kFastSlabs = 31;
 
 // The float32 slab of offset y (the lookup of filtered_test).
