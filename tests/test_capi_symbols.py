@@ -64,3 +64,47 @@ def test_point_in_polygon_argument_checks_on_host():
     st = lib.cspt_pairwise_point_in_polygon(None, None, 5, p, 6, r, 6, None, None, 20, 7,
                                             _lib.METHOD_EXACT, None, None, None)
     assert st == _lib.UNSUPPORTED
+
+
+def test_host_buffer_entry_points_argument_checks_on_host():
+    # the host-buffer entry points check their arguments before any device work
+    import ctypes
+
+    import pytest
+    import torch
+
+    import cuspatial_gb300 as cs
+    from cuspatial_gb300 import _lib
+    lib = _lib.load()
+    pi, tree = ctypes.c_void_p(), _lib.CsptQuadtree()
+    args = (0.0, 1.0, 0.0, 1.0, 0.1, 3, 8)
+    assert lib.cspt_quadtree_on_points_host(None, None, 0, _lib.FLOAT64, *args, None, None, None,
+                                            None, ctypes.byref(pi), ctypes.byref(tree)) == _lib.OK
+    assert tree.num_nodes == 0 and not pi.value
+    assert lib.cspt_quadtree_on_points_host(None, None, 5, 7, *args, None, None, None, None,
+                                            ctypes.byref(pi), ctypes.byref(tree)) == _lib.UNSUPPORTED
+    assert lib.cspt_quadtree_on_points_host(None, None, 5, _lib.FLOAT64, *args, None, None, None,
+                                            None, ctypes.byref(pi),
+                                            ctypes.byref(tree)) == _lib.INVALID_ARGUMENT
+    assert lib.cspt_last_error_message() == b"x and y columns must have the same length"
+
+    n = ctypes.c_size_t(7)
+    common = (None, None, 0, ctypes.byref(tree), None, 0, None, None, 0, None, 1, None, 1, None,
+              None, 0, _lib.FLOAT64, _lib.METHOD_FILTERED, None, None)
+    assert lib.cspt_quadtree_point_in_polygon_host(*common, None, None, 0,
+                                                   None) == _lib.INVALID_ARGUMENT
+    assert lib.cspt_last_error_message() == b"output pointers must not be null"
+    assert lib.cspt_quadtree_point_in_polygon_host(*common, None, None, 4,
+                                                   ctypes.byref(n)) == _lib.INVALID_ARGUMENT
+    assert lib.cspt_last_error_message() == b"host output arrays must not be null"
+    # no pairs: nothing to write
+    assert lib.cspt_quadtree_point_in_polygon_host(*common, None, None, 0,
+                                                   ctypes.byref(n)) == _lib.OK
+    assert n.value == 0
+
+    with pytest.raises(TypeError):
+        cs.quadtree_on_points_host(torch.zeros(3, dtype=torch.int32),
+                                   torch.zeros(3, dtype=torch.int32), *args)
+    with pytest.raises(RuntimeError):
+        cs.quadtree_on_points_host(torch.zeros(3, dtype=torch.float64),
+                                   torch.zeros(2, dtype=torch.float64), *args)
