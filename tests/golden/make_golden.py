@@ -552,45 +552,54 @@ def _dtype_params(fdef):
     return None
 
 
+def kats_from_python_source(rel, text):
+    """The cases and skipped tests of one Python test file's source text."""
+    cases, skipped = [], []
+    tree = ast.parse(text)
+    env, helpers, tests = {}, {}, []
+    for st in tree.body:
+        if isinstance(st, ast.Assign):
+            try:
+                v = _Eval(env, helpers).ev(st.value)
+            except _Unsupported:
+                continue
+            for t in st.targets:
+                if isinstance(t, ast.Name):
+                    env[t.id] = v
+        elif isinstance(st, ast.FunctionDef):
+            if st.name.startswith("test_"):
+                tests.append(st)
+            else:
+                helpers[st.name] = st
+    for fdef in tests:
+        dtypes = _dtype_params(fdef) or [None]
+        for dt in dtypes:
+            e = _Eval(env, helpers)
+            if dt is not None:
+                e.env["dtype"] = dt
+            try:
+                e.run(fdef.body)
+            except (_Unsupported, KeyError, IndexError, TypeError) as exc:
+                skipped.append(dict(source=rel, test=fdef.name, reason=str(exc)))
+                break
+            for actual, expected in e.checks:
+                if isinstance(expected, dict) and "op" in expected:
+                    actual, expected = expected, actual
+                cases.append(dict(source="%s:%d" % (rel, fdef.lineno), test=fdef.name,
+                                  dtype=dt or "float64", actual=actual,
+                                  expected={str(k): v for k, v in expected.items()}))
+    return cases, skipped
+
+
 def python_test_kats(root):
     files = ["python/cuspatial/cuspatial/tests/spatial/indexing/test_indexing.py",
              "python/cuspatial/cuspatial/tests/spatial/join/test_spatial_join.py",
              "python/cuspatial/cuspatial/tests/spatial/join/test_point_in_polygon.py"]
     cases, skipped = [], []
     for rel in files:
-        tree = ast.parse(open(os.path.join(root, rel)).read())
-        env, helpers, tests = {}, {}, []
-        for st in tree.body:
-            if isinstance(st, ast.Assign):
-                try:
-                    v = _Eval(env, helpers).ev(st.value)
-                except _Unsupported:
-                    continue
-                for t in st.targets:
-                    if isinstance(t, ast.Name):
-                        env[t.id] = v
-            elif isinstance(st, ast.FunctionDef):
-                if st.name.startswith("test_"):
-                    tests.append(st)
-                else:
-                    helpers[st.name] = st
-        for fdef in tests:
-            dtypes = _dtype_params(fdef) or [None]
-            for dt in dtypes:
-                e = _Eval(env, helpers)
-                if dt is not None:
-                    e.env["dtype"] = dt
-                try:
-                    e.run(fdef.body)
-                except (_Unsupported, KeyError, IndexError, TypeError) as exc:
-                    skipped.append(dict(source=rel, test=fdef.name, reason=str(exc)))
-                    break
-                for actual, expected in e.checks:
-                    if isinstance(expected, dict) and "op" in expected:
-                        actual, expected = expected, actual
-                    cases.append(dict(source="%s:%d" % (rel, fdef.lineno), test=fdef.name,
-                                      dtype=dt or "float64", actual=actual,
-                                      expected={str(k): v for k, v in expected.items()}))
+        c, sk = kats_from_python_source(rel, open(os.path.join(root, rel)).read())
+        cases += c
+        skipped += sk
     return dict(note="each case: an op record (the value under test, built from the "
                      "reference's Python API calls) and the frame the test expects",
                 cases=cases, skipped=skipped)
