@@ -13,8 +13,12 @@ namespace cspt {
 void quadtree_on_points(void const* x, void const* y, size_t n, cspt_dtype dtype, double x_min,
                         double x_max, double y_min, double y_max, double scale, int max_depth,
                         int32_t max_size, Allocator const& alloc, uint32_t** out_point_indices,
-                        cspt_quadtree* out_tree, void const* host_x = nullptr,
-                        void const* host_y = nullptr);
+                        cspt_quadtree* out_tree);
+void quadtree_on_points_from_host(void const* host_x, void const* host_y, void* dev_x,
+                                  void* dev_y, size_t n, cspt_dtype dtype, double x_min,
+                                  double x_max, double y_min, double y_max, double scale,
+                                  int max_depth, int32_t max_size, Allocator const& alloc,
+                                  uint32_t** out_point_indices, cspt_quadtree* out_tree);
 void polygon_bounding_boxes(uint32_t const* poly_offsets, size_t npo,
                             uint32_t const* ring_offsets, size_t nro, void const* x,
                             void const* y, size_t nv, cspt_dtype dtype, double r, void* ominx,
@@ -299,8 +303,9 @@ cspt_status cspt_quadtree_on_points_host(const void* host_x, const void* host_y,
     CSPT_EXPECTS(host_x && host_y && device_x && device_y,
                  "x and y columns must have the same length");
     Allocator alloc(mr, as_stream(stream));
-    quadtree_on_points(device_x, device_y, num_points, dtype, x_min, x_max, y_min, y_max, scale,
-                       max_depth, max_size, alloc, out_point_indices, out_tree, host_x, host_y);
+    quadtree_on_points_from_host(host_x, host_y, device_x, device_y, num_points, dtype, x_min,
+                                 x_max, y_min, y_max, scale, max_depth, max_size, alloc,
+                                 out_point_indices, out_tree);
   });
 }
 

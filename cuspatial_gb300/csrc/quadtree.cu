@@ -232,12 +232,15 @@ __global__ void internal_offset_kernel(uint8_t const* __restrict__ internal,
 }
 
 // Host input: the points are copied from host memory (hx, hy) into the
-// caller's device arrays (x, y) in chunks on a second stream, and the Morton
-// keys of each chunk are computed as soon as its copy has landed.
+// caller's device arrays (dx, dy, which build() then reads as x and y) in
+// chunks on a second stream, and the Morton keys of each chunk are computed
+// as soon as its copy has landed.
 template <typename T>
 struct HostInput {
   T const* hx;
   T const* hy;
+  T* dx;
+  T* dy;
 };
 constexpr size_t kHostChunks = 8;
 
@@ -283,10 +286,9 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
     size_t const nch = std::max<size_t>(1, std::min<size_t>(kHostChunks, n >> 20));
     for (size_t c = 0; c < nch; ++c) {
       size_t const i0 = n * c / nch, m = n * (c + 1) / nch - i0;
-      // x and y are the caller's device destinations in this mode
-      CSPT_CUDA_TRY(cudaMemcpyAsync(const_cast<T*>(x) + i0, host->hx + i0, m * sizeof(T),
+      CSPT_CUDA_TRY(cudaMemcpyAsync(host->dx + i0, host->hx + i0, m * sizeof(T),
                                     cudaMemcpyHostToDevice, copy));
-      CSPT_CUDA_TRY(cudaMemcpyAsync(const_cast<T*>(y) + i0, host->hy + i0, m * sizeof(T),
+      CSPT_CUDA_TRY(cudaMemcpyAsync(host->dy + i0, host->hy + i0, m * sizeof(T),
                                     cudaMemcpyHostToDevice, copy));
       stream_wait(s, copy);
       morton_keys_kernel<T><<<grid_for(m, blk, 152u * 16u), blk, 0, s>>>(
@@ -462,19 +464,33 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
 void quadtree_on_points(void const* x, void const* y, size_t n, cspt_dtype dtype, double x_min,
                         double x_max, double y_min, double y_max, double scale, int max_depth,
                         int32_t max_size, Allocator const& alloc, uint32_t** out_point_indices,
-                        cspt_quadtree* out_tree, void const* host_x, void const* host_y)
+                        cspt_quadtree* out_tree)
+{
+  if (dtype == CSPT_FLOAT64)
+    build<double>(static_cast<double const*>(x), static_cast<double const*>(y), n, x_min, x_max,
+                  y_min, y_max, scale, max_depth, max_size, alloc, out_point_indices, out_tree);
+  else
+    build<float>(static_cast<float const*>(x), static_cast<float const*>(y), n, x_min, x_max,
+                 y_min, y_max, scale, max_depth, max_size, alloc, out_point_indices, out_tree);
+}
+
+void quadtree_on_points_from_host(void const* host_x, void const* host_y, void* dev_x,
+                                  void* dev_y, size_t n, cspt_dtype dtype, double x_min,
+                                  double x_max, double y_min, double y_max, double scale,
+                                  int max_depth, int32_t max_size, Allocator const& alloc,
+                                  uint32_t** out_point_indices, cspt_quadtree* out_tree)
 {
   if (dtype == CSPT_FLOAT64) {
     HostInput<double> const h{static_cast<double const*>(host_x),
-                              static_cast<double const*>(host_y)};
-    build<double>(static_cast<double const*>(x), static_cast<double const*>(y), n, x_min, x_max,
-                  y_min, y_max, scale, max_depth, max_size, alloc, out_point_indices, out_tree,
-                  host_x ? &h : nullptr);
+                              static_cast<double const*>(host_y), static_cast<double*>(dev_x),
+                              static_cast<double*>(dev_y)};
+    build<double>(h.dx, h.dy, n, x_min, x_max, y_min, y_max, scale, max_depth, max_size, alloc,
+                  out_point_indices, out_tree, &h);
   } else {
-    HostInput<float> const h{static_cast<float const*>(host_x), static_cast<float const*>(host_y)};
-    build<float>(static_cast<float const*>(x), static_cast<float const*>(y), n, x_min, x_max,
-                 y_min, y_max, scale, max_depth, max_size, alloc, out_point_indices, out_tree,
-                 host_x ? &h : nullptr);
+    HostInput<float> const h{static_cast<float const*>(host_x), static_cast<float const*>(host_y),
+                             static_cast<float*>(dev_x), static_cast<float*>(dev_y)};
+    build<float>(h.dx, h.dy, n, x_min, x_max, y_min, y_max, scale, max_depth, max_size, alloc,
+                 out_point_indices, out_tree, &h);
   }
 }
 
