@@ -154,7 +154,7 @@ struct LinestringIndexView {
 // per linestring: box, anchor, float32 segments, chunk boxes (one warp each)
 __global__ void __launch_bounds__(256)
   ls_box_kernel(uint32_t const* __restrict__ lso, size_t nls, double const* __restrict__ lx,
-                double const* __restrict__ ly, double4* __restrict__ box, uint8_t* exact,
+                double const* __restrict__ ly, double4_16a* __restrict__ box, uint8_t* exact,
                 uint32_t* nchunks)
 {
   int const lane      = threadIdx.x & 31;
@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(256)
     }
     bad = __any_sync(0xFFFFFFFFu, bad);
     if (lane == 0) {
-      box[l]         = make_double4(mnx, mny, mxx, mxy);
+      box[l]         = make_double4_16a(mnx, mny, mxx, mxy);
       exact[l]       = bad ? 1 : 0;
       uint32_t const ns = v1 > v0 + 1 ? v1 - v0 - 1 : 0;
       nchunks[l]     = (ns + kSegChunk - 1) / kSegChunk;
@@ -188,13 +188,13 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-__global__ void __launch_bounds__(1024) ls_grid_kernel(double4 const* __restrict__ box, size_t nls,
+__global__ void __launch_bounds__(1024) ls_grid_kernel(double4_16a const* __restrict__ box, size_t nls,
                                                        double* grid)
 {
   __shared__ double part[32];
   double m = 0;
   for (size_t l = threadIdx.x; l < nls; l += blockDim.x) {
-    double4 const b = box[l];
+    double4_16a const b = box[l];
     double const v[4] = {b.x, b.y, b.z, b.w};
     for (double a : v)
       if (isfinite(a)) m = fmax(m, fabs(a));
@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(1024) ls_grid_kernel(double4 const* __restrict
 
 __global__ void __launch_bounds__(256)
   ls_fill_kernel(uint32_t const* __restrict__ lso, size_t nls, double const* __restrict__ lx,
-                 double const* __restrict__ ly, double4 const* __restrict__ box,
+                 double const* __restrict__ ly, double4_16a const* __restrict__ box,
                  double const* __restrict__ gridp, uint32_t const* __restrict__ chunk_base,
                  long long* aix, long long* aiy, float* maxoff, float4* chunk_box, float4* seg32)
 {
@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(256)
   for (size_t l = (blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5; l < nls;
        l += nwarps) {
     uint32_t const v0 = lso[l], v1 = lso[l + 1];
-    double4 const b   = box[l];
+    double4_16a const b   = box[l];
     double rx = v1 > v0 ? rint((b.x + b.z) * 0.5 / g) : 0.0;
     double ry = v1 > v0 ? rint((b.y + b.w) * 0.5 / g) : 0.0;
     if (!(fabs(rx) < 4.0e18)) rx = 0.0;
@@ -478,7 +478,7 @@ void run(uint32_t const* pair_ls, uint32_t const* pair_quad, size_t npairs,
   if constexpr (std::is_same<T, double>::value) {
     if (method == CSPT_METHOD_FILTERED) {
       // linestring index
-      Buffer<double4> box(alloc, nls);
+      Buffer<double4_16a> box(alloc, nls);
       Buffer<uint8_t> lexact(alloc, nls);
       Buffer<uint32_t> nch(alloc, nls + 1), cbase(alloc, nls + 1);
       Buffer<double> grid(alloc, 1);

@@ -79,35 +79,6 @@ __global__ void node_count_kernel(uint32_t const* __restrict__ starts, size_t nl
   }
 }
 
-// children of the previous level's nodes = next-level starts inside them
-__global__ void child_count_kernel(uint32_t const* __restrict__ prev_starts, size_t nprev,
-                                   uint32_t const* __restrict__ rank_cur, size_t n,
-                                   uint32_t* __restrict__ child)
-{
-  for (size_t p = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; p < nprev;
-       p += static_cast<size_t>(gridDim.x) * blockDim.x) {
-    size_t const e = (p + 1 < nprev) ? prev_starts[p + 1] : n;
-    child[p]       = rank_cur[e] - rank_cur[prev_starts[p]];
-  }
-}
-
-// A level-l node (l >= 1) survives iff its parent holds more than max_size
-// points (phase_2.cuh:206-236).
-__global__ void keep_kernel(uint32_t const* __restrict__ starts, size_t nl,
-                            uint8_t const* __restrict__ lvl, int prev_level,
-                            uint32_t const* __restrict__ rank_prev,
-                            uint32_t const* __restrict__ count_prev, uint32_t max_size,
-                            uint8_t* __restrict__ keep)
-{
-  for (size_t k = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; k < nl;
-       k += static_cast<size_t>(gridDim.x) * blockDim.x) {
-    uint32_t const i      = starts[k];
-    uint32_t const is_beg = (lvl[i] != kNoStart && lvl[i] <= prev_level) ? 1u : 0u;
-    uint32_t const parent = rank_prev[i] + is_beg - 1u;
-    keep[k]               = count_prev[parent] > max_size ? 1 : 0;
-  }
-}
-
 // finest level (d-1): every position whose key differs from its predecessor
 struct FinestStart {
   uint8_t const* lvl;
