@@ -4,7 +4,9 @@ points away from the boundary, the quadtree against the invariants of
 cpp/include/cuspatial/detail/index/construction/phase_2.cuh (a permutation,
 leaves that partition the sorted points, internal nodes above max_size), and
 the box join against a brute-force overlap of every leaf's cell with every
-box (pairs clearly overlapping must be there, pairs present must overlap)."""
+box (pairs clearly overlapping must be there, pairs clearly apart must not),
+and the pairwise and nearest-linestring distances against a numpy
+point-segment distance."""
 
 import numpy as np
 import pytest
@@ -14,7 +16,7 @@ from oracle import oracle as O
 
 def _convex_polygons(rng, n, dtype):
     """n convex polygons (regular k-gons, random centre, radius, rotation),
-    closed rings; returns offsets, vertices and the (centre, radius, k, phase)."""
+    closed rings; returns offsets, vertices and each polygon's own vertices."""
     xs, ys, ro, po, shapes = [], [], [0], [0], []
     for _ in range(n):
         k = int(rng.integers(3, 12))
@@ -33,8 +35,8 @@ def _convex_polygons(rng, n, dtype):
 
 
 def _inside_convex(px, py, vx, vy):
-    """Signed distances to the edges of a counter-clockwise convex polygon:
-    (all inside beyond margin, all-but-one clear); computed in float64."""
+    """Signed distance of each point to each edge line of a counter-clockwise
+    convex polygon (positive inside), in float64."""
     vx = vx.astype(np.float64)
     vy = vy.astype(np.float64)
     ax, ay = vx, vy
@@ -142,3 +144,77 @@ def test_join_matches_brute_force_overlap():
     # the reference's order: leaf first point, then box
     order = list(zip(t["offset"][j["quad_offset"]].tolist(), j["bbox_offset"].tolist()))
     assert order == sorted(order)
+
+
+def _segment_distances(px, py, lx, ly):
+    """Distance from each point to each segment (float64, numpy)."""
+    ax, ay, bx, by = lx[:-1], ly[:-1], lx[1:], ly[1:]
+    ex, ey = bx - ax, by - ay
+    l2 = ex * ex + ey * ey
+    t = ((px[:, None] - ax) * ex + (py[:, None] - ay) * ey) / np.where(l2 > 0, l2, 1.0)
+    t = np.clip(np.where(l2 > 0, t, 0.0), 0.0, 1.0)
+    dx = px[:, None] - (ax + t * ex)
+    dy = py[:, None] - (ay + t * ey)
+    return np.hypot(dx, dy)
+
+
+def test_pairwise_distance_matches_brute_force():
+    rng = np.random.default_rng(17)
+    n = 400
+    nv = rng.integers(2, 30, n)
+    start = np.concatenate([[0], np.cumsum(nv)])
+    lx = np.concatenate([c + np.cumsum(rng.normal(0, 3, k)) for c, k in
+                         zip(rng.uniform(-100, 100, n), nv)])
+    ly = np.concatenate([c + np.cumsum(rng.normal(0, 3, k)) for c, k in
+                         zip(rng.uniform(-100, 100, n), nv)])
+    x = lx[start[:-1]] + rng.normal(0, 10, n)
+    y = ly[start[:-1]] + rng.normal(0, 10, n)
+    o = O.pairwise_point_linestring(x, y, start, lx, ly)
+    for i in range(n):
+        s = slice(start[i], start[i + 1])
+        d = _segment_distances(x[i:i + 1], y[i:i + 1], lx[s], ly[s])[0]
+        assert abs(o["distance"][i] - d.min()) <= 1e-9 * max(1.0, d.min())
+        seg = int(o["segment_id"][i])
+        assert abs(d[seg] - d.min()) <= 1e-9 * max(1.0, d.min())
+        assert abs(np.hypot(o["x"][i] - x[i], o["y"][i] - y[i]) - d.min()) <= 1e-9 * max(1.0,
+                                                                                         d.min())
+
+
+def test_nearest_linestring_matches_brute_force():
+    rng = np.random.default_rng(23)
+    d, n, L = 5, 5000, 60
+    x = rng.uniform(0, 1000, n)
+    y = rng.uniform(0, 1000, n)
+    scale = 1000.0 / (1 << d)
+    pi, t = O.quadtree_on_points(x, y, 0.0, 1000.0, 0.0, 1000.0, scale, d, 64)
+    nv = rng.integers(2, 20, L)
+    lo = np.concatenate([[0], np.cumsum(nv)]).astype(np.uint32)
+    lx = np.concatenate([c + np.cumsum(rng.normal(0, 15, k)) for c, k in
+                         zip(rng.uniform(0, 1000, L), nv)])
+    ly = np.concatenate([c + np.cumsum(rng.normal(0, 15, k)) for c, k in
+                         zip(rng.uniform(0, 1000, L), nv)])
+    bb = O.linestring_bounding_boxes(lo, lx, ly, 60.0)
+    j = O.join_quadtree_and_bounding_boxes(t, bb, 0.0, 1000.0, 0.0, 1000.0, scale, d)
+    r = O.quadtree_point_to_nearest_linestring(j, t, pi, x, y, lo, lx, ly)
+    # candidates of each sorted position: the linestrings paired with its leaf
+    cand = {}
+    off, ln = t["offset"], t["length"]
+    for b, q in zip(j["bbox_offset"], j["quad_offset"]):
+        for pos in range(int(off[q]), int(off[q] + ln[q])):
+            cand.setdefault(pos, []).append(int(b))
+    checked = 0
+    for row, (pos, ls, dist) in enumerate(zip(r["point_index"], r["linestring_index"],
+                                              r["distance"])):
+        if int(pos) not in cand:
+            continue
+        p = int(pi[pos])
+        best = [(_segment_distances(x[p:p + 1], y[p:p + 1], lx[lo[c]:lo[c + 1]],
+                                    ly[lo[c]:lo[c + 1]])[0].min(), c) for c in cand[int(pos)]]
+        dmin = min(b[0] for b in best)
+        assert abs(dist - dmin) <= 1e-9 * max(1.0, dmin)
+        # ties (equal distances) go to the lower id; a clear winner must be it
+        clear = sorted(b[0] for b in best)
+        if len(clear) == 1 or clear[1] - clear[0] > 1e-6:
+            assert int(ls) == min(best)[1]
+        checked += 1
+    assert checked > 2000
