@@ -129,12 +129,12 @@ class BatchedPip {
   void execute(cudaStream_t s)
   {
     pip_->execute(s, op_.data(), oq_.data(), m_);
-    unsigned const g1 = grid_for(ni_ + 1, kBlk, kGridCap);
+    unsigned const g1 = grid_for(ni_ + 1, kBlk, grid_cap());
     row_offsets_kernel<<<g1, kBlk, 0, s>>>(pair_begin_.data(), pip_->pair_out_offsets(),
                                             static_cast<uint32_t>(ni_), row_off_.data());
     CSPT_CHECK_LAUNCH();
     if (m_) {
-      localize_kernel<<<grid_for(m_, kBlk, kGridCap), kBlk, 0, s>>>(
+      localize_kernel<<<grid_for(m_, kBlk, grid_cap()), kBlk, 0, s>>>(
         op_.data(), oq_.data(), m_, f_.pt_begin_.data(), static_cast<uint32_t>(ni_),
         f_.inst_.data(), true);
       CSPT_CHECK_LAUNCH();
@@ -230,7 +230,7 @@ class BatchedPip {
     CSPT_CUDA_TRY(cudaMemsetAsync(status.data(), 0, 2 * sizeof(uint32_t), s));
     int* err           = reinterpret_cast<int*>(status.data() + 1);
     unsigned const blk = kJoinWarps * 32;
-    unsigned const grd = grid_for(nb * 32, blk, kGridCap);
+    unsigned const grd = grid_for(nb * 32, blk, grid_cap());
     join_warp_kernel<double, false><<<grd, blk, 0, s>>>(
       tv, trees, bminx_.data(), bminy_.data(), bmaxx_.data(), bmaxy_.data(), nb, counts.data(),
       status.data(), nullptr, nullptr, nullptr, nullptr, err);
@@ -258,11 +258,11 @@ class BatchedPip {
                                                 perm_alt.data(), k_, 0, key_bits, true, a);
     pair_poly_ = Buffer<uint32_t>(a, k_);
     pair_quad_ = Buffer<uint32_t>(a, k_);
-    gather_pairs_kernel<<<grid_for(k_, kBlk, kGridCap), kBlk, 0, s>>>(
+    gather_pairs_kernel<<<grid_for(k_, kBlk, grid_cap()), kBlk, 0, s>>>(
       alt ? perm_alt.data() : perm.data(), node.data(), box.data(), k_, pair_poly_.data(),
       pair_quad_.data());
     CSPT_CHECK_LAUNCH();
-    pair_begin_kernel<<<grid_for(ni_ + 1, kBlk, kGridCap), kBlk, 0, s>>>(
+    pair_begin_kernel<<<grid_for(ni_ + 1, kBlk, grid_cap()), kBlk, 0, s>>>(
       alt ? key_alt.data() : key.data(), k_, f_.inst_.data(), ni, pair_begin_.data());
     CSPT_CHECK_LAUNCH();
   }

@@ -136,7 +136,7 @@ void run(uint32_t const* goff, size_t ngeom, uint32_t const* via, T const* x, T 
     },
     [rw] __device__(size_t g, uint32_t e, uint32_t) { rw[g] = e; }, ngeom, nonempty.data(),
     alloc);
-  bbox_kernel<T><<<grid_for(ngeom * 32, 256, 152u * 32u), 256, 0, s>>>(
+  bbox_kernel<T><<<grid_for(ngeom * 32, 256, sm_grid(32u)), 256, 0, s>>>(
     goff, goff + 1, via, ngeom, x, y, rw, r, ominx, ominy, omaxx, omaxy);
   CSPT_CHECK_LAUNCH();
   // rows past the number of non-empty geometries: NaN (the reference leaves
@@ -267,11 +267,11 @@ void run_noalloc(uint32_t const* po, size_t np, uint32_t const* ro, T const* x, 
   uint32_t* partials = scratch + kNoAllocMaxPolygons;
   uint32_t* nonempty = partials + kNoAllocPartials;
   scan_apply_prealloc<uint32_t>(NonEmptyPolygon{po, ro}, StoreRow{row}, np, nonempty, partials, s);
-  bbox_kernel<T><<<grid_for(np * 32, 256, 152u * 32u), 256, 0, s>>>(
+  bbox_kernel<T><<<grid_for(np * 32, 256, sm_grid(32u)), 256, 0, s>>>(
     po, po + 1, ro, np, x, y, row, r, ominx, ominy, omaxx, omaxy);
   CSPT_CHECK_LAUNCH();
   nan_tail_kernel<T>
-    <<<grid_for(np, 256, 152u * 16u), 256, 0, s>>>(nonempty, np, ominx, ominy, omaxx, omaxy);
+    <<<grid_for(np, 256, sm_grid(16u)), 256, 0, s>>>(nonempty, np, ominx, ominy, omaxx, omaxy);
   CSPT_CHECK_LAUNCH();
 }
 

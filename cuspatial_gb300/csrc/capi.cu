@@ -100,13 +100,22 @@ void clear_last_error() { t_last_error.clear(); }
 
 int num_sms()
 {
-  static int sms = [] {
-    int dev = 0, n = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    return n > 0 ? n : 152;
-  }();
-  return sms;
+  // one entry per device ordinal, filled on first use with that device current
+  constexpr int kMaxDevices = 64;
+  static std::atomic<int> sms[kMaxDevices];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    (void)cudaGetLastError();
+    dev = 0;
+  }
+  int n = sms[dev].load(std::memory_order_relaxed);
+  if (n > 0) return n;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+    (void)cudaGetLastError();
+    n = 152;  // GB300
+  }
+  sms[dev].store(n, std::memory_order_relaxed);
+  return n;
 }
 
 cudaStream_t side_stream()

@@ -201,7 +201,10 @@ inline unsigned grid_for(size_t n, unsigned block, unsigned cap = 1u << 20)
   return static_cast<unsigned>(g);
 }
 
+// Streaming multiprocessors of the current device (cached per device).
 int num_sms();
+// Grid cap of `per_sm` blocks on every SM of the current device.
+inline unsigned sm_grid(unsigned per_sm) { return static_cast<unsigned>(num_sms()) * per_sm; }
 
 // A second stream of the calling thread on the current device, for work that
 // overlaps the caller's stream inside one call (created on first use;

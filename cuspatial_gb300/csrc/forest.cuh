@@ -35,7 +35,7 @@ namespace {
 constexpr int kLevels       = 16;
 constexpr uint8_t kNoStart  = 0xFF;
 constexpr unsigned kBlk     = 256;
-constexpr unsigned kGridCap = 152u * 16u;
+inline unsigned grid_cap() { return sm_grid(16u); }
 
 struct Inst {
   double minx, miny, maxx, maxy, scale, rscale;
@@ -430,7 +430,7 @@ class Forest {
       return;
     }
     KernelTimer timer("forest_build", s);
-    unsigned const grd   = grid_for(n, kBlk, kGridCap);
+    unsigned const grd   = grid_for(n, kBlk, grid_cap());
     int const kb         = dmax_ >= 2 ? 2 * dmax_ + 2 : 2 * dmax_ + 4;
     int ib               = 0;
     while ((uint64_t{1} << ib) < ni_) ++ib;
@@ -485,14 +485,14 @@ class Forest {
       L.start        = Buffer<uint32_t>(a, m);
       L.inst         = Buffer<uint32_t>(a, m);
       if (nl) {
-        compact_level_kernel<<<grid_for(nl, kBlk, kGridCap), kBlk, 0, s>>>(
+        compact_level_kernel<<<grid_for(nl, kBlk, grid_cap()), kBlk, 0, s>>>(
           nl, kp, pos.data(), starts.data(), counts.data(), childs ? childs->data() : nullptr,
           ninst.data(), sk.data(), kb, inst_.data(), lv, L.key.data(), L.count.data(),
           L.child.data(), L.start.data(), L.inst.data());
         CSPT_CHECK_LAUNCH();
       }
       if (m) {
-        level_span_kernel<<<grid_for(m, kBlk, kGridCap), kBlk, 0, s>>>(L.inst.data(), m, lv,
+        level_span_kernel<<<grid_for(m, kBlk, grid_cap()), kBlk, 0, s>>>(L.inst.data(), m, lv,
                                                                        first.data(), end.data());
         CSPT_CHECK_LAUNCH();
       }
@@ -507,7 +507,7 @@ class Forest {
       count_cur       = Buffer<uint32_t>(a, nl);
       inst_cur        = Buffer<uint32_t>(a, nl);
       keep_cur        = Buffer<uint8_t>(a, nl);
-      unsigned const g = grid_for(nl, kBlk, kGridCap);
+      unsigned const g = grid_for(nl, kBlk, grid_cap());
       if (nl) {
         count_kernel<<<g, kBlk, 0, s>>>(starts_cur.data(), nl, sk.data(), kb, inst_.data(),
                                         count_cur.data(), inst_cur.data());
@@ -524,7 +524,7 @@ class Forest {
         }
         Buffer<uint32_t> child_prev(a, n_prev);
         if (n_prev) {
-          child_count_kernel<<<grid_for(n_prev, kBlk, kGridCap), kBlk, 0, s>>>(
+          child_count_kernel<<<grid_for(n_prev, kBlk, grid_cap()), kBlk, 0, s>>>(
             starts_prev.data(), n_prev, inst_prev.data(), inst_.data(), rank_cur.data(),
             child_prev.data());
           CSPT_CHECK_LAUNCH();
@@ -573,7 +573,7 @@ class Forest {
     for (int l = 0; l < dmax_; ++l) {
       Level& L = levels[l];
       if (L.size) {
-        assemble_kernel<<<grid_for(L.size, kBlk, kGridCap), kBlk, 0, s>>>(
+        assemble_kernel<<<grid_for(L.size, kBlk, grid_cap()), kBlk, 0, s>>>(
           L.key.data(), L.count.data(), L.child.data(), L.start.data(), L.inst.data(), L.size,
           l, inst_.data(), shift.data(), key_.data(), level_.data(), internal_.data(),
           length_.data(), offset_.data(), ichild.data(), node_inst.data());
@@ -582,7 +582,7 @@ class Forest {
       L = Level{};
     }
     exclusive_scan<uint32_t>(ichild.data(), ichild.data(), q, static_cast<uint32_t*>(nullptr), a);
-    offsets_kernel<<<grid_for(q, kBlk, kGridCap), kBlk, 0, s>>>(
+    offsets_kernel<<<grid_for(q, kBlk, grid_cap()), kBlk, 0, s>>>(
       internal_.data(), ichild.data(), node_inst.data(), inst_.data(), q, offset_.data(),
       goff_.data());
     CSPT_CHECK_LAUNCH();

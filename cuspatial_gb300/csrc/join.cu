@@ -62,7 +62,7 @@ void run(cspt_quadtree const* tree, T const* bminx, T const* bminy, T const* bma
   CSPT_CUDA_TRY(cudaMemsetAsync(status.data(), 0, 2 * sizeof(uint32_t), s));
   int* err           = reinterpret_cast<int*>(status.data() + 1);
   unsigned const blk = kJoinWarps * 32;
-  unsigned const grd = grid_for(nb * 32, blk, 152u * 16u);
+  unsigned const grd = grid_for(nb * 32, blk, sm_grid(16u));
   // the count pass also appends each (node, box) it finds while they fit
   size_t const cap = join_append_capacity(nb);
   Buffer<uint32_t> app_node(alloc, cap), app_box(alloc, cap);
@@ -104,14 +104,14 @@ void run(cspt_quadtree const* tree, T const* bminx, T const* bminy, T const* bma
     Buffer<uint32_t> perm(alloc, k), perm_alt(alloc, k);
     {
       KernelTimer timer("join_write", s);
-      composite_key_kernel<<<grid_for(k, 256, 152u * 16u), 256, 0, s>>>(
+      composite_key_kernel<<<grid_for(k, 256, sm_grid(16u)), 256, 0, s>>>(
         app_node.data(), app_box.data(), k, tv.offset, box_bits, key.data());
       CSPT_CHECK_LAUNCH();
     }
     bool const alt = radix_sort_pairs<uint64_t>(key.data(), perm.data(), key_alt.data(),
                                                 perm_alt.data(), k, 0, key_bits + box_bits, true,
                                                 alloc);
-    gather_pairs_kernel<<<grid_for(k, 256, 152u * 16u), 256, 0, s>>>(
+    gather_pairs_kernel<<<grid_for(k, 256, sm_grid(16u)), 256, 0, s>>>(
       alt ? perm_alt.data() : perm.data(), app_node.data(), app_box.data(), k, ob.data(),
       on.data());
     CSPT_CHECK_LAUNCH();
@@ -129,7 +129,7 @@ void run(cspt_quadtree const* tree, T const* bminx, T const* bminy, T const* bma
     }
     bool const alt = radix_sort_pairs<uint32_t>(key.data(), perm.data(), key_alt.data(),
                                                 perm_alt.data(), k, 0, key_bits, true, alloc);
-    gather_pairs_kernel<<<grid_for(k, 256, 152u * 16u), 256, 0, s>>>(
+    gather_pairs_kernel<<<grid_for(k, 256, sm_grid(16u)), 256, 0, s>>>(
       alt ? perm_alt.data() : perm.data(), node.data(), box.data(), k, ob.data(), on.data());
     CSPT_CHECK_LAUNCH();
   }

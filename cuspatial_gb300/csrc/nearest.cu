@@ -460,7 +460,7 @@ void run(uint32_t const* pair_ls, uint32_t const* pair_quad, size_t npairs,
          cspt_method method, Allocator const& alloc, uint32_t* opt, uint32_t* ols, T* od)
 {
   cudaStream_t const s = alloc.stream();
-  init_rows_kernel<<<grid_for(npi, 256, 152u * 16u), 256, 0, s>>>(npi, opt, ols, od, sizeof(T));
+  init_rows_kernel<<<grid_for(npi, 256, sm_grid(16u)), 256, 0, s>>>(npi, opt, ols, od, sizeof(T));
   CSPT_CHECK_LAUNCH();
   // groups: runs of consecutive pairs with the same quadrant first-point offset
   uint32_t const* qoff = tree->offset;
@@ -482,7 +482,7 @@ void run(uint32_t const* pair_ls, uint32_t const* pair_quad, size_t npairs,
       Buffer<uint8_t> lexact(alloc, nls);
       Buffer<uint32_t> nch(alloc, nls + 1), cbase(alloc, nls + 1);
       Buffer<double> grid(alloc, 1);
-      unsigned const lgrd = grid_for(nls * 32, 256, 152u * 32u);
+      unsigned const lgrd = grid_for(nls * 32, 256, sm_grid(32u));
       ls_box_kernel<<<lgrd, 256, 0, s>>>(lso, nls, lx, ly, box.data(), lexact.data(), nch.data());
       CSPT_CHECK_LAUNCH();
       ls_grid_kernel<<<1, 1024, 0, s>>>(box.data(), nls, grid.data());
@@ -500,7 +500,7 @@ void run(uint32_t const* pair_ls, uint32_t const* pair_quad, size_t npairs,
       // leaf frames of the groups
       Buffer<float2> u(alloc, npi);
       Buffer<LeafFrame> frames(alloc, npairs);
-      leaf_frame_kernel<<<grid_for(npairs * 32, 256, 152u * 32u), 256, 0, s>>>(
+      leaf_frame_kernel<<<grid_for(npairs * 32, 256, sm_grid(32u)), 256, 0, s>>>(
         gs, gs + npairs, pair_quad, tree->length, qoff, point_indices, npi, x, y, grid.data(),
         u.data(), frames.data());
       CSPT_CHECK_LAUNCH();
@@ -509,7 +509,7 @@ void run(uint32_t const* pair_ls, uint32_t const* pair_quad, size_t npairs,
       Buffer<unsigned long long> fb(alloc, 1);
       CSPT_CUDA_TRY(cudaMemsetAsync(fb.data(), 0, sizeof(unsigned long long), s));
       KernelTimer timer("nearest", s);
-      nearest_filtered_kernel<<<grid_for(npairs * 32, 256, 152u * 32u), 256, 0, s>>>(
+      nearest_filtered_kernel<<<grid_for(npairs * 32, 256, sm_grid(32u)), 256, 0, s>>>(
         gs, gs + npairs, npairs, pair_ls, pair_quad, tree->length, qoff, point_indices, npi, x,
         y, lso, nls, lx, ly, u.data(), frames.data(), liv, static_cast<float>(g), opt, ols, od,
         fb.data());
@@ -521,7 +521,7 @@ void run(uint32_t const* pair_ls, uint32_t const* pair_quad, size_t npairs,
   size_t const ng = read_back(gs + npairs, s);
   {
     KernelTimer timer("nearest", s);
-    nearest_kernel<T, false><<<grid_for(ng * 32, 256, 152u * 32u), 256, 0, s>>>(
+    nearest_kernel<T, false><<<grid_for(ng * 32, 256, sm_grid(32u)), 256, 0, s>>>(
       gs, ng, npairs, pair_ls, pair_quad, tree->length, qoff, point_indices, npi, x, y, lso,
       nls, lx, ly, opt, ols, od);
     CSPT_CHECK_LAUNCH();

@@ -606,7 +606,7 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
             nullptr, nullptr, index.view(), word_off.data() + k0, bits.data(), counts.data() + k0,
             nullptr, refined.data() + 1);
     } else {
-      pip_pair_kernel_f32<<<grid_for(n * 32, blk, 152u * 8u * 4u), blk, 0, s>>>(
+      pip_pair_kernel_f32<<<grid_for(n * 32, blk, sm_grid(8u * 4u)), blk, 0, s>>>(
         pair_poly + k0, pair_quad + k0, n, qlen, qoff, point_indices, npi, x, y, index.view(),
         word_off.data() + k0, bits.data(), counts.data() + k0);
     }
@@ -625,7 +625,7 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
   auto expand = [&](size_t k0, size_t n, Buffer<uint64_t> const& out_off, uint32_t* op,
                     uint32_t* oq, size_t m) {
     KernelTimer timer("pip_expand", s);
-    pip_expand_kernel<<<grid_for(n * 32, blk, 152u * 8u * 4u), blk, 0, s>>>(
+    pip_expand_kernel<<<grid_for(n * 32, blk, sm_grid(8u * 4u)), blk, 0, s>>>(
       pair_poly + k0, pair_quad + k0, n, qlen, qoff, word_off.data() + k0, bits.data(),
       out_off.data(), op, oq, m);
     CSPT_CHECK_LAUNCH();
@@ -776,7 +776,7 @@ class PipExec::Impl {
   void evaluate(cudaStream_t s)
   {
     unsigned const blk = blk_;
-    unsigned const grd = grid_for(np_ * 32, blk, 152u * 8u * 1024u / blk);
+    unsigned const grd = grid_for(np_ * 32, blk, sm_grid(8u * 1024u / blk));
     CSPT_CUDA_TRY(cudaMemsetAsync(refined_.data(), 0, 2 * sizeof(unsigned long long), s));
     if (filtered_) {
       leaf_frame_kernel<<<grd, blk, 0, s>>>(gstart_.data(), gstart_.data() + np_, pq_, qlen_,
@@ -807,7 +807,7 @@ class PipExec::Impl {
   void expand(cudaStream_t s, uint32_t* op, uint32_t* oq, uint64_t cap)
   {
     unsigned const blk = blk_;
-    unsigned const grd = grid_for(np_ * 32, blk, 152u * 8u * 1024u / blk);
+    unsigned const grd = grid_for(np_ * 32, blk, sm_grid(8u * 1024u / blk));
     pip_expand_kernel<<<grd, blk, 0, s>>>(pp_, pq_, np_, qlen_, qoff_, word_off_.data(),
                                           bits_.data(), out_off_.data(), op, oq, cap);
     CSPT_CHECK_LAUNCH();

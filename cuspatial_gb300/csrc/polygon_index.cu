@@ -753,7 +753,7 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
   Buffer<uint32_t> spans(alloc, nv);
   Buffer<float> yslab(alloc, nv);
 
-  unsigned const grd = static_cast<unsigned>(np < 152u * 64u ? (np ? np : 1) : 152u * 64u);
+  unsigned const grd = static_cast<unsigned>(np < sm_grid(64u) ? (np ? np : 1) : sm_grid(64u));
   if (np > 0) {
     index_count_kernel<T><<<grd, kIdxBlock, 0, s>>>(
       po, ro, vx, vy, np, pminx_.data(), pminy_.data(), pmaxx_.data(), pmaxy_.data(),
@@ -775,7 +775,7 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
   Buffer<unsigned long long> wide(alloc, 2);
   CSPT_CUDA_TRY(cudaMemsetAsync(wide.data(), 0, 2 * sizeof(unsigned long long), s));
   if (np > 0) {
-    wide_totals_kernel<<<grid_for(np, 256, 152u * 4u), 256, 0, s>>>(nslab_.data(), nent.data(),
+    wide_totals_kernel<<<grid_for(np, 256, sm_grid(4u)), 256, 0, s>>>(nslab_.data(), nent.data(),
                                                                      np, wide.data());
     CSPT_CHECK_LAUNCH();
   }
@@ -828,7 +828,7 @@ void PolygonIndex<T>::fill()
       slab_edges_.data(), slab_e32_.data(), vert_x_.data(), vert_x32_.data(), vxy32.data(),
       z->yslab.data());
     CSPT_CHECK_LAUNCH();
-    vert_end_kernel<<<grid_for(np, 256, 152u * 16u), 256, 0, s>>>(vbeg_.data(), z->nvert.data(),
+    vert_end_kernel<<<grid_for(np, 256, sm_grid(16u)), 256, 0, s>>>(vbeg_.data(), z->nvert.data(),
                                                                   np, vend_.data());
     CSPT_CHECK_LAUNCH();
   }

@@ -240,7 +240,7 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
   scale                   = scale > min_scale ? scale : min_scale;
 
   unsigned const blk = 256;
-  unsigned const grd = grid_for(n, blk, 152u * 16u);
+  unsigned const grd = grid_for(n, blk, sm_grid(16u));
   KernelTimer timer("quadtree_build", s);
 
   Buffer<uint32_t> keys(alloc, n), keys_alt(alloc, n);
@@ -262,7 +262,7 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
       CSPT_CUDA_TRY(cudaMemcpyAsync(host->dy + i0, host->hy + i0, m * sizeof(T),
                                     cudaMemcpyHostToDevice, copy));
       stream_wait(s, copy);
-      morton_keys_kernel<T><<<grid_for(m, blk, 152u * 16u), blk, 0, s>>>(
+      morton_keys_kernel<T><<<grid_for(m, blk, sm_grid(16u)), blk, 0, s>>>(
         x + i0, y + i0, m, minx, miny, maxx, maxy, scale, T{1} / scale, d, keys.data() + i0);
       CSPT_CHECK_LAUNCH();
     }
@@ -300,7 +300,7 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
     size_t const q = read_back(total.data(), s);
     Buffer<uint32_t> okey(alloc, q), olen(alloc, q), ooff(alloc, q);
     Buffer<uint8_t> olev(alloc, q), oint(alloc, q);
-    node_count_kernel<<<grid_for(q, blk, 152u * 16u), blk, 0, s>>>(st, q, n, olen.data());
+    node_count_kernel<<<grid_for(q, blk, sm_grid(16u)), blk, 0, s>>>(st, q, n, olen.data());
     CSPT_CHECK_LAUNCH();
     uint32_t const* sk = skeys.data();
     uint32_t* ok       = okey.data();
@@ -363,7 +363,7 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
     Buffer<uint32_t> child(alloc, l + 1 < d ? nl : 0);
     Buffer<uint8_t> keep(alloc, nl);
     if (nl) {
-      level_nodes_kernel<<<grid_for(nl, blk, 152u * 16u), blk, 0, s>>>(
+      level_nodes_kernel<<<grid_for(nl, blk, sm_grid(16u)), blk, 0, s>>>(
         R.S.data(), R.X.data(), nl, n, l + 1 < d ? raw[l + 1].n : 0, l > 0 ? R.P.data() : nullptr,
         l > 0 ? raw[l - 1].count.data() : nullptr, max_size, R.count.data(),
         l + 1 < d ? child.data() : nullptr, keep.data());
@@ -384,7 +384,7 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
     L.child        = Buffer<uint32_t>(alloc, m);
     L.start        = Buffer<uint32_t>(alloc, m);
     if (nl) {
-      compact_nodes_kernel<<<grid_for(nl, blk, 152u * 16u), blk, 0, s>>>(
+      compact_nodes_kernel<<<grid_for(nl, blk, sm_grid(16u)), blk, 0, s>>>(
         nl, kp, ps, R.S.data(), R.count.data(), l + 1 < d ? child.data() : nullptr,
         skeys.data(), 2 * (d - 1 - l), L.key.data(), L.count.data(), L.child.data(),
         L.start.data());
@@ -410,7 +410,7 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
   for (int l = 0; l < d; ++l) {
     LevelNodes& L = levels[l];
     if (L.size) {
-      assemble_kernel<<<grid_for(L.size, blk, 152u * 16u), blk, 0, s>>>(
+      assemble_kernel<<<grid_for(L.size, blk, sm_grid(16u)), blk, 0, s>>>(
         L.key.data(), L.count.data(), L.child.data(), L.start.data(), L.size,
         static_cast<uint8_t>(l), l <= d - 2, max_size, base, okey.data(), olev.data(),
         oint.data(), olen.data(), ooff.data(), ichild.data());
@@ -422,7 +422,7 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
   // detail/point_quadtree.cuh:82-109: internal offsets = level_1_size + scan
   exclusive_scan<uint32_t>(ichild.data(), ichild.data(), q, static_cast<uint32_t*>(nullptr),
                            alloc);
-  internal_offset_kernel<<<grid_for(q, blk, 152u * 16u), blk, 0, s>>>(
+  internal_offset_kernel<<<grid_for(q, blk, sm_grid(16u)), blk, 0, s>>>(
     oint.data(), ichild.data(), q, static_cast<uint32_t>(level_1_size), ooff.data());
   CSPT_CHECK_LAUNCH();
   *out_point_indices = sidx.release();

@@ -344,7 +344,7 @@ class PolygonSet {
     Buffer<uint32_t> cursor(a, ncell);
     CSPT_CUDA_TRY(cudaMemsetAsync(cell_start_.data(), 0, (ncell + 1) * 4, s));
     CSPT_CUDA_TRY(cudaMemsetAsync(cursor.data(), 0, ncell * 4, s));
-    unsigned const grd = grid_for(np_, 256, 152u * 16u);
+    unsigned const grd = grid_for(np_, 256, sm_grid(16u));
     grid_count_kernel<<<grd, 256, 0, s>>>(g_, np_, cell_start_.data(), poly_cell_.data());
     CSPT_CHECK_LAUNCH();
     exclusive_scan<uint32_t>(cell_start_.data(), cell_start_.data(), ncell,
@@ -411,14 +411,14 @@ class ServingBatch {
     size_t nitems = 0;
     {
       KernelTimer timer("serving_join", s);
-      leaf_cells_kernel<<<grid_for(q, blk, 152u * 16u), blk, 0, s>>>(
+      leaf_cells_kernel<<<grid_for(q, blk, sm_grid(16u)), blk, 0, s>>>(
         f_.view(), f_.node_off_.data(), ni32, f_.inst_.data(), g, lc.data(), cell_off.data());
       CSPT_CHECK_LAUNCH();
       exclusive_scan<uint32_t>(cell_off.data(), cell_off.data(), q, cell_off.data() + q, a);
       nitems = read_back(cell_off.data() + q, s);
       counts = Buffer<uint32_t>(a, nitems + 1);
       if (nitems) {
-        leaf_cell_join_kernel<false><<<grid_for(nitems, blk, 152u * 16u), blk, 0, s>>>(
+        leaf_cell_join_kernel<false><<<grid_for(nitems, blk, sm_grid(16u)), blk, 0, s>>>(
           lc.data(), cell_off.data(), q, nitems, g, f_.goff_.data(), counts.data(), nullptr,
           pbits, nullptr, nullptr, nullptr);
         CSPT_CHECK_LAUNCH();
@@ -434,7 +434,7 @@ class ServingBatch {
     {
       Buffer<uint64_t> key(a, k_), key_alt(a, k_);
       Buffer<uint32_t> poly(a, k_), node(a, k_), perm(a, k_), perm_alt(a, k_);
-      leaf_cell_join_kernel<true><<<grid_for(nitems, blk, 152u * 16u), blk, 0, s>>>(
+      leaf_cell_join_kernel<true><<<grid_for(nitems, blk, sm_grid(16u)), blk, 0, s>>>(
         lc.data(), cell_off.data(), q, nitems, g, f_.goff_.data(), nullptr, counts.data(), pbits,
         key.data(), poly.data(), node.data());
       CSPT_CHECK_LAUNCH();
@@ -444,11 +444,11 @@ class ServingBatch {
                                                   perm_alt.data(), k_, 0, bits, true, a);
       pair_poly_ = Buffer<uint32_t>(a, k_);
       pair_quad_ = Buffer<uint32_t>(a, k_);
-      gather_sorted_pairs_kernel<<<grid_for(k_, 256, 152u * 16u), 256, 0, s>>>(
+      gather_sorted_pairs_kernel<<<grid_for(k_, 256, sm_grid(16u)), 256, 0, s>>>(
         alt ? perm_alt.data() : perm.data(), poly.data(), node.data(), k_, pair_poly_.data(),
         pair_quad_.data());
       CSPT_CHECK_LAUNCH();
-      pair_begin64_kernel<<<grid_for(ni + 1, 256, 152u * 16u), 256, 0, s>>>(
+      pair_begin64_kernel<<<grid_for(ni + 1, 256, sm_grid(16u)), 256, 0, s>>>(
         alt ? key_alt.data() : key.data(), k_, pbits, f_.inst_.data(), ni32,
         pair_begin_.data());
       CSPT_CHECK_LAUNCH();
@@ -464,11 +464,11 @@ class ServingBatch {
     op_ = Buffer<uint32_t>(a, m_);
     oq_ = Buffer<uint32_t>(a, m_);
     pip.expand(s, op_.data(), oq_.data(), m_);
-    row_offsets_kernel<<<grid_for(ni + 1, 256, 152u * 16u), 256, 0, s>>>(
+    row_offsets_kernel<<<grid_for(ni + 1, 256, sm_grid(16u)), 256, 0, s>>>(
       pair_begin_.data(), pip.pair_out_offsets(), ni32, row_off_.data());
     CSPT_CHECK_LAUNCH();
     if (m_) {
-      localize_kernel<<<grid_for(m_, 256, 152u * 16u), 256, 0, s>>>(
+      localize_kernel<<<grid_for(m_, 256, sm_grid(16u)), 256, 0, s>>>(
         op_.data(), oq_.data(), m_, f_.pt_begin_.data(), ni32, f_.inst_.data(), false);
       CSPT_CHECK_LAUNCH();
     }
