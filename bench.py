@@ -43,8 +43,6 @@ def parse_args():
     ap.add_argument("--method", choices=["filtered", "exact"], default="filtered")
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--cpu-seconds", type=float, default=15.0,
-                    help="target CPU time of the oracle baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", choices=["precision", "batched", "serving", "nearest",
                                            "unindexed"],
@@ -94,6 +92,78 @@ class Dist:
         t = torch.tensor([float(v)], device="cuda" if torch.cuda.is_available() else "cpu")
         self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
         return float(t.item())
+
+
+# --------------------------------------------------------------------------
+# host link: where the GPU and the page-locked buffers sit, and what one
+# plain copy of 1 GiB each way sustains (the e2e leg's copies are bounded by
+# it)
+# --------------------------------------------------------------------------
+def gpu_numa(device_index):
+    """NUMA node and local CPUs of the GPU's PCI device (Linux sysfs)."""
+    import torch
+    info = {}
+    try:
+        bus = torch.cuda.get_device_properties(device_index).pci_bus_id.lower()
+    except Exception:  # noqa: BLE001 - older torch: no bus id
+        return info
+    for dom in (bus, bus.replace("00000000:", "0000:")):
+        base = "/sys/bus/pci/devices/" + dom
+        if os.path.isdir(base):
+            for k in ("numa_node", "local_cpulist"):
+                try:
+                    info[k] = open(os.path.join(base, k)).read().strip()
+                except OSError:
+                    pass
+            info["pci_bus_id"] = dom
+            break
+    return info
+
+
+def pages_by_node(ptr, nbytes):
+    """Resident pages of [ptr, ptr + nbytes) per NUMA node, from
+    /proc/self/numa_maps of the mapping that holds ptr."""
+    try:
+        start = None
+        for line in open("/proc/self/maps"):
+            lo, hi = (int(v, 16) for v in line.split()[0].split("-"))
+            if lo <= ptr < hi:
+                start = lo
+                break
+        if start is None:
+            return None
+        for line in open("/proc/self/numa_maps"):
+            f = line.split()
+            if int(f[0], 16) == start:
+                return {kv.split("=")[0]: int(kv.split("=")[1]) for kv in f[1:]
+                        if kv.startswith("N") and "=" in kv}
+    except (OSError, ValueError):
+        return None
+    return None
+
+
+def measure_link(stream, nbytes=1 << 30, reps=3):
+    """GB/s of one cudaMemcpyAsync of nbytes from page-locked host memory to
+    the device and back, best of reps, with the pages' NUMA placement."""
+    import torch
+    h = torch.empty(nbytes // 8, dtype=torch.float64).pin_memory()
+    h.fill_(1.0)
+    d = torch.empty_like(h, device="cuda")
+    out = {"bytes": nbytes, "host_pages_by_node": pages_by_node(h.data_ptr(), nbytes)}
+    for name, dst, src in (("h2d_gbs", d, h), ("d2h_gbs", h, d)):
+        best = None
+        for _ in range(reps):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            dst.copy_(src, non_blocking=True)
+            b.record(stream)
+            b.synchronize()
+            ms = a.elapsed_time(b)
+            best = ms if best is None else min(best, ms)
+        out[name] = nbytes / (best / 1e3) / 1e9
+    del d, h
+    return out
 
 
 # --------------------------------------------------------------------------
@@ -206,51 +276,62 @@ def polygons_xy(P):
 # --------------------------------------------------------------------------
 # CPU oracle baseline on a polygon sample (and an at-scale parity check)
 # --------------------------------------------------------------------------
-def cpu_baseline(w, tree_np, pi_np, pairs_np, gpu_pip, target_s):
-    from oracle import oracle as O
+# One sampling rule for both arms: the polygons i with i % CPU_STRIDE == offset
+# (5% of them) against the full point set.  The sample's wall time is
+# measured; the full join's time is estimated by scaling the join by the
+# polygon fraction and the point-in-polygon tests by the candidate fraction.
+CPU_STRIDE = 20
+
+
+def cpu_sample(O, w, tree_np, pi_np, bb, qlen, cand_total, offset):
     P = w.polygons
     npoly = P.num_polygons
+    sel = np.arange(offset % CPU_STRIDE, npoly, CPU_STRIDE)
+    sbb = {k: np.ascontiguousarray(v[sel]) for k, v in bb.items()}
+    t0 = time.perf_counter()
+    sj = O.join_quadtree_and_bounding_boxes(tree_np, sbb, w.x_min, w.x_max, w.y_min, w.y_max,
+                                            w.scale, w.max_depth)
+    t1 = time.perf_counter()
+    sj = dict(bbox_offset=sel[sj["bbox_offset"]].astype(np.uint32), quad_offset=sj["quad_offset"])
+    r = O.quadtree_point_in_polygon(sj, tree_np, pi_np, w.x, w.y, P.part_offset, P.ring_offset,
+                                    P.x, P.y)
+    t2 = time.perf_counter()
+    cand_s = int(qlen[sj["quad_offset"]].sum())
+    full_s = (t1 - t0) * npoly / len(sel) + (t2 - t1) * cand_total / max(cand_s, 1)
+    return {"sel": sel, "rows": r, "sample_s": t2 - t0, "full_s": full_s,
+            "cand_fraction": cand_s / max(cand_total, 1), "polygons": len(sel),
+            "value": len(w.x) / full_s}
+
+
+def cpu_sample_text(res, n):
+    return ("polygons i with i %% %d == offset (%d of %d, %.2f%% of candidates) against all "
+            "%d points; sampled wall time %.2f s, scaled to the full join (join by polygons, "
+            "point-in-polygon by candidates) %.1f s" %
+            (CPU_STRIDE, res["polygons"], res["polygons"] * CPU_STRIDE, 100 * res["cand_fraction"],
+             n, res["sample_s"], res["full_s"]))
+
+
+# --------------------------------------------------------------------------
+# CPU oracle baseline on a polygon sample (and an at-scale parity check)
+# --------------------------------------------------------------------------
+def cpu_baseline(w, tree_np, pi_np, pairs_np, gpu_pip):
+    from oracle import oracle as O
+    P = w.polygons
     qlen = tree_np["length"].astype(np.int64)
     cand_total = int(qlen[pairs_np["quad_offset"]].sum())
-    # size the sample from a small probe: every stride-th polygon
-    stride = max(1, npoly // 50)
-    tried = []
     bb = O.polygon_bounding_boxes(P.part_offset, P.ring_offset, P.x, P.y)
-    while True:
-        sel = np.arange(0, npoly, stride)
-        sbb = {k: np.ascontiguousarray(v[sel]) for k, v in bb.items()}
-        t0 = time.perf_counter()
-        sj = O.join_quadtree_and_bounding_boxes(tree_np, sbb, w.x_min, w.x_max, w.y_min, w.y_max,
-                                                w.scale, w.max_depth)
-        t1 = time.perf_counter()
-        sj = dict(bbox_offset=sel[sj["bbox_offset"]].astype(np.uint32),
-                  quad_offset=sj["quad_offset"])
-        r = O.quadtree_point_in_polygon(sj, tree_np, pi_np, w.x, w.y, P.part_offset,
-                                        P.ring_offset, P.x, P.y)
-        t2 = time.perf_counter()
-        tried.append((stride, t2 - t0))
-        if t2 - t0 >= target_s / 4 or stride == 1:
-            break
-        stride = max(1, int(stride * (t2 - t0) / target_s))
-        if stride == tried[-1][0]:
-            break
-    cand_s = int(qlen[sj["quad_offset"]].sum())
-    t_join_full = (t1 - t0) * npoly / len(sel)
-    t_pip_full = (t2 - t1) * cand_total / max(cand_s, 1)
-    value = len(w.x) / (t_join_full + t_pip_full)
+    res = cpu_sample(O, w, tree_np, pi_np, bb, qlen, cand_total, 0)
+    r = res["rows"]
     # parity at scale: the GPU pairs of the sampled polygons, in order
     gp = gpu_pip["polygon_index"]
-    keep = np.isin(gp, sel)
+    keep = np.isin(gp, res["sel"])
     parity = bool(np.array_equal(gp[keep], r["polygon_index"]) and
                   np.array_equal(gpu_pip["point_index"][keep], r["point_index"]))
     return {
-        "value": value, "unit": "points/s", "cores": O.num_threads(), "kind": "port",
-        "sample": ("every %d-th polygon (%d of %d, %.2f%% of candidates), full %d-point set; "
-                   "oracle join %.2fs + PiP %.2fs scaled by polygons/candidates" %
-                   (stride, len(sel), npoly, 100.0 * cand_s / max(cand_total, 1), len(w.x),
-                    t1 - t0, t2 - t1)),
-        "sample_pairs": int(len(r["polygon_index"])),
-        "sample_parity_exact": parity,
+        "value": res["value"], "unit": "points/s", "cores": O.num_threads(), "kind": "port",
+        "sample": cpu_sample_text(res, len(w.x)), "sample_s": res["sample_s"],
+        "scale_to_full": res["full_s"] / res["sample_s"],
+        "sample_pairs": int(len(r["polygon_index"])), "sample_parity_exact": parity,
     }
 
 
@@ -282,22 +363,28 @@ def run_ours(args, dist):
     stream = torch.cuda.current_stream()
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
 
-    # quadtree build (reported separately)
-    build_ms = []
+    # point index build (reported separately): the quadtree and the points
+    # in its order, built together; the tree alone for comparison
+    build_ms, tree_ms = [], []
     for _ in range(3):
-        a, b = ev(), ev()
+        a, b, c = ev(), ev(), ev()
         a.record(stream)
-        pi, tree = cs.quadtree_on_points(pts, w.x_min, w.x_max, w.y_min, w.y_max, w.scale,
-                                         w.max_depth, w.max_size)
+        pi, tree, xy = cs.quadtree_on_points_ordered(pts, w.x_min, w.x_max, w.y_min, w.y_max,
+                                                     w.scale, w.max_depth, w.max_size)
         b.record(stream)
-        b.synchronize()
+        cs.quadtree_on_points(pts, w.x_min, w.x_max, w.y_min, w.y_max, w.scale, w.max_depth,
+                              w.max_size)
+        c.record(stream)
+        c.synchronize()
         build_ms.append(a.elapsed_time(b))
+        tree_ms.append(b.elapsed_time(c))
 
     def step(method):
         bb = cs.polygon_bounding_boxes(polys)
         pairs = cs.join_quadtree_and_bounding_boxes(tree, bb, w.x_min, w.x_max, w.y_min,
                                                     w.y_max, w.scale, w.max_depth)
-        res = cs.quadtree_point_in_polygon(pairs, tree, pi, pts, polys, method=method)
+        res = cs.quadtree_point_in_polygon(pairs, tree, pi, pts, polys, method=method,
+                                           ordered_points=xy)
         return pairs, res
 
     for _ in range(args.warmup):
@@ -383,6 +470,24 @@ def run_ours(args, dist):
     # allocated once
     e2e = None
     if args.e2e_steps > 0:
+        # page-locked buffers are first touched by this thread: run it on
+        # the GPU's local CPUs (when sysfs names them) so the pages land on
+        # the GPU's own NUMA node
+        numa = gpu_numa(dist.local)
+        old_aff = None
+        if hasattr(os, "sched_setaffinity") and numa.get("local_cpulist"):
+            cpus = set()
+            for part in numa["local_cpulist"].split(","):
+                lo, _, hi = part.partition("-")
+                if lo.strip():
+                    cpus.update(range(int(lo), int(hi or lo) + 1))
+            try:
+                old_aff = os.sched_getaffinity(0)
+                os.sched_setaffinity(0, cpus & old_aff or old_aff)
+            except (OSError, ValueError):
+                old_aff = None
+        link = measure_link(stream)
+        link["gpu"] = numa
         hx = torch.from_numpy(w.x).pin_memory()
         hy = torch.from_numpy(w.y).pin_memory()
         hpxy = torch.from_numpy(polygons_xy(P)).pin_memory()
@@ -395,6 +500,9 @@ def run_ours(args, dist):
         M0 = int(res["polygon_index"].numel())
         o1 = torch.empty(M0, dtype=torch.int32, pin_memory=True)
         o2 = torch.empty(M0, dtype=torch.int32, pin_memory=True)
+        link["points_pages_by_node"] = pages_by_node(hx.data_ptr(), hx.numel() * 8)
+        if old_aff is not None:
+            os.sched_setaffinity(0, old_aff)
         ems, phases, h2d, d2h = [], [], 0, 0
         for it in range(args.e2e_steps + 1):
             ph = [ev() for _ in range(5)]
@@ -405,16 +513,16 @@ def run_ours(args, dist):
                                                    hgo.to("cuda", non_blocking=True))
             ph[1].record(stream)
             # the points' copy overlaps their Morton keys, chunk by chunk
-            epts, epi, etree = cs.quadtree_on_points_host(hx, hy, w.x_min, w.x_max, w.y_min,
-                                                          w.y_max, w.scale, w.max_depth,
-                                                          w.max_size)
+            epts, epi, etree, exy = cs.quadtree_on_points_host(
+                hx, hy, w.x_min, w.x_max, w.y_min, w.y_max, w.scale, w.max_depth, w.max_size,
+                ordered=True)
             ph[2].record(stream)
             ebb = cs.polygon_bounding_boxes(epolys)
             ej = cs.join_quadtree_and_bounding_boxes(etree, ebb, w.x_min, w.x_max, w.y_min,
                                                      w.y_max, w.scale, w.max_depth)
             ph[3].record(stream)
             m = cs.quadtree_point_in_polygon_host(ej, etree, epi, epts, epolys, o1, o2,
-                                                  method=args.method)
+                                                  method=args.method, ordered_points=exy)
             ph[4].record(stream)
             ph[4].synchronize()
             if it > 0:  # the first pass warms the allocators
@@ -424,10 +532,16 @@ def run_ours(args, dist):
                                                                    hgo.numel()) * 4
             d2h = 2 * m * 4
         e2e_ms = dist.max(statistics.mean(ems))
+        # lower bounds of one e2e step: its copies at the link's measured
+        # rates (the two directions do not overlap each other here), and its
+        # device work (point index build + the step)
+        link["copy_floor_ms"] = 1e3 * (h2d / (link["h2d_gbs"] * 1e9) +
+                                       d2h / (link["d2h_gbs"] * 1e9))
+        link["device_work_ms"] = min(build_ms) + ms_per_step
         e2e = {"value": n * args.gpus / (e2e_ms / 1e3), "unit": "points/s",
                "ms_per_step": e2e_ms, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h),
-               "api": "quadtree_on_points_host, polygon_bounding_boxes, "
+               "d2h_bytes_per_step": int(d2h), "link": link,
+               "api": "quadtree_on_points_host (ordered), polygon_bounding_boxes, "
                       "join_quadtree_and_bounding_boxes, quadtree_point_in_polygon_host",
                "phases_ms": dict(zip(["polygons_h2d", "points_h2d_and_quadtree_build",
                                       "boxes_join", "pip_and_d2h"],
@@ -443,8 +557,7 @@ def run_ours(args, dist):
         tree_np["is_internal_node"] = tree_np["is_internal_node"].astype(bool)
         pairs_np = {k: v.cpu().numpy().view(np.uint32) for k, v in pairs.items()}
         gpu_pip = {k: v.cpu().numpy().view(np.uint32) for k, v in res.items()}
-        cpu = cpu_baseline(w, tree_np, pi.cpu().numpy().view(np.uint32), pairs_np, gpu_pip,
-                           args.cpu_seconds)
+        cpu = cpu_baseline(w, tree_np, pi.cpu().numpy().view(np.uint32), pairs_np, gpu_pip)
 
     line = {
         "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": args.gpus,
@@ -458,12 +571,14 @@ def run_ours(args, dist):
                    "precision_at_scale scaled to %d points / %d polygons" % (n, P.num_polygons),
                    "points": n, "polygons": P.num_polygons, "vertices": V,
                    "method": args.method, "step": "polygon_bounding_boxes + "
-                   "join_quadtree_and_bounding_boxes + quadtree_point_in_polygon",
+                   "join_quadtree_and_bounding_boxes + quadtree_point_in_polygon (points "
+                   "in quadtree order, gathered once with the quadtree build)",
                    "l2": "inputs larger than L2 (%.1f GB of points resident)" % (16 * n / 1e9),
                    "parallelism": "replicas" if args.gpus > 1 else "single GPU"},
         "pairs": K, "candidates": cand, "hits": M,
         "refined_candidates": refined, "refine_fraction": refined / max(cand, 1),
-        "build_ms": min(build_ms), "generation_s": gen_s,
+        "build_ms": min(build_ms), "tree_only_build_ms": min(tree_ms),
+        "generation_s": gen_s,
         "kernels_ms_per_step": {k: v[0] / max(args.steps, 1) for k, v in kern.items()},
         "plain_fp64": plain,
         "speedup_vs_plain": (plain["ms_per_step"] / ms_per_step) if plain else None,
@@ -492,42 +607,34 @@ def run_reference(args, dist):
     bb = O.polygon_bounding_boxes(P.part_offset, P.ring_offset, P.x, P.y)
     npoly = P.num_polygons
     qlen = tree["length"].astype(np.int64)
-    # per step: every stride-th polygon, offset by the step number
-    stride = max(1, npoly // 200)
-    times, cand_frac = [], []
     full = O.join_quadtree_and_bounding_boxes(tree, bb, w.x_min, w.x_max, w.y_min, w.y_max,
                                               w.scale, w.max_depth)
     cand_total = int(qlen[full["quad_offset"]].sum())
+    # per step: the shared sample rule, its offset moving with the step
+    samples = []
     for it in range(args.warmup + args.steps):
-        sel = np.arange(it % stride, npoly, stride)
-        sbb = {k: np.ascontiguousarray(v[sel]) for k, v in bb.items()}
-        t0 = time.perf_counter()
-        sj = O.join_quadtree_and_bounding_boxes(tree, sbb, w.x_min, w.x_max, w.y_min, w.y_max,
-                                                w.scale, w.max_depth)
-        t1 = time.perf_counter()
-        sj = dict(bbox_offset=sel[sj["bbox_offset"]].astype(np.uint32),
-                  quad_offset=sj["quad_offset"])
-        O.quadtree_point_in_polygon(sj, tree, pi, w.x, w.y, P.part_offset, P.ring_offset, P.x,
-                                    P.y)
-        t2 = time.perf_counter()
+        res = cpu_sample(O, w, tree, pi, bb, qlen, cand_total, it)
         if it >= args.warmup:
-            cs_ = int(qlen[sj["quad_offset"]].sum())
-            times.append((t1 - t0) * npoly / len(sel) + (t2 - t1) * cand_total / max(cs_, 1))
-            cand_frac.append(cs_ / max(cand_total, 1))
-    s_per_step = statistics.mean(times)
-    value = n / s_per_step
-    sample = ("per step every %d-th polygon (%.2f%% of candidates), full %d-point set; time "
-              "scaled to the full join" % (stride, 100 * statistics.mean(cand_frac), n))
+            samples.append(res)
+    sample_s = [r["sample_s"] for r in samples]
+    values = [r["value"] for r in samples]
+    value = len(samples) / sum(1.0 / v for v in values)  # points over summed estimated time
+    s_per_step = statistics.mean(sample_s)
+    sample = cpu_sample_text(samples[0], n) + "; ms_per_step is the sampled wall time"
     line = {
         "metric": METRIC, "impl": "reference", "value": value, "unit": "points/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": s_per_step * 1e3, "p50_ms": percentile([t * 1e3 for t in times], 0.5),
-        "p99_ms": percentile([t * 1e3 for t in times], 0.99), "higher_is_better": True,
+        "ms_per_step": s_per_step * 1e3, "p50_ms": percentile([t * 1e3 for t in sample_s], 0.5),
+        "p99_ms": percentile([t * 1e3 for t in sample_s], 0.99), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "precision_at_scale", "points": n, "polygons": npoly,
                    "method": "reference crossing test (CPU oracle port)"},
         "cpu_baseline": {"value": value, "unit": "points/s", "cores": O.num_threads(),
-                         "kind": "port", "sample": sample},
+                         "kind": "port", "sample": sample,
+                         "scale_to_full": statistics.mean(r["full_s"] / r["sample_s"]
+                                                          for r in samples),
+                         "value_spread": {"min": min(values), "max": max(values),
+                                          "stdev": statistics.pstdev(values)}},
         "e2e": {"value": value, "unit": "points/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "build_s": build_s,
@@ -853,6 +960,7 @@ def run_nearest(args, dist):
     a.record(stream)
     pi, tree = cs.quadtree_on_points(pts, w.x_min, w.x_max, w.y_min, w.y_max, w.scale,
                                      w.max_depth, w.max_size)
+    oxy = cs.points_in_quadtree_order(pi, pts)
     b.record(stream)
     b.synchronize()
     build_ms = a.elapsed_time(b)
@@ -862,7 +970,8 @@ def run_nearest(args, dist):
         pairs = cs.join_quadtree_and_bounding_boxes(tree, bb, w.x_min, w.x_max, w.y_min,
                                                     w.y_max, w.scale, w.max_depth)
         return pairs, cs.quadtree_point_to_nearest_linestring(pairs, tree, pi, pts, lines,
-                                                              method="filtered")
+                                                              method="filtered",
+                                                              ordered_points=oxy)
 
     for _ in range(args.warmup):
         pairs, res = step()
@@ -882,6 +991,7 @@ def run_nearest(args, dist):
     clock_info = clocks.stop()
     ms = [x.elapsed_time(y) for x, y in times]
     f_ms = dist.max(statistics.mean(ms))
+    paths = cs.last_nearest_stats()
 
     # plain float64 on every 64th leaf's pairs
     pq = pairs["quad_offset"].long()
@@ -902,6 +1012,29 @@ def run_nearest(args, dist):
                 torch.equal(fi["distance"], ex["distance"]) and
                 torch.equal(fi["point_index"], ex["point_index"]))
     plain_ms = sub_ms * cand_all / max(cand_sub, 1)
+
+    # the oracle on the pairs of every 4096th leaf (rows of those leaves' points)
+    oracle_check = None
+    if dist.rank == 0 and not args.no_cpu:
+        from oracle import oracle as O
+        osel = (pq % 4096) == 0
+        osub = {"bbox_offset": pairs["bbox_offset"][osel].cpu().numpy().view(np.uint32),
+                "quad_offset": pairs["quad_offset"][osel].cpu().numpy().view(np.uint32)}
+        tree_np = {k: (v.cpu().numpy().view(np.uint32) if v.dtype == torch.int32 else
+                       v.cpu().numpy()) for k, v in tree.items()}
+        tree_np["is_internal_node"] = tree_np["is_internal_node"].astype(bool)
+        t0 = time.perf_counter()
+        orr = O.quadtree_point_to_nearest_linestring(osub, tree_np, pi.cpu().numpy().view(
+            np.uint32), w.x, w.y, L.part_offset, L.x, L.y)
+        o_s = time.perf_counter() - t0
+        rows = orr["linestring_index"] != 0xFFFFFFFF
+        g_ls = res["linestring_index"].cpu().numpy().view(np.uint32)
+        g_d = res["distance"].cpu().numpy()
+        oracle_check = {"leaves": "every 4096th", "rows": int(rows.sum()),
+                        "oracle_s": o_s, "cores": O.num_threads(),
+                        "rows_identical": bool(np.array_equal(g_ls[rows],
+                                                              orr["linestring_index"][rows]) and
+                                               np.array_equal(g_d[rows], orr["distance"][rows]))}
     line = {
         "metric": METRIC, "workload": "nearest", "value": n * args.gpus / (f_ms / 1e3),
         "unit": "points/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -921,7 +1054,7 @@ def run_nearest(args, dist):
                                "ms_per_step_scaled": plain_ms,
                                "rows_identical_to_filtered": same},
         "speedup_vs_plain": plain_ms / f_ms, "gpu_launches": launches, "clocks": clock_info,
-        "generation_s": gen_s,
+        "generation_s": gen_s, "paths": paths, "oracle_sample": oracle_check,
     }
     if dist.rank == 0:
         print(json.dumps(line), flush=True)

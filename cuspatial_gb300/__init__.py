@@ -8,11 +8,13 @@ the pairwise point-linestring distance and nearest points;
 they run hand-written CUDA kernels in libcuspatial_gb300.so through its C ABI.
 """
 
-from .api import (HostRowsTooFew, join_quadtree_and_bounding_boxes, last_refined_count,
+from .api import (HostRowsTooFew, join_quadtree_and_bounding_boxes, last_nearest_stats,
+                  last_refined_count,
                   linestring_bounding_boxes, pairwise_point_in_polygon,
                   pairwise_point_linestring_distance, pairwise_point_linestring_nearest_points,
-                  point_in_polygon, point_in_polygon_bitmask, polygon_bounding_boxes,
-                  quadtree_on_points, quadtree_on_points_host, quadtree_point_in_polygon,
+                  point_in_polygon, point_in_polygon_bitmask, points_in_quadtree_order,
+                  polygon_bounding_boxes, quadtree_on_points, quadtree_on_points_host, quadtree_on_points_ordered,
+                  quadtree_point_in_polygon,
                   quadtree_point_in_polygon_host, quadtree_point_to_nearest_linestring)
 from .contains import contains_properly, polygons_contains_properly
 from .geoseries import GeoSeries, Table
@@ -23,6 +25,7 @@ __all__ = [
     "Table",
     "contains_properly",
     "join_quadtree_and_bounding_boxes",
+    "last_nearest_stats",
     "last_refined_count",
     "linestring_bounding_boxes",
     "pairwise_point_in_polygon",
@@ -30,10 +33,12 @@ __all__ = [
     "pairwise_point_linestring_nearest_points",
     "point_in_polygon",
     "point_in_polygon_bitmask",
+    "points_in_quadtree_order",
     "polygon_bounding_boxes",
     "polygons_contains_properly",
     "quadtree_on_points",
     "quadtree_on_points_host",
+    "quadtree_on_points_ordered",
     "quadtree_point_in_polygon",
     "quadtree_point_in_polygon_host",
     "quadtree_point_to_nearest_linestring",

@@ -85,6 +85,9 @@ def _declare(lib):
     lib.cspt_last_error_message.restype = ctypes.c_char_p
     lib.cspt_version.restype = ctypes.c_char_p
     lib.cspt_last_refined_count.restype = ctypes.c_uint64
+    lib.cspt_last_nearest_stats.argtypes = [ctypes.POINTER(ctypes.c_uint64),
+                                            ctypes.POINTER(ctypes.c_uint64)]
+    lib.cspt_last_nearest_stats.restype = None
     lib.cspt_free.argtypes = [ctypes.POINTER(CsptAllocator), _vp, _sz, _vp]
     lib.cspt_quadtree_free.argtypes = [ctypes.POINTER(CsptAllocator),
                                        ctypes.POINTER(CsptQuadtree), _vp]
@@ -116,6 +119,24 @@ def _declare(lib):
     lib.cspt_quadtree_point_to_nearest_linestring.argtypes = [
         _vp, _vp, _sz, ctypes.POINTER(CsptQuadtree), _vp, _sz, _vp, _vp, _sz, _vp, _sz, _vp, _vp,
         _sz, ctypes.c_int, ctypes.c_int, ctypes.POINTER(CsptAllocator), _vp, _vp, _vp, _vp,
+        ctypes.POINTER(_sz)]
+    lib.cspt_quadtree_on_points_ordered.argtypes = (lib.cspt_quadtree_on_points.argtypes +
+                                                    [_vp])
+    lib.cspt_quadtree_on_points_host_ordered.argtypes = (
+        lib.cspt_quadtree_on_points_host.argtypes + [_vp])
+    lib.cspt_points_in_quadtree_order.argtypes = [_vp, _sz, _vp, _vp, _sz, ctypes.c_int, _vp,
+                                                  _vp]
+    lib.cspt_quadtree_point_in_polygon_ordered.argtypes = [
+        _vp, _vp, _sz, ctypes.POINTER(CsptQuadtree), _vp, _sz, _vp, _sz, _vp, _sz, _vp, _vp, _sz,
+        ctypes.c_int, ctypes.c_int, ctypes.POINTER(CsptAllocator), _vp, ctypes.POINTER(_vp),
+        ctypes.POINTER(_vp), ctypes.POINTER(_sz)]
+    lib.cspt_quadtree_point_in_polygon_host_ordered.argtypes = [
+        _vp, _vp, _sz, ctypes.POINTER(CsptQuadtree), _vp, _sz, _vp, _sz, _vp, _sz, _vp, _vp, _sz,
+        ctypes.c_int, ctypes.c_int, ctypes.POINTER(CsptAllocator), _vp, _vp, _vp, _sz,
+        ctypes.POINTER(_sz)]
+    lib.cspt_quadtree_point_to_nearest_linestring_ordered.argtypes = [
+        _vp, _vp, _sz, ctypes.POINTER(CsptQuadtree), _vp, _sz, _vp, _sz, _vp, _vp, _sz,
+        ctypes.c_int, ctypes.c_int, ctypes.POINTER(CsptAllocator), _vp, _vp, _vp, _vp,
         ctypes.POINTER(_sz)]
     for name in ("cspt_point_in_polygon", "cspt_pairwise_point_in_polygon"):
         getattr(lib, name).argtypes = [

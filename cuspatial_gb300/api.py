@@ -52,6 +52,25 @@ def quadtree_on_points(points: GeoSeries, x_min, x_max, y_min, y_max, scale, max
     input point indices; quadtree holds key, level, is_internal_node, length
     and offset.  uint32 columns are returned in int32 tensors (same bits).
     """
+    return _quadtree_on_points(points, x_min, x_max, y_min, y_max, scale, max_depth, max_size,
+                               False)
+
+
+def quadtree_on_points_ordered(points: GeoSeries, x_min, x_max, y_min, y_max, scale, max_depth,
+                               max_size):
+    """quadtree_on_points that also returns the points in quadtree order.
+
+    Returns (point_indices, quadtree, ordered_points); ordered_points equals
+    points_in_quadtree_order(point_indices, points) and is built in the same
+    pass (the key computation writes the points interleaved, the gather after
+    the sort reads one row per point).  No counterpart in the reference.
+    """
+    return _quadtree_on_points(points, x_min, x_max, y_min, y_max, scale, max_depth, max_size,
+                               True)
+
+
+def _quadtree_on_points(points, x_min, x_max, y_min, y_max, scale, max_depth, max_size,
+                        ordered):
     if not len(points) == 0 and not contains_only_points(points):
         raise ValueError("GeoSeries must contain only points.")
     lib = _lib.load()
@@ -66,11 +85,16 @@ def quadtree_on_points(points: GeoSeries, x_min, x_max, y_min, y_max, scale, max
     alloc = _lib.TorchAllocator(xs.device)
     pi = ctypes.c_void_p()
     tree = _lib.CsptQuadtree()
-    _lib.check(lib.cspt_quadtree_on_points(
-        _lib.ptr(xs), _lib.ptr(ys), int(xs.numel()), _dtype_code(xs), float(x_min), float(x_max),
-        float(y_min), float(y_max), float(max(scale, min_scale)), int(max_depth), int(max_size),
-        alloc.ref, _lib.stream_ptr(), ctypes.byref(pi), ctypes.byref(tree)), lib)
-    return _adopt_tree(alloc, pi, tree, int(xs.numel()))
+    args = [_lib.ptr(xs), _lib.ptr(ys), int(xs.numel()), _dtype_code(xs), float(x_min),
+            float(x_max), float(y_min), float(y_max), float(max(scale, min_scale)),
+            int(max_depth), int(max_size), alloc.ref, _lib.stream_ptr(), ctypes.byref(pi),
+            ctypes.byref(tree)]
+    if not ordered:
+        _lib.check(lib.cspt_quadtree_on_points(*args), lib)
+        return _adopt_tree(alloc, pi, tree, int(xs.numel()))
+    oxy = torch.empty((int(xs.numel()), 2), dtype=xs.dtype, device=xs.device)
+    _lib.check(lib.cspt_quadtree_on_points_ordered(*args, _lib.ptr(oxy)), lib)
+    return (*_adopt_tree(alloc, pi, tree, int(xs.numel())), oxy)
 
 
 def _adopt_tree(alloc, pi, tree, n):
@@ -85,13 +109,16 @@ def _adopt_tree(alloc, pi, tree, n):
     return point_indices, qt
 
 
-def quadtree_on_points_host(x, y, x_min, x_max, y_min, y_max, scale, max_depth, max_size):
+def quadtree_on_points_host(x, y, x_min, x_max, y_min, y_max, scale, max_depth, max_size,
+                            ordered=False):
     """quadtree_on_points for points in host memory.
 
     x and y are CPU tensors of one floating type (page-locked, for the copy to
     the device to overlap the Morton keys of the chunks already copied).
     Returns (points, point_indices, quadtree): points is a GeoSeries over the
-    device copies of x and y, for the calls that follow.
+    device copies of x and y, for the calls that follow.  ordered=True also
+    returns the points in quadtree order, as quadtree_on_points_ordered does:
+    (points, point_indices, quadtree, ordered_points).
     """
     for t in (x, y):
         if t.device.type != "cpu" or not t.is_contiguous():
@@ -112,13 +139,19 @@ def quadtree_on_points_host(x, y, x_min, x_max, y_min, y_max, scale, max_depth, 
     alloc = _lib.TorchAllocator(dx.device)
     pi = ctypes.c_void_p()
     tree = _lib.CsptQuadtree()
-    _lib.check(lib.cspt_quadtree_on_points_host(
-        x.data_ptr() if x.numel() else None, y.data_ptr() if y.numel() else None,
-        int(x.numel()), _dtype_code(x), float(x_min), float(x_max), float(y_min), float(y_max),
-        float(max(scale, min_scale)), int(max_depth), int(max_size), _lib.ptr(dx), _lib.ptr(dy),
-        alloc.ref, _lib.stream_ptr(), ctypes.byref(pi), ctypes.byref(tree)), lib)
+    args = [x.data_ptr() if x.numel() else None, y.data_ptr() if y.numel() else None,
+            int(x.numel()), _dtype_code(x), float(x_min), float(x_max), float(y_min),
+            float(y_max), float(max(scale, min_scale)), int(max_depth), int(max_size),
+            _lib.ptr(dx), _lib.ptr(dy), alloc.ref, _lib.stream_ptr(), ctypes.byref(pi),
+            ctypes.byref(tree)]
+    if not ordered:
+        _lib.check(lib.cspt_quadtree_on_points_host(*args), lib)
+        point_indices, qt = _adopt_tree(alloc, pi, tree, int(x.numel()))
+        return GeoSeries.from_points(dx, dy), point_indices, qt
+    oxy = torch.empty((int(x.numel()), 2), dtype=x.dtype, device="cuda")
+    _lib.check(lib.cspt_quadtree_on_points_host_ordered(*args, _lib.ptr(oxy)), lib)
     point_indices, qt = _adopt_tree(alloc, pi, tree, int(x.numel()))
-    return GeoSeries.from_points(dx, dy), point_indices, qt
+    return GeoSeries.from_points(dx, dy), point_indices, qt, oxy
 
 
 def _empty_boxes(dtype):
@@ -195,13 +228,48 @@ def join_quadtree_and_bounding_boxes(quadtree, bounding_boxes, x_min, x_max, y_m
     return out
 
 
+def points_in_quadtree_order(point_indices, points: GeoSeries):
+    """The points gathered into quadtree order: an (n, 2) tensor whose row i
+    is (x, y) of point point_indices[i].
+
+    No counterpart in the reference.  quadtree_point_in_polygon and
+    quadtree_point_to_nearest_linestring take it as `ordered_points`, and then
+    read each quadrant's points contiguously instead of through point_indices
+    on every call; build it once per quadtree.
+    """
+    if not contains_only_points(points):
+        raise ValueError("`point` Geoseries must contains only point geometries.")
+    lib = _lib.load()
+    pi = as_device_tensor(point_indices, dtype=torch.int32)
+    pts = points.points
+    out = torch.empty((int(pi.numel()), 2), dtype=pts.x.dtype, device=pts.x.device)
+    _lib.check(lib.cspt_points_in_quadtree_order(
+        _lib.ptr(pi), int(pi.numel()), _lib.ptr(pts.x), _lib.ptr(pts.y), int(pts.x.numel()),
+        _dtype_code(pts.x), _lib.ptr(out), _lib.stream_ptr()), lib)
+    return out
+
+
+def _check_ordered(ordered_points, point_indices, points):
+    """ordered_points must be points_in_quadtree_order(point_indices, points)."""
+    t = ordered_points
+    if not isinstance(t, torch.Tensor) or t.dim() != 2 or t.shape[1] != 2 or \
+            not t.is_contiguous() or t.device.type != "cuda":
+        raise ValueError("ordered_points must be the contiguous (n, 2) CUDA tensor that "
+                         "points_in_quadtree_order returns")
+    if int(t.shape[0]) != int(point_indices.numel()) or t.dtype != points.points.x.dtype:
+        raise ValueError("ordered_points must hold one row per point index, in the points' "
+                         "dtype")
+
+
 def quadtree_point_in_polygon(poly_quad_pairs, quadtree, point_indices, points: GeoSeries,
-                              polygons: GeoSeries, method="exact"):
+                              polygons: GeoSeries, method="exact", ordered_points=None):
     """Points inside polygons, using (polygon, quadrant) pairs (join.py:177).
 
     point_index in the result is a position in point_indices (an index to an
     index), as in the reference.  method="filtered" runs the float32 filter
     with float64 refinement; the pairs are identical to method="exact".
+    ordered_points (optional): points_in_quadtree_order(point_indices, points);
+    the result is the same, the points are read in order.
     """
     if not contains_only_points(points):
         raise ValueError("`point` Geoseries must contains only point geometries.")
@@ -217,13 +285,24 @@ def quadtree_point_in_polygon(poly_quad_pairs, quadtree, point_indices, points: 
     poly = polygons.polygons
     alloc = _lib.TorchAllocator(pts.x.device)
     op, oq, nn = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_size_t()
-    _lib.check(lib.cspt_quadtree_point_in_polygon(
-        _lib.ptr(pp), _lib.ptr(pq), int(pp.numel()), ctypes.byref(st), _lib.ptr(pi),
-        int(pi.numel()), _lib.ptr(pts.x), _lib.ptr(pts.y), int(pts.x.numel()),
-        _lib.ptr(poly.part_offset), int(poly.part_offset.numel()), _lib.ptr(poly.ring_offset),
-        int(poly.ring_offset.numel()), _lib.ptr(poly.x), _lib.ptr(poly.y), int(poly.x.numel()),
-        _dtype_code(pts.x), _METHODS[method], alloc.ref, _lib.stream_ptr(), ctypes.byref(op),
-        ctypes.byref(oq), ctypes.byref(nn)), lib)
+    if ordered_points is not None:
+        _check_ordered(ordered_points, pi, points)
+        _lib.check(lib.cspt_quadtree_point_in_polygon_ordered(
+            _lib.ptr(pp), _lib.ptr(pq), int(pp.numel()), ctypes.byref(st),
+            _lib.ptr(ordered_points), int(pi.numel()), _lib.ptr(poly.part_offset),
+            int(poly.part_offset.numel()), _lib.ptr(poly.ring_offset),
+            int(poly.ring_offset.numel()), _lib.ptr(poly.x), _lib.ptr(poly.y),
+            int(poly.x.numel()), _dtype_code(pts.x), _METHODS[method], alloc.ref,
+            _lib.stream_ptr(), ctypes.byref(op), ctypes.byref(oq), ctypes.byref(nn)), lib)
+    else:
+        _lib.check(lib.cspt_quadtree_point_in_polygon(
+            _lib.ptr(pp), _lib.ptr(pq), int(pp.numel()), ctypes.byref(st), _lib.ptr(pi),
+            int(pi.numel()), _lib.ptr(pts.x), _lib.ptr(pts.y), int(pts.x.numel()),
+            _lib.ptr(poly.part_offset), int(poly.part_offset.numel()),
+            _lib.ptr(poly.ring_offset), int(poly.ring_offset.numel()), _lib.ptr(poly.x),
+            _lib.ptr(poly.y), int(poly.x.numel()), _dtype_code(pts.x), _METHODS[method],
+            alloc.ref, _lib.stream_ptr(), ctypes.byref(op), ctypes.byref(oq),
+            ctypes.byref(nn)), lib)
     del keep
     n = int(nn.value)
     out = Table()
@@ -243,14 +322,15 @@ class HostRowsTooFew(RuntimeError):
 
 def quadtree_point_in_polygon_host(poly_quad_pairs, quadtree, point_indices, points: GeoSeries,
                                    polygons: GeoSeries, polygon_index_out, point_index_out,
-                                   method="exact"):
+                                   method="exact", ordered_points=None):
     """quadtree_point_in_polygon with the rows written into host tensors.
 
     polygon_index_out and point_index_out are int32 CPU tensors of equal
     length (page-locked, for the device-to-host copies to overlap the
     evaluation, which runs in chunks of pairs).  Returns the number of rows
     written, in the order of quadtree_point_in_polygon.  Raises HostRowsTooFew
-    (with the row count) when the tensors are too short.
+    (with the row count) when the tensors are too short.  ordered_points as in
+    quadtree_point_in_polygon.
     """
     if not contains_only_points(points):
         raise ValueError("`point` Geoseries must contains only point geometries.")
@@ -270,14 +350,25 @@ def quadtree_point_in_polygon_host(poly_quad_pairs, quadtree, point_indices, poi
     poly = polygons.polygons
     alloc = _lib.TorchAllocator(pts.x.device)
     nn = ctypes.c_size_t()
-    status = lib.cspt_quadtree_point_in_polygon_host(
-        _lib.ptr(pp), _lib.ptr(pq), int(pp.numel()), ctypes.byref(st), _lib.ptr(pi),
-        int(pi.numel()), _lib.ptr(pts.x), _lib.ptr(pts.y), int(pts.x.numel()),
-        _lib.ptr(poly.part_offset), int(poly.part_offset.numel()), _lib.ptr(poly.ring_offset),
-        int(poly.ring_offset.numel()), _lib.ptr(poly.x), _lib.ptr(poly.y), int(poly.x.numel()),
-        _dtype_code(pts.x), _METHODS[method], alloc.ref, _lib.stream_ptr(),
-        polygon_index_out.data_ptr() if cap else None, point_index_out.data_ptr() if cap else None,
-        cap, ctypes.byref(nn))
+    host_p = polygon_index_out.data_ptr() if cap else None
+    host_q = point_index_out.data_ptr() if cap else None
+    if ordered_points is not None:
+        _check_ordered(ordered_points, pi, points)
+        status = lib.cspt_quadtree_point_in_polygon_host_ordered(
+            _lib.ptr(pp), _lib.ptr(pq), int(pp.numel()), ctypes.byref(st),
+            _lib.ptr(ordered_points), int(pi.numel()), _lib.ptr(poly.part_offset),
+            int(poly.part_offset.numel()), _lib.ptr(poly.ring_offset),
+            int(poly.ring_offset.numel()), _lib.ptr(poly.x), _lib.ptr(poly.y),
+            int(poly.x.numel()), _dtype_code(pts.x), _METHODS[method], alloc.ref,
+            _lib.stream_ptr(), host_p, host_q, cap, ctypes.byref(nn))
+    else:
+        status = lib.cspt_quadtree_point_in_polygon_host(
+            _lib.ptr(pp), _lib.ptr(pq), int(pp.numel()), ctypes.byref(st), _lib.ptr(pi),
+            int(pi.numel()), _lib.ptr(pts.x), _lib.ptr(pts.y), int(pts.x.numel()),
+            _lib.ptr(poly.part_offset), int(poly.part_offset.numel()),
+            _lib.ptr(poly.ring_offset), int(poly.ring_offset.numel()), _lib.ptr(poly.x),
+            _lib.ptr(poly.y), int(poly.x.numel()), _dtype_code(pts.x), _METHODS[method],
+            alloc.ref, _lib.stream_ptr(), host_p, host_q, cap, ctypes.byref(nn))
     del keep
     if status != _lib.OK and int(nn.value) > cap:
         raise HostRowsTooFew(lib.cspt_last_error_message().decode(), int(nn.value))
@@ -287,8 +378,12 @@ def quadtree_point_in_polygon_host(poly_quad_pairs, quadtree, point_indices, poi
 
 def quadtree_point_to_nearest_linestring(linestring_quad_pairs, quadtree, point_indices,
                                          points: GeoSeries, linestrings: GeoSeries,
-                                         method="exact"):
-    """Nearest linestring of each point in the paired quadrants (join.py:265)."""
+                                         method="exact", ordered_points=None):
+    """Nearest linestring of each point in the paired quadrants (join.py:265).
+
+    ordered_points (optional): points_in_quadtree_order(point_indices, points);
+    the rows are the same, the points are read in order.
+    """
     if not contains_only_points(points):
         raise ValueError("`point` Geoseries must contains only point geometries.")
     if not contains_only_linestrings(linestrings):
@@ -310,12 +405,21 @@ def quadtree_point_to_nearest_linestring(linestring_quad_pairs, quadtree, point_
     o_d = torch.empty(n, dtype=pts.x.dtype, device=pts.x.device)
     alloc = _lib.TorchAllocator(pts.x.device)
     rows = ctypes.c_size_t()
-    _lib.check(lib.cspt_quadtree_point_to_nearest_linestring(
-        _lib.ptr(pl), _lib.ptr(pq), int(pl.numel()), ctypes.byref(st), _lib.ptr(pi), n,
-        _lib.ptr(pts.x), _lib.ptr(pts.y), int(pts.x.numel()), _lib.ptr(ls.part_offset),
-        int(ls.part_offset.numel()), _lib.ptr(ls.x), _lib.ptr(ls.y), int(ls.x.numel()),
-        _dtype_code(pts.x), _METHODS[method], alloc.ref, _lib.stream_ptr(), _lib.ptr(o_pt),
-        _lib.ptr(o_ls), _lib.ptr(o_d), ctypes.byref(rows)), lib)
+    if ordered_points is not None:
+        _check_ordered(ordered_points, pi, points)
+        _lib.check(lib.cspt_quadtree_point_to_nearest_linestring_ordered(
+            _lib.ptr(pl), _lib.ptr(pq), int(pl.numel()), ctypes.byref(st),
+            _lib.ptr(ordered_points), n, _lib.ptr(ls.part_offset), int(ls.part_offset.numel()),
+            _lib.ptr(ls.x), _lib.ptr(ls.y), int(ls.x.numel()), _dtype_code(pts.x),
+            _METHODS[method], alloc.ref, _lib.stream_ptr(), _lib.ptr(o_pt), _lib.ptr(o_ls),
+            _lib.ptr(o_d), ctypes.byref(rows)), lib)
+    else:
+        _lib.check(lib.cspt_quadtree_point_to_nearest_linestring(
+            _lib.ptr(pl), _lib.ptr(pq), int(pl.numel()), ctypes.byref(st), _lib.ptr(pi), n,
+            _lib.ptr(pts.x), _lib.ptr(pts.y), int(pts.x.numel()), _lib.ptr(ls.part_offset),
+            int(ls.part_offset.numel()), _lib.ptr(ls.x), _lib.ptr(ls.y), int(ls.x.numel()),
+            _dtype_code(pts.x), _METHODS[method], alloc.ref, _lib.stream_ptr(), _lib.ptr(o_pt),
+            _lib.ptr(o_ls), _lib.ptr(o_d), ctypes.byref(rows)), lib)
     del keep
     r = int(rows.value)
     out = Table()
@@ -457,3 +561,13 @@ def pairwise_point_linestring_nearest_points(points: GeoSeries, linestrings: Geo
 def last_refined_count():
     """Candidates re-evaluated in float64 by the last filtered PiP call."""
     return int(_lib.load().cspt_last_refined_count())
+
+
+def last_nearest_stats():
+    """Paths of the last filtered float64 nearest-linestring call on this
+    thread: {"points_folded_whole": points folded over every candidate in
+    float64, "groups_scanned": quadrant groups scanned point by point instead
+    of through their segment list}."""
+    a, b = ctypes.c_uint64(), ctypes.c_uint64()
+    _lib.load().cspt_last_nearest_stats(ctypes.byref(a), ctypes.byref(b))
+    return {"points_folded_whole": int(a.value), "groups_scanned": int(b.value)}

@@ -122,6 +122,7 @@ void run(uint32_t const* goff, size_t ngeom, uint32_t const* via, T const* x, T 
 {
   cudaStream_t const s = alloc.stream();
   if (ngeom == 0) return;
+  KernelTimer timer("bounding_boxes", s);
   Buffer<uint32_t> row(alloc, ngeom);
   Buffer<uint32_t> nonempty(alloc, 1);
   uint32_t* rw = row.data();

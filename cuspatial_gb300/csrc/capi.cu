@@ -5,6 +5,8 @@
 #include <mutex>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "common.cuh"
 
 namespace cspt {
@@ -13,12 +15,18 @@ namespace cspt {
 void quadtree_on_points(void const* x, void const* y, size_t n, cspt_dtype dtype, double x_min,
                         double x_max, double y_min, double y_max, double scale, int max_depth,
                         int32_t max_size, Allocator const& alloc, uint32_t** out_point_indices,
-                        cspt_quadtree* out_tree);
+                        cspt_quadtree* out_tree, void* ordered = nullptr);
 void quadtree_on_points_from_host(void const* host_x, void const* host_y, void* dev_x,
                                   void* dev_y, size_t n, cspt_dtype dtype, double x_min,
                                   double x_max, double y_min, double y_max, double scale,
                                   int max_depth, int32_t max_size, Allocator const& alloc,
-                                  uint32_t** out_point_indices, cspt_quadtree* out_tree);
+                                  uint32_t** out_point_indices, cspt_quadtree* out_tree,
+                                  void* ordered = nullptr);
+uint64_t& last_fallbacks();
+uint64_t& last_group_scans();
+void points_in_quadtree_order(uint32_t const* point_indices, size_t n, void const* x,
+                              void const* y, size_t npts, cspt_dtype dtype, void* out_xy,
+                              cudaStream_t s);
 void polygon_bounding_boxes(uint32_t const* poly_offsets, size_t npo,
                             uint32_t const* ring_offsets, size_t nro, void const* x,
                             void const* y, size_t nv, cspt_dtype dtype, double r, void* ominx,
@@ -38,7 +46,8 @@ void quadtree_point_in_polygon(uint32_t const* pair_poly, uint32_t const* pair_q
                                size_t nro, void const* vx, void const* vy, size_t nv,
                                cspt_dtype dtype, cspt_method method, Allocator const& alloc,
                                uint32_t** out_poly, uint32_t** out_point, size_t* out_n,
-                               uint64_t* out_refined, HostRows const* host = nullptr);
+                               uint64_t* out_refined, HostRows const* host = nullptr,
+                               void const* ordered = nullptr);
 void quadtree_point_to_nearest_linestring(uint32_t const* pair_ls, uint32_t const* pair_quad,
                                           size_t npairs, cspt_quadtree const* tree,
                                           uint32_t const* point_indices, size_t npi,
@@ -46,7 +55,7 @@ void quadtree_point_to_nearest_linestring(uint32_t const* pair_ls, uint32_t cons
                                           size_t nlso, void const* lx, void const* ly,
                                           cspt_dtype dtype, cspt_method method,
                                           Allocator const& alloc, uint32_t* opt, uint32_t* ols,
-                                          void* od);
+                                          void* od, void const* ordered = nullptr);
 void point_in_polygon(void const* x, void const* y, size_t n, uint32_t const* po, size_t npo,
                       uint32_t const* ro, size_t nro, void const* vx, void const* vy, size_t nv,
                       cspt_dtype dtype, cspt_method method, Allocator const& alloc, int32_t* out,
@@ -198,8 +207,13 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 void uncount_launches(uint64_t n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
 
+// Each named stage is also an NVTX range (key, sort, tree, boxes, join
+// traversal, index, frames, pip, expansion, nearest, ...), so a profiler's
+// timeline shows the library's stages; without a profiler attached the
+// range calls return at once.
 KernelTimer::KernelTimer(char const* name, cudaStream_t stream) : name_(name), stream_(stream)
 {
+  nvtxRangePushA(name);
   if (!g_profile.load(std::memory_order_relaxed)) return;
   if (cudaEventCreate(&start_) != cudaSuccess || cudaEventCreate(&stop_) != cudaSuccess) {
     (void)cudaGetLastError();
@@ -211,6 +225,7 @@ KernelTimer::KernelTimer(char const* name, cudaStream_t stream) : name_(name), s
 
 KernelTimer::~KernelTimer()
 {
+  nvtxRangePop();
   if (!start_) return;
   cudaEventRecord(stop_, stream_);
   std::lock_guard<std::mutex> lk(g_prof_mu);
@@ -258,6 +273,12 @@ int cspt_profile_read(const char* name, double* total_ms, uint64_t* launches)
 // Candidates re-evaluated in float64 by the last filtered point-in-polygon
 // call on this thread (diagnostic; not part of the reference interface).
 uint64_t cspt_last_refined_count(void) { return t_last_refined; }
+
+void cspt_last_nearest_stats(uint64_t* points_folded_whole, uint64_t* groups_scanned)
+{
+  if (points_folded_whole) *points_folded_whole = last_fallbacks();
+  if (groups_scanned) *groups_scanned = last_group_scans();
+}
 
 void cspt_free(const cspt_allocator* mr, void* ptr, size_t bytes, void* stream)
 {
@@ -315,6 +336,74 @@ cspt_status cspt_quadtree_on_points_host(const void* host_x, const void* host_y,
     quadtree_on_points_from_host(host_x, host_y, device_x, device_y, num_points, dtype, x_min,
                                  x_max, y_min, y_max, scale, max_depth, max_size, alloc,
                                  out_point_indices, out_tree);
+  });
+}
+
+cspt_status cspt_quadtree_on_points_ordered(const void* x, const void* y, size_t num_points,
+                                            cspt_dtype dtype, double x_min, double x_max,
+                                            double y_min, double y_max, double scale,
+                                            int8_t max_depth, int32_t max_size,
+                                            const cspt_allocator* mr, void* stream,
+                                            uint32_t** out_point_indices,
+                                            cspt_quadtree* out_tree, void* out_ordered_xy)
+{
+  return guarded([&] {
+    CSPT_EXPECTS(out_point_indices && out_tree, "output pointers must not be null");
+    *out_point_indices = nullptr;
+    *out_tree          = cspt_quadtree{nullptr, nullptr, nullptr, nullptr, nullptr, 0};
+    check_dtype(dtype);
+    if (num_points == 0) return;  // point_quadtree.cu:167-177
+    CSPT_EXPECTS(x && y, "x and y columns must have the same length");
+    size_t const vec = dtype == CSPT_FLOAT64 ? 16 : 8;
+    CSPT_EXPECTS(out_ordered_xy && reinterpret_cast<uintptr_t>(out_ordered_xy) % vec == 0,
+                 "the ordered points must start on a " + std::to_string(vec) +
+                   "-byte boundary");
+    Allocator alloc(mr, as_stream(stream));
+    quadtree_on_points(x, y, num_points, dtype, x_min, x_max, y_min, y_max, scale, max_depth,
+                       max_size, alloc, out_point_indices, out_tree, out_ordered_xy);
+  });
+}
+
+cspt_status cspt_quadtree_on_points_host_ordered(
+  const void* host_x, const void* host_y, size_t num_points, cspt_dtype dtype, double x_min,
+  double x_max, double y_min, double y_max, double scale, int8_t max_depth, int32_t max_size,
+  void* device_x, void* device_y, const cspt_allocator* mr, void* stream,
+  uint32_t** out_point_indices, cspt_quadtree* out_tree, void* out_ordered_xy)
+{
+  return guarded([&] {
+    CSPT_EXPECTS(out_point_indices && out_tree, "output pointers must not be null");
+    *out_point_indices = nullptr;
+    *out_tree          = cspt_quadtree{nullptr, nullptr, nullptr, nullptr, nullptr, 0};
+    check_dtype(dtype);
+    if (num_points == 0) return;  // point_quadtree.cu:167-177
+    CSPT_EXPECTS(host_x && host_y && device_x && device_y,
+                 "x and y columns must have the same length");
+    size_t const vec = dtype == CSPT_FLOAT64 ? 16 : 8;
+    CSPT_EXPECTS(out_ordered_xy && reinterpret_cast<uintptr_t>(out_ordered_xy) % vec == 0,
+                 "the ordered points must start on a " + std::to_string(vec) +
+                   "-byte boundary");
+    Allocator alloc(mr, as_stream(stream));
+    quadtree_on_points_from_host(host_x, host_y, device_x, device_y, num_points, dtype, x_min,
+                                 x_max, y_min, y_max, scale, max_depth, max_size, alloc,
+                                 out_point_indices, out_tree, out_ordered_xy);
+  });
+}
+
+cspt_status cspt_points_in_quadtree_order(const uint32_t* point_indices,
+                                          size_t num_point_indices, const void* x, const void* y,
+                                          size_t num_points, cspt_dtype dtype, void* out_xy,
+                                          void* stream)
+{
+  return guarded([&] {
+    check_dtype(dtype);
+    if (num_point_indices == 0) return;
+    CSPT_EXPECTS(point_indices && x && y && out_xy, "input and output arrays must not be null");
+    size_t const vec = dtype == CSPT_FLOAT64 ? 16 : 8;
+    CSPT_EXPECTS(reinterpret_cast<uintptr_t>(out_xy) % vec == 0,
+                 "the ordered points must start on a " + std::to_string(vec) +
+                   "-byte boundary");
+    points_in_quadtree_order(point_indices, num_point_indices, x, y, num_points, dtype, out_xy,
+                             as_stream(stream));
   });
 }
 
@@ -507,6 +596,119 @@ cspt_status cspt_quadtree_point_to_nearest_linestring(
                                          dtype, method, alloc, out_point_index,
                                          out_linestring_index, out_distance);
     *out_num_rows = num_point_indices;
+  });
+}
+
+// Points in quadtree order (cspt_points_in_quadtree_order) given instead of
+// point_indices, x and y: present, aligned for one vector load per point.
+static void check_ordered(void const* ordered_xy, cspt_dtype dtype)
+{
+  size_t const vec = dtype == CSPT_FLOAT64 ? 16 : 8;
+  CSPT_EXPECTS(ordered_xy, "the ordered points must not be null");
+  CSPT_EXPECTS(reinterpret_cast<uintptr_t>(ordered_xy) % vec == 0,
+               "the ordered points must start on a " + std::to_string(vec) + "-byte boundary");
+}
+
+cspt_status cspt_quadtree_point_in_polygon_ordered(
+  const uint32_t* pair_polygon, const uint32_t* pair_quad, size_t num_pairs,
+  const cspt_quadtree* tree, const void* ordered_xy, size_t num_points,
+  const uint32_t* poly_offsets, size_t num_poly_offsets, const uint32_t* ring_offsets,
+  size_t num_ring_offsets, const void* poly_x, const void* poly_y, size_t num_poly_vertices,
+  cspt_dtype dtype, cspt_method method, const cspt_allocator* mr, void* stream,
+  uint32_t** out_polygon_index, uint32_t** out_point_index, size_t* out_num_pairs)
+{
+  return guarded([&] {
+    CSPT_EXPECTS(out_polygon_index && out_point_index && out_num_pairs,
+                 "output pointers must not be null");
+    *out_polygon_index = nullptr;
+    *out_point_index   = nullptr;
+    *out_num_pairs     = 0;
+    t_last_refined     = 0;
+    CSPT_EXPECTS(tree, "a quadtree table must have 5 columns");
+    check_dtype(dtype);
+    CSPT_EXPECTS(method == CSPT_METHOD_EXACT || method == CSPT_METHOD_FILTERED,
+                 "unknown point-in-polygon method");
+    if (num_pairs == 0 || tree->num_nodes == 0 || num_points == 0 || num_poly_offsets == 0)
+      return;
+    check_ordered(ordered_xy, dtype);
+    CSPT_EXPECTS(num_ring_offsets > 0,
+                 "Polygon ring offsets must contain at least one (1) value");
+    Allocator alloc(mr, as_stream(stream));
+    uint64_t refined = 0;
+    quadtree_point_in_polygon(pair_polygon, pair_quad, num_pairs, tree, nullptr, num_points,
+                              nullptr, nullptr, poly_offsets, num_poly_offsets, ring_offsets,
+                              num_ring_offsets, poly_x, poly_y, num_poly_vertices, dtype, method,
+                              alloc, out_polygon_index, out_point_index, out_num_pairs, &refined,
+                              nullptr, ordered_xy);
+    t_last_refined = refined;
+  });
+}
+
+cspt_status cspt_quadtree_point_in_polygon_host_ordered(
+  const uint32_t* pair_polygon, const uint32_t* pair_quad, size_t num_pairs,
+  const cspt_quadtree* tree, const void* ordered_xy, size_t num_points,
+  const uint32_t* poly_offsets, size_t num_poly_offsets, const uint32_t* ring_offsets,
+  size_t num_ring_offsets, const void* poly_x, const void* poly_y, size_t num_poly_vertices,
+  cspt_dtype dtype, cspt_method method, const cspt_allocator* mr, void* stream,
+  uint32_t* host_polygon_index, uint32_t* host_point_index, size_t host_capacity,
+  size_t* out_num_pairs)
+{
+  return guarded([&] {
+    CSPT_EXPECTS(out_num_pairs, "output pointers must not be null");
+    *out_num_pairs = 0;
+    t_last_refined = 0;
+    CSPT_EXPECTS(tree, "a quadtree table must have 5 columns");
+    check_dtype(dtype);
+    CSPT_EXPECTS(method == CSPT_METHOD_EXACT || method == CSPT_METHOD_FILTERED,
+                 "unknown point-in-polygon method");
+    CSPT_EXPECTS(host_capacity == 0 || (host_polygon_index && host_point_index),
+                 "host output arrays must not be null");
+    if (num_pairs == 0 || tree->num_nodes == 0 || num_points == 0 || num_poly_offsets == 0)
+      return;
+    check_ordered(ordered_xy, dtype);
+    CSPT_EXPECTS(num_ring_offsets > 0,
+                 "Polygon ring offsets must contain at least one (1) value");
+    Allocator alloc(mr, as_stream(stream));
+    uint64_t refined = 0;
+    HostRows const host{host_polygon_index, host_point_index, host_capacity};
+    quadtree_point_in_polygon(pair_polygon, pair_quad, num_pairs, tree, nullptr, num_points,
+                              nullptr, nullptr, poly_offsets, num_poly_offsets, ring_offsets,
+                              num_ring_offsets, poly_x, poly_y, num_poly_vertices, dtype, method,
+                              alloc, nullptr, nullptr, out_num_pairs, &refined, &host,
+                              ordered_xy);
+    t_last_refined = refined;
+  });
+}
+
+cspt_status cspt_quadtree_point_to_nearest_linestring_ordered(
+  const uint32_t* pair_linestring, const uint32_t* pair_quad, size_t num_pairs,
+  const cspt_quadtree* tree, const void* ordered_xy, size_t num_points,
+  const uint32_t* linestring_offsets, size_t num_linestring_offsets, const void* ls_x,
+  const void* ls_y, size_t num_ls_vertices, cspt_dtype dtype, cspt_method method,
+  const cspt_allocator* mr, void* stream, uint32_t* out_point_index,
+  uint32_t* out_linestring_index, void* out_distance, size_t* out_num_rows)
+{
+  return guarded([&] {
+    (void)num_ls_vertices;
+    CSPT_EXPECTS(out_num_rows, "output pointers must not be null");
+    *out_num_rows = 0;
+    CSPT_EXPECTS(tree, "a quadtree table must have 5 columns");
+    check_dtype(dtype);
+    CSPT_EXPECTS(method == CSPT_METHOD_EXACT || method == CSPT_METHOD_FILTERED,
+                 "unknown nearest-linestring method");
+    if (num_pairs == 0 || tree->num_nodes == 0 || num_points == 0 ||
+        num_linestring_offsets == 0)
+      return;
+    check_ordered(ordered_xy, dtype);
+    CSPT_EXPECTS(out_point_index && out_linestring_index && out_distance,
+                 "output pointers must not be null");
+    Allocator alloc(mr, as_stream(stream));
+    quadtree_point_to_nearest_linestring(pair_linestring, pair_quad, num_pairs, tree, nullptr,
+                                         num_points, nullptr, nullptr, linestring_offsets,
+                                         num_linestring_offsets, ls_x, ls_y, dtype, method,
+                                         alloc, out_point_index, out_linestring_index,
+                                         out_distance, ordered_xy);
+    *out_num_rows = num_points;
   });
 }
 

@@ -214,6 +214,39 @@ cudaStream_t side_stream();
 // Makes `waiter` wait for everything enqueued on `on` so far.
 void stream_wait(cudaStream_t waiter, cudaStream_t on);
 
+// Where a kernel reads the coordinates of the point at sorted position pos
+// (a position in the quadtree's point_indices): through the permutation,
+// x[point_indices[pos]] and y[point_indices[pos]] (the reference's gather,
+// two dependent random reads), or from a copy of the points already in
+// quadtree order, xy[2 pos] and xy[2 pos + 1] (one aligned vector read,
+// coalesced across a warp).
+template <typename T>
+struct PointSource {
+  uint32_t const* point_indices;
+  T const* x;
+  T const* y;
+  T const* xy;  // interleaved (x, y) in quadtree order, or null
+
+  __device__ __forceinline__ void load(uint64_t pos, T& px, T& py) const
+  {
+    if (xy) {
+      if constexpr (sizeof(T) == 8) {
+        double2 const v = reinterpret_cast<double2 const*>(xy)[pos];
+        px              = v.x;
+        py              = v.y;
+      } else {
+        float2 const v = reinterpret_cast<float2 const*>(xy)[pos];
+        px             = v.x;
+        py             = v.y;
+      }
+    } else {
+      uint32_t const i = point_indices[pos];
+      px               = x[i];
+      py               = y[i];
+    }
+  }
+};
+
 // Caller's host arrays for result rows written to host memory.
 struct HostRows {
   uint32_t* polygon_index;

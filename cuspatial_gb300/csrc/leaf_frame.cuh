@@ -36,9 +36,8 @@ struct LeafFrame {
 __global__ void __launch_bounds__(256)
   leaf_frame_kernel(uint32_t const* __restrict__ group_start, uint32_t const* __restrict__ ngroups_p,
                     uint32_t const* __restrict__ pair_quad, uint32_t const* __restrict__ qlen,
-                    uint32_t const* __restrict__ qoff, uint32_t const* __restrict__ point_indices,
-                    size_t npi, double const* __restrict__ x, double const* __restrict__ y,
-                    double const* __restrict__ gridp, float2* __restrict__ u,
+                    uint32_t const* __restrict__ qoff, PointSource<double> const src,
+                    size_t npi, double const* __restrict__ gridp, float2* __restrict__ u,
                     LeafFrame* __restrict__ frames)
 {
   int const lane      = threadIdx.x & 31;
@@ -53,18 +52,16 @@ __global__ void __launch_bounds__(256)
     uint32_t const len  = qlen[quad];
     uint64_t const off  = qoff[quad];
     double x0 = 0.0, y0 = 0.0;
-    if (len > 0 && off < npi) {
-      uint32_t const i0 = point_indices[off];
-      x0                = x[i0];
-      y0                = y[i0];
-    }
+    if (len > 0 && off < npi) src.load(off, x0, y0);
     double rx = rint(ginv_ok ? x0 * ginv : x0 / g), ry = rint(ginv_ok ? y0 * ginv : y0 / g);
     if (!(fabs(rx) < 4.0e18)) rx = 0.0;  // also NaN
     if (!(fabs(ry) < 4.0e18)) ry = 0.0;
     double const ax = rx * g, ay = ry * g;
     float m = 0.0f, xmn = INFINITY, xmx = -INFINITY, ymn = INFINITY, ymx = -INFINITY;
     bool bad = false;
-    // four independent gathers per lane per round
+    // four independent loads per lane per round (with points in quadtree
+    // order one coalesced 16-byte load each; otherwise the index, then the
+    // two gathers)
     for (uint32_t c0 = 0; c0 < len; c0 += 128) {
       uint32_t pi[4];
       bool ok[4];
@@ -73,13 +70,22 @@ __global__ void __launch_bounds__(256)
         uint32_t const c   = c0 + t * 32 + lane;
         uint64_t const pos = off + c;
         ok[t]              = c < len && pos < npi;
-        pi[t]              = ok[t] ? point_indices[pos] : 0u;
+        pi[t]              = (ok[t] && !src.xy) ? src.point_indices[pos] : 0u;
       }
       double px[4], py[4];
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
-        px[t] = ok[t] ? x[pi[t]] : 0.0;
-        py[t] = ok[t] ? y[pi[t]] : 0.0;
+        px[t] = 0.0;
+        py[t] = 0.0;
+        if (!ok[t]) continue;
+        if (src.xy) {
+          double2 const v = reinterpret_cast<double2 const*>(src.xy)[off + c0 + t * 32 + lane];
+          px[t]           = v.x;
+          py[t]           = v.y;
+        } else {
+          px[t] = src.x[pi[t]];
+          py[t] = src.y[pi[t]];
+        }
       }
 #pragma unroll
       for (int t = 0; t < 4; ++t) {

@@ -31,6 +31,11 @@ uint64_t& last_fallbacks()
   static thread_local uint64_t n = 0;
   return n;
 }
+uint64_t& last_group_scans()
+{
+  static thread_local uint64_t n = 0;
+  return n;
+}
 
 namespace {
 
@@ -95,8 +100,7 @@ __global__ void __launch_bounds__(256)
   nearest_kernel(uint32_t const* __restrict__ group_start, size_t ngroups, size_t npairs,
                  uint32_t const* __restrict__ pair_ls, uint32_t const* __restrict__ pair_quad,
                  uint32_t const* __restrict__ qlen, uint32_t const* __restrict__ qoff,
-                 uint32_t const* __restrict__ point_indices, size_t npi, T const* __restrict__ x,
-                 T const* __restrict__ y, uint32_t const* __restrict__ lso, size_t nls,
+                 PointSource<T> const src, size_t npi, uint32_t const* __restrict__ lso, size_t nls,
                  T const* __restrict__ lx, T const* __restrict__ ly, uint32_t* __restrict__ opt,
                  uint32_t* __restrict__ ols, T* __restrict__ od)
 {
@@ -112,8 +116,8 @@ __global__ void __launch_bounds__(256)
     for (uint32_t c = lane; c < len; c += 32) {
       uint64_t const pos = off + c;
       if (pos >= npi) continue;
-      uint32_t const pi = point_indices[pos];
-      T const px = x[pi], py = y[pi];
+      T px, py;
+      src.load(pos, px, py);
       bool have    = false;
       uint32_t bid = 0;
       T bd         = 0;
@@ -303,153 +307,436 @@ __device__ inline float box_lb(float qx, float qy, float4 b, float tol)
   return __fmaf_rn(dx, dx, dy * dy) * 0.9999999990686774f;
 }
 
-__global__ void __launch_bounds__(256)
-  nearest_filtered_kernel(uint32_t const* __restrict__ group_start,
-                          uint32_t const* __restrict__ ngroups_p, size_t npairs,
-                          uint32_t const* __restrict__ pair_ls,
-                          uint32_t const* __restrict__ pair_quad, uint32_t const* __restrict__ qlen,
-                          uint32_t const* __restrict__ qoff,
-                          uint32_t const* __restrict__ point_indices, size_t npi,
-                          double const* __restrict__ x, double const* __restrict__ y,
-                          uint32_t const* __restrict__ lso, size_t nls,
-                          double const* __restrict__ lx, double const* __restrict__ ly,
-                          float2 const* __restrict__ u, LeafFrame const* __restrict__ frames,
-                          LinestringIndexView li, float gf, uint32_t* __restrict__ opt,
-                          uint32_t* __restrict__ ols, double* __restrict__ od,
-                          unsigned long long* __restrict__ fallbacks)
+// squared distance between two boxes, each side widened by tol, shrunk by
+// 2^-30 relative: a lower bound of box_lb for every point of box a
+__device__ inline float boxbox_lb(float4 a, float4 b, float tol)
 {
-  int const lane      = threadIdx.x & 31;
-  size_t const nwarps = (static_cast<size_t>(gridDim.x) * blockDim.x) >> 5;
-  uint32_t const ng   = *ngroups_p;
-  bool const gok      = gf >= 1.17549435e-38f && gf < 1.0e30f;
-  uint32_t nfb        = 0;
-  for (size_t gi = (blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5; gi < ng;
-       gi += nwarps) {
-    uint32_t const k0   = group_start[gi];
-    uint32_t const k1   = gi + 1 < ng ? group_start[gi + 1] : static_cast<uint32_t>(npairs);
-    uint32_t const quad = pair_quad[k0];
-    uint32_t const len  = qlen[quad];
-    uint64_t const off  = qoff[quad];
-    LeafFrame const lf  = frames[gi];
-    for (uint32_t c = lane; c < len; c += 32) {
-      uint64_t const pos = off + c;
-      if (pos >= npi) continue;
-      float2 const uv = u[pos];
-      bool full       = lf.nonfinite || !gok;
-      // pass 1: an upper bound on the best squared distance
-      float U = INFINITY;
-      for (uint32_t k = k0; k < k1 && !full; ++k) {
-        uint32_t const lid = pair_ls[k];
-        if (lid >= nls) continue;
-        long long const dix = li.aix[lid] - lf.ix, diy = li.aiy[lid] - lf.iy;
-        if (li.exact[lid] || dix <= -16777216LL || dix >= 16777216LL || diy <= -16777216LL ||
-            diy >= 16777216LL) {
-          full = true;
-          break;
-        }
-        float const qx = uv.x - static_cast<float>(static_cast<int>(dix)) * gf;
-        float const qy = uv.y - static_cast<float>(static_cast<int>(diy)) * gf;
-        float const m  = fmaxf(fmaxf(li.maxoff[lid], lf.m), fmaxf(fabsf(qx), fabsf(qy)));
-        float const dm = 1.1920928955078125e-07f * m;  // 2 u32 M
-        float const tol = 4.76837158203125e-07f * m;
-        uint32_t const v0 = lso[lid], v1 = lso[lid + 1];
-        uint32_t const nseg = v1 > v0 + 1 ? v1 - v0 - 1 : 0;
-        uint32_t const cb   = li.chunk_base[lid];
-        for (uint32_t ch = 0; ch * kSegChunk < nseg; ++ch) {
-          if (box_lb(qx, qy, li.chunk_box[cb + ch], tol) > U) continue;
-          uint32_t const s0 = v0 + ch * kSegChunk, s1 = min(s0 + kSegChunk, v0 + nseg);
-          for (uint32_t sg = s0; sg < s1; ++sg) {
-            float est, err;
-            seg_estimate(qx, qy, li.seg32[sg], dm, est, err);
-            U = fminf(U, est + err);
-          }
-        }
-      }
-      double px = 0.0, py = 0.0;
-      bool have64 = false;
-      auto load64 = [&]() {
-        if (!have64) {
-          uint32_t const pi = point_indices[pos];
-          px                = x[pi];
-          py                = y[pi];
-          have64            = true;
-        }
-      };
-      bool have = false, skipped = false, nonzero = false;
-      uint32_t bid = 0;
-      double bd    = 0.0;
-      if (!full) {
-        // pass 2: float64 on every segment that can reach U (widened so
-        // that distances left out are larger even after the square root)
-        float const Uw = U * 1.0000000009313226f + 7.52316384526264e-37f;
-        for (uint32_t k = k0; k < k1; ++k) {
-          uint32_t const lid = pair_ls[k];
-          if (lid >= nls) continue;
-          long long const dix = li.aix[lid] - lf.ix, diy = li.aiy[lid] - lf.iy;
-          float const qx = uv.x - static_cast<float>(static_cast<int>(dix)) * gf;
-          float const qy = uv.y - static_cast<float>(static_cast<int>(diy)) * gf;
-          float const m  = fmaxf(fmaxf(li.maxoff[lid], lf.m), fmaxf(fabsf(qx), fabsf(qy)));
-          float const dm = 1.1920928955078125e-07f * m;
-          float const tol = 4.76837158203125e-07f * m;
-          uint32_t const v0 = lso[lid], v1 = lso[lid + 1];
-          uint32_t const nseg = v1 > v0 + 1 ? v1 - v0 - 1 : 0;
-          uint32_t const cb   = li.chunk_base[lid];
-          double dmin         = std::numeric_limits<double>::max();
-          bool evaluated      = false;
-          for (uint32_t ch = 0; ch * kSegChunk < nseg; ++ch) {
-            if (box_lb(qx, qy, li.chunk_box[cb + ch], tol) > Uw) continue;
-            uint32_t const s0 = v0 + ch * kSegChunk, s1 = min(s0 + kSegChunk, v0 + nseg);
-            for (uint32_t sg = s0; sg < s1; ++sg) {
-              float est, err;
-              seg_estimate(qx, qy, li.seg32[sg], dm, est, err);
-              if (est - err > Uw) continue;
-              load64();
-              dmin = fmin(dmin, segment_dist2<double>(px, py, lx[sg], ly[sg], lx[sg + 1],
-                                                      ly[sg + 1]));
-              evaluated = true;
-            }
-          }
-          if (!evaluated || !(dmin <= static_cast<double>(Uw))) {
-            skipped = true;  // farther than the best: cannot win
-            continue;
-          }
-          double const d = sqrt(dmin);
-          if (!have || take_rhs<double>(bd, bid, d, lid)) {
-            bid = lid;
-            bd  = d;
-          }
-          have = true;
-          nonzero |= d != 0.0;
-        }
-        // only zero distances among the candidates while others were left
-        // out: the winner is the nearest non-zero one, find it exactly
-        if (!have || (!nonzero && skipped)) full = true;
-      }
-      if (full) {
-        ++nfb;
-        load64();
-        have = false;
-        for (uint32_t k = k0; k < k1; ++k) {
-          uint32_t const lid = pair_ls[k];
-          if (lid >= nls) continue;
-          double const d = linestring_distance<double>(px, py, lx, ly, lso[lid], lso[lid + 1]);
-          if (!have || take_rhs<double>(bd, bid, d, lid)) {
-            bid = lid;
-            bd  = d;
-          }
-          have = true;
-        }
-      }
-      if (have) {
-        opt[pos] = static_cast<uint32_t>(pos);
-        ols[pos] = bid;
-        od[pos]  = bd;
+  float const dx = fmaxf(fmaxf(b.x - tol - a.z, 0.0f), a.x - b.z - tol);
+  float const dy = fmaxf(fmaxf(b.y - tol - a.w, 0.0f), a.y - b.w - tol);
+  return __fmaf_rn(dx, dx, dy * dy) * 0.9999999990686774f;
+}
+
+// Arguments of the filtered nearest-linestring kernel.
+struct NearestArgs {
+  uint32_t const* group_start;
+  uint32_t const* ngroups_p;
+  size_t npairs;
+  uint32_t const* pair_ls;
+  uint32_t const* pair_quad;
+  uint32_t const* qlen;
+  uint32_t const* qoff;
+  PointSource<double> src;
+  size_t npi;
+  uint32_t const* lso;
+  size_t nls;
+  double const* lx;
+  double const* ly;
+  float2 const* u;
+  LeafFrame const* frames;
+  LinestringIndexView li;
+  float gf;
+  uint32_t* opt;
+  uint32_t* ols;
+  double* od;
+  unsigned long long* stats;  // [0] points folded over every candidate, [1] groups scanned whole
+  unsigned long long* next_group;
+};
+
+// The reference's fold over every candidate of the group, in float64 (the
+// literal per-point loop of the reference).
+__device__ inline void fold_all(NearestArgs const& a, uint32_t k0, uint32_t k1, double px,
+                                double py, bool& have, uint32_t& bid, double& bd)
+{
+  have = false;
+  for (uint32_t k = k0; k < k1; ++k) {
+    uint32_t const lid = a.pair_ls[k];
+    if (lid >= a.nls) continue;
+    double const d = linestring_distance<double>(px, py, a.lx, a.ly, a.lso[lid], a.lso[lid + 1]);
+    if (!have || take_rhs<double>(bd, bid, d, lid)) {
+      bid = lid;
+      bd  = d;
+    }
+    have = true;
+  }
+}
+
+// One point against every candidate linestring of its group, chunk by chunk:
+// pass 1 bounds the running minimum U with float32 estimates and chunk
+// pruning, pass 2 evaluates in float64 only the segments whose estimate can
+// reach U, then the fold; a point whose candidates reach only zero distances
+// (or none) takes fold_all.  Used for groups the listing below cannot take.
+__device__ inline void nearest_point_scan(NearestArgs const& a, uint32_t k0, uint32_t k1,
+                                          LeafFrame const& lf, uint64_t pos, bool gok,
+                                          uint32_t& nfb)
+{
+  LinestringIndexView const& li = a.li;
+  float const gf  = a.gf;
+  float2 const uv = a.u[pos];
+  bool full       = lf.nonfinite || !gok;
+  float U         = INFINITY;
+  for (uint32_t k = k0; k < k1 && !full; ++k) {
+    uint32_t const lid = a.pair_ls[k];
+    if (lid >= a.nls) continue;
+    long long const dix = li.aix[lid] - lf.ix, diy = li.aiy[lid] - lf.iy;
+    if (li.exact[lid] || dix <= -16777216LL || dix >= 16777216LL || diy <= -16777216LL ||
+        diy >= 16777216LL) {
+      full = true;
+      break;
+    }
+    float const qx  = uv.x - static_cast<float>(static_cast<int>(dix)) * gf;
+    float const qy  = uv.y - static_cast<float>(static_cast<int>(diy)) * gf;
+    float const m   = fmaxf(fmaxf(li.maxoff[lid], lf.m), fmaxf(fabsf(qx), fabsf(qy)));
+    float const dm  = 1.1920928955078125e-07f * m;  // 2 u32 M
+    float const tol = 4.76837158203125e-07f * m;
+    uint32_t const v0 = a.lso[lid], v1 = a.lso[lid + 1];
+    uint32_t const nseg = v1 > v0 + 1 ? v1 - v0 - 1 : 0;
+    uint32_t const cb   = li.chunk_base[lid];
+    for (uint32_t ch = 0; ch * kSegChunk < nseg; ++ch) {
+      if (box_lb(qx, qy, li.chunk_box[cb + ch], tol) > U) continue;
+      uint32_t const s0 = v0 + ch * kSegChunk, s1 = min(s0 + kSegChunk, v0 + nseg);
+      for (uint32_t sg = s0; sg < s1; ++sg) {
+        float est, err;
+        seg_estimate(qx, qy, li.seg32[sg], dm, est, err);
+        U = fminf(U, est + err);
       }
     }
   }
-  if (fallbacks) {
-    for (int o = 16; o > 0; o >>= 1) nfb += __shfl_xor_sync(0xFFFFFFFFu, nfb, o);
-    if (lane == 0 && nfb) atomicAdd(fallbacks, static_cast<unsigned long long>(nfb));
+  double px = 0.0, py = 0.0;
+  a.src.load(pos, px, py);
+  bool have = false, skipped = false, nonzero = false;
+  uint32_t bid = 0;
+  double bd    = 0.0;
+  if (!full) {
+    // pass 2: float64 on every segment that can reach U (widened so that
+    // distances left out are larger even after the square root)
+    float const Uw = U * 1.0000000009313226f + 7.52316384526264e-37f;
+    for (uint32_t k = k0; k < k1; ++k) {
+      uint32_t const lid = a.pair_ls[k];
+      if (lid >= a.nls) continue;
+      long long const dix = li.aix[lid] - lf.ix, diy = li.aiy[lid] - lf.iy;
+      float const qx  = uv.x - static_cast<float>(static_cast<int>(dix)) * gf;
+      float const qy  = uv.y - static_cast<float>(static_cast<int>(diy)) * gf;
+      float const m   = fmaxf(fmaxf(li.maxoff[lid], lf.m), fmaxf(fabsf(qx), fabsf(qy)));
+      float const dm  = 1.1920928955078125e-07f * m;
+      float const tol = 4.76837158203125e-07f * m;
+      uint32_t const v0 = a.lso[lid], v1 = a.lso[lid + 1];
+      uint32_t const nseg = v1 > v0 + 1 ? v1 - v0 - 1 : 0;
+      uint32_t const cb   = li.chunk_base[lid];
+      double dmin         = std::numeric_limits<double>::max();
+      bool evaluated      = false;
+      for (uint32_t ch = 0; ch * kSegChunk < nseg; ++ch) {
+        if (box_lb(qx, qy, li.chunk_box[cb + ch], tol) > Uw) continue;
+        uint32_t const s0 = v0 + ch * kSegChunk, s1 = min(s0 + kSegChunk, v0 + nseg);
+        for (uint32_t sg = s0; sg < s1; ++sg) {
+          float est, err;
+          seg_estimate(qx, qy, li.seg32[sg], dm, est, err);
+          if (est - err > Uw) continue;
+          dmin = fmin(dmin, segment_dist2<double>(px, py, a.lx[sg], a.ly[sg], a.lx[sg + 1],
+                                                  a.ly[sg + 1]));
+          evaluated = true;
+        }
+      }
+      if (!evaluated || !(dmin <= static_cast<double>(Uw))) {
+        skipped = true;  // farther than the best: cannot win
+        continue;
+      }
+      double const d = sqrt(dmin);
+      if (!have || take_rhs<double>(bd, bid, d, lid)) {
+        bid = lid;
+        bd  = d;
+      }
+      have = true;
+      nonzero |= d != 0.0;
+    }
+    // only zero distances among the candidates while others were left out:
+    // the winner is the nearest non-zero one, find it exactly
+    if (!have || (!nonzero && skipped)) full = true;
+  }
+  if (full) {
+    ++nfb;
+    fold_all(a, k0, k1, px, py, have, bid, bd);
+  }
+  if (have) {
+    a.opt[pos] = static_cast<uint32_t>(pos);
+    a.ols[pos] = bid;
+    a.od[pos]  = bd;
+  }
+}
+
+// The group's segment list (per warp, in shared memory): the candidate
+// segments whose box lies within a radius of the leaf's point box, each in
+// the leaf's float32 frame, with its global start vertex and its pair (the
+// pair gives the linestring and the fold order).
+constexpr int kNearWarps    = 4;    // warps per block
+constexpr uint32_t kNearCap = 384;  // listed segments per warp
+struct NearList {
+  float4 e[kNearCap];
+  uint32_t seg[kNearCap];
+  uint32_t pair[kNearCap];
+};
+constexpr uint32_t kListOverflow = 0xFFFFFFFEu;  // more than kNearCap segments
+constexpr uint32_t kListFrame    = 0xFFFFFFFFu;  // a linestring outside the float32 frames
+
+// Lists, in pair order, the segments of the group's linestrings whose box
+// is within squared distance r2 of the leaf's point box (box-to-box lower
+// bound with the filter's margin tol, computed in each linestring's frame;
+// the leaf box maps into that frame monotonically, so it holds every point's
+// mapped offset and the bound is below each point's own box_lb).  Chunk
+// boxes are tested first; four near chunks are expanded per round, eight
+// lanes per chunk, one segment each.  mg receives the largest magnitude the
+// listed segments involve (their linestrings' offsets and their leaf-frame
+// coordinates).  Returns the count, kListOverflow or kListFrame.
+__device__ uint32_t list_segments(NearestArgs const& a, NearList& L, uint32_t k0, uint32_t k1,
+                                  LeafFrame const& lf, float r2, float& mg)
+{
+  LinestringIndexView const& li = a.li;
+  int const lane    = threadIdx.x & 31;
+  unsigned const lt = (1u << lane) - 1u;
+  uint32_t n        = 0;
+  float m           = lf.m;
+  for (uint32_t k = k0; k < k1; ++k) {
+    uint32_t const lid = a.pair_ls[k];
+    if (lid >= a.nls) continue;
+    long long const dix = li.aix[lid] - lf.ix, diy = li.aiy[lid] - lf.iy;
+    if (li.exact[lid] || dix <= -16777216LL || dix >= 16777216LL || diy <= -16777216LL ||
+        diy >= 16777216LL)
+      return kListFrame;
+    float const sx  = static_cast<float>(static_cast<int>(dix)) * a.gf;
+    float const sy  = static_cast<float>(static_cast<int>(diy)) * a.gf;
+    float4 const lb = make_float4(lf.uxmin - sx, lf.uymin - sy, lf.uxmax - sx, lf.uymax - sy);
+    float const mk  = fmaxf(fmaxf(li.maxoff[lid], lf.m),
+                            fmaxf(fmaxf(fabsf(lb.x), fabsf(lb.y)), fmaxf(fabsf(lb.z), fabsf(lb.w))));
+    float const tol = 4.76837158203125e-07f * mk;
+    uint32_t const v0 = a.lso[lid], v1 = a.lso[lid + 1];
+    uint32_t const nseg = v1 > v0 + 1 ? v1 - v0 - 1 : 0;
+    uint32_t const nch  = (nseg + kSegChunk - 1) / kSegChunk;
+    uint32_t const cb   = li.chunk_base[lid];
+    for (uint32_t c0 = 0; c0 < nch; c0 += 32) {
+      bool const near = c0 + lane < nch && boxbox_lb(lb, li.chunk_box[cb + c0 + lane], tol) <= r2;
+      unsigned cm     = __ballot_sync(0xFFFFFFFFu, near);
+      while (cm) {
+        // lane l expands the (l / 8)-th remaining near chunk, segment l % 8
+        unsigned mm = cm;
+        for (int t = 0; t < (lane >> 3); ++t) mm &= mm - 1u;
+        uint32_t const ch = c0 + static_cast<uint32_t>(__ffs(mm) - 1);
+        uint32_t const sg = v0 + ch * kSegChunk + static_cast<uint32_t>(lane & 7);
+        bool keep         = false;
+        float4 e{};
+        if (mm && ch < nch && sg < v0 + nseg) {
+          e                = li.seg32[sg];
+          float4 const sbx = make_float4(fminf(e.x, e.z), fminf(e.y, e.w), fmaxf(e.x, e.z),
+                                         fmaxf(e.y, e.w));
+          keep             = boxbox_lb(lb, sbx, tol) <= r2;
+        }
+        unsigned const km = __ballot_sync(0xFFFFFFFFu, keep);
+        if (n + __popc(km) > kNearCap) return kListOverflow;
+        if (keep) {
+          uint32_t const slot = n + __popc(km & lt);
+          float4 const el = make_float4(e.x + sx, e.y + sy, e.z + sx, e.w + sy);
+          L.e[slot]       = el;
+          L.seg[slot]     = sg;
+          L.pair[slot]    = k;
+          m = fmaxf(fmaxf(m, mk), fmaxf(fmaxf(fabsf(el.x), fabsf(el.y)),
+                                        fmaxf(fabsf(el.z), fabsf(el.w))));
+        }
+        n += __popc(km);
+        for (int t = 0; t < 4 && cm; ++t) cm &= cm - 1u;
+      }
+    }
+  }
+  __syncwarp();
+  mg = warp_max(m);
+  return n;
+}
+
+// An upper bound, valid for every point of the leaf, of the squared
+// float64 distance to its nearest candidate segment: the smallest, over the
+// candidate chunks, of the largest squared distance from the leaf box to the
+// chunk's first vertex (a segment's distance is at most its start vertex's),
+// each coordinate widened by the margin tol (above the mapping errors) and
+// the result by 2^-20 (above the float32 rounding).  Infinite when a
+// linestring lies outside the float32 frames or there is no segment.
+__device__ float group_upper(NearestArgs const& a, uint32_t k0, uint32_t k1, LeafFrame const& lf)
+{
+  LinestringIndexView const& li = a.li;
+  int const lane = threadIdx.x & 31;
+  float ub       = INFINITY;
+  bool frame_ok  = true;
+  for (uint32_t k = k0; k < k1; ++k) {
+    uint32_t const lid = a.pair_ls[k];
+    if (lid >= a.nls) continue;
+    long long const dix = li.aix[lid] - lf.ix, diy = li.aiy[lid] - lf.iy;
+    if (li.exact[lid] || dix <= -16777216LL || dix >= 16777216LL || diy <= -16777216LL ||
+        diy >= 16777216LL) {
+      frame_ok = false;
+      break;
+    }
+    float const sx  = static_cast<float>(static_cast<int>(dix)) * a.gf;
+    float const sy  = static_cast<float>(static_cast<int>(diy)) * a.gf;
+    float4 const lb = make_float4(lf.uxmin - sx, lf.uymin - sy, lf.uxmax - sx, lf.uymax - sy);
+    float const mk  = fmaxf(fmaxf(li.maxoff[lid], lf.m),
+                            fmaxf(fmaxf(fabsf(lb.x), fabsf(lb.y)), fmaxf(fabsf(lb.z), fabsf(lb.w))));
+    float const tol = 4.76837158203125e-07f * mk;
+    uint32_t const v0 = a.lso[lid], v1 = a.lso[lid + 1];
+    uint32_t const nseg = v1 > v0 + 1 ? v1 - v0 - 1 : 0;
+    for (uint32_t ch = lane; ch * kSegChunk < nseg; ch += 32) {
+      float4 const e = li.seg32[v0 + ch * kSegChunk];
+      float const dx = fmaxf(fabsf(e.x - lb.x), fabsf(e.x - lb.z)) + tol;
+      float const dy = fmaxf(fabsf(e.y - lb.y), fabsf(e.y - lb.w)) + tol;
+      ub             = fminf(ub, __fmaf_rn(dx, dx, dy * dy) * 1.0000009536743164f);
+    }
+  }
+  ub = warp_min(ub);
+  return frame_ok ? ub : INFINITY;
+}
+
+// Smallest float32 upper bound (estimate + error) of the squared distance
+// from point offset (qx, qy) to the listed segments.
+__device__ inline float list_upper(NearList const& L, uint32_t n, float qx, float qy, float dm)
+{
+  float U = INFINITY;
+  for (uint32_t t = 0; t < n; ++t) {
+    float est, err;
+    seg_estimate(qx, qy, L.e[t], dm, est, err);
+    U = fminf(U, est + err);
+  }
+  return U;
+}
+
+// One warp per group of pairs sharing a quadrant (handed out from a device
+// counter), one lane per point.
+//   1. list the segments whose box meets the leaf's point box (radius 0);
+//   2. each point's float32 upper bound U over that list; r2 = the largest U
+//      of the group's points: every point's nearest segment lies within r2
+//      of the leaf box;
+//   3. list the segments within r2 of the leaf box: a segment left out has
+//      a float64 distance above r2 >= U for every point, so it can neither
+//      win nor tie;
+//   4. per point: U over the list, then float64 (the reference's expression)
+//      on every listed segment whose estimate can reach U, folded per
+//      linestring in pair order with the reference's rule.  A point that
+//      reaches only zero distances (the winner is then the nearest non-zero
+//      candidate, possibly unlisted) or none is folded over every candidate.
+// A group whose list overflows, or that meets a linestring outside the
+// float32 frames, a non-finite point or an unusable grid, is scanned whole
+// per point (nearest_point_scan).
+__global__ void __launch_bounds__(kNearWarps * 32)
+  nearest_filtered_kernel(NearestArgs const a)
+{
+  __shared__ NearList s_list[kNearWarps];
+  int const lane    = threadIdx.x & 31;
+  NearList& L       = s_list[threadIdx.x >> 5];
+  uint32_t const ng = *a.ngroups_p;
+  bool const gok    = a.gf >= 1.17549435e-38f && a.gf < 1.0e30f;
+  uint32_t nfb = 0, nscan = 0;
+  for (;;) {
+    unsigned long long gg = 0;
+    if (lane == 0) gg = atomicAdd(a.next_group, 1ull);
+    uint64_t const gi = __shfl_sync(0xFFFFFFFFu, gg, 0);
+    if (gi >= ng) break;
+    uint32_t const k0   = a.group_start[gi];
+    uint32_t const k1   = gi + 1 < ng ? a.group_start[gi + 1] : static_cast<uint32_t>(a.npairs);
+    uint32_t const quad = a.pair_quad[k0];
+    uint32_t const len  = a.qlen[quad];
+    uint64_t const off  = a.qoff[quad];
+    LeafFrame const lf  = a.frames[gi];
+    bool listed         = !lf.nonfinite && gok;
+    float mg            = 0.0f;
+    uint32_t n          = 0;
+    if (listed) {
+      n = list_segments(a, L, k0, k1, lf, 0.0f, mg);
+      listed = n != kListOverflow && n != kListFrame;
+      if (listed && n == 0) {
+        // no segment meets the leaf box: a radius from the chunks' vertices
+        float const r2 = group_upper(a, k0, k1, lf);
+        listed         = r2 < INFINITY;
+        if (listed) {
+          n      = list_segments(a, L, k0, k1, lf, r2, mg);
+          listed = n != kListOverflow && n != kListFrame && n > 0;
+        }
+      }
+    }
+    if (listed) {
+      float const dm = 1.1920928955078125e-07f * mg;
+      float r2       = 0.0f;
+      for (uint32_t c = lane; c < len; c += 32) {
+        uint64_t const pos = off + c;
+        if (pos >= a.npi) continue;
+        float2 const uv = a.u[pos];
+        r2              = fmaxf(r2, list_upper(L, n, uv.x, uv.y, dm));
+      }
+      r2 = warp_max(r2);
+      __syncwarp();  // every lane is done with the first list
+      listed = r2 < INFINITY;
+      if (listed) {
+        n      = list_segments(a, L, k0, k1, lf, r2 * 1.0000009536743164f, mg);
+        listed = n != kListOverflow && n != kListFrame && n > 0;
+      }
+    }
+    if (!listed) {
+      __syncwarp();
+      ++nscan;
+      for (uint32_t c = lane; c < len; c += 32) {
+        uint64_t const pos = off + c;
+        if (pos < a.npi) nearest_point_scan(a, k0, k1, lf, pos, gok, nfb);
+      }
+      __syncwarp();
+      continue;
+    }
+    float const dm = 1.1920928955078125e-07f * mg;
+    for (uint32_t c = lane; c < len; c += 32) {
+      uint64_t const pos = off + c;
+      if (pos >= a.npi) continue;
+      float2 const uv = a.u[pos];
+      float const U   = list_upper(L, n, uv.x, uv.y, dm);
+      float const Uw  = U * 1.0000000009313226f + 7.52316384526264e-37f;
+      double px = 0.0, py = 0.0;
+      a.src.load(pos, px, py);
+      bool have = false, nonzero = false;
+      uint32_t bid = 0;
+      double bd    = 0.0;
+      for (uint32_t t = 0; t < n;) {
+        // the run of entries of one pair (one linestring)
+        uint32_t const k = L.pair[t];
+        double dmin      = std::numeric_limits<double>::max();
+        bool evaluated   = false;
+        for (; t < n && L.pair[t] == k; ++t) {
+          float est, err;
+          seg_estimate(uv.x, uv.y, L.e[t], dm, est, err);
+          if (est - err > Uw) continue;
+          uint32_t const sg = L.seg[t];
+          dmin = fmin(dmin, segment_dist2<double>(px, py, a.lx[sg], a.ly[sg], a.lx[sg + 1],
+                                                  a.ly[sg + 1]));
+          evaluated = true;
+        }
+        if (!evaluated || !(dmin <= static_cast<double>(Uw))) continue;
+        uint32_t const lid = a.pair_ls[k];
+        double const d     = sqrt(dmin);
+        if (!have || take_rhs<double>(bd, bid, d, lid)) {
+          bid = lid;
+          bd  = d;
+        }
+        have = true;
+        nonzero |= d != 0.0;
+      }
+      if (!have || !nonzero) {
+        ++nfb;
+        fold_all(a, k0, k1, px, py, have, bid, bd);
+      }
+      if (have) {
+        a.opt[pos] = static_cast<uint32_t>(pos);
+        a.ols[pos] = bid;
+        a.od[pos]  = bd;
+      }
+    }
+    __syncwarp();  // the next group rewrites this warp's list
+  }
+  if (a.stats) {
+    for (int o = 16; o > 0; o >>= 1) {
+      nfb += __shfl_xor_sync(0xFFFFFFFFu, nfb, o);
+    }
+    if (lane == 0 && nfb) atomicAdd(a.stats, static_cast<unsigned long long>(nfb));
+    if (lane == 0 && nscan) atomicAdd(a.stats + 1, static_cast<unsigned long long>(nscan));
   }
 }
 
@@ -457,9 +744,11 @@ template <typename T>
 void run(uint32_t const* pair_ls, uint32_t const* pair_quad, size_t npairs,
          cspt_quadtree const* tree, uint32_t const* point_indices, size_t npi, T const* x,
          T const* y, uint32_t const* lso, size_t nlso, T const* lx, T const* ly,
-         cspt_method method, Allocator const& alloc, uint32_t* opt, uint32_t* ols, T* od)
+         cspt_method method, Allocator const& alloc, uint32_t* opt, uint32_t* ols, T* od,
+         T const* ordered)
 {
   cudaStream_t const s = alloc.stream();
+  PointSource<T> const src{point_indices, x, y, ordered};
   init_rows_kernel<<<grid_for(npi, 256, sm_grid(16u)), 256, 0, s>>>(npi, opt, ols, od, sizeof(T));
   CSPT_CHECK_LAUNCH();
   // groups: runs of consecutive pairs with the same quadrant first-point offset
@@ -501,20 +790,35 @@ void run(uint32_t const* pair_ls, uint32_t const* pair_quad, size_t npairs,
       Buffer<float2> u(alloc, npi);
       Buffer<LeafFrame> frames(alloc, npairs);
       leaf_frame_kernel<<<grid_for(npairs * 32, 256, sm_grid(32u)), 256, 0, s>>>(
-        gs, gs + npairs, pair_quad, tree->length, qoff, point_indices, npi, x, y, grid.data(),
-        u.data(), frames.data());
+        gs, gs + npairs, pair_quad, tree->length, qoff, src, npi, grid.data(), u.data(),
+        frames.data());
       CSPT_CHECK_LAUNCH();
       LinestringIndexView liv{aix.data(),   aiy.data(),  maxoff.data(), cbase.data(),
                               cbox.data(),  seg32.data(), lexact.data()};
-      Buffer<unsigned long long> fb(alloc, 1);
-      CSPT_CUDA_TRY(cudaMemsetAsync(fb.data(), 0, sizeof(unsigned long long), s));
+      Buffer<unsigned long long> fb(alloc, 3);  // points folded whole, groups scanned, next group
+      CSPT_CUDA_TRY(cudaMemsetAsync(fb.data(), 0, 3 * sizeof(unsigned long long), s));
+      NearestArgs const na{gs,          gs + npairs,  npairs,     pair_ls,   pair_quad,
+                           tree->length, qoff,        src,        npi,       lso,
+                           nls,          lx,          ly,         u.data(),  frames.data(),
+                           liv,          static_cast<float>(g), opt, ols,    od,
+                           fb.data(),    fb.data() + 2};
       KernelTimer timer("nearest", s);
-      nearest_filtered_kernel<<<grid_for(npairs * 32, 256, sm_grid(32u)), 256, 0, s>>>(
-        gs, gs + npairs, npairs, pair_ls, pair_quad, tree->length, qoff, point_indices, npi, x,
-        y, lso, nls, lx, ly, u.data(), frames.data(), liv, static_cast<float>(g), opt, ols, od,
-        fb.data());
+      int per_sm = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nearest_filtered_kernel,
+                                                        kNearWarps * 32, 0) != cudaSuccess ||
+          per_sm < 1) {
+        (void)cudaGetLastError();
+        per_sm = 1;
+      }
+      nearest_filtered_kernel<<<grid_for(npairs * 32, kNearWarps * 32,
+                                         sm_grid(static_cast<unsigned>(per_sm))),
+                                kNearWarps * 32, 0, s>>>(na);
       CSPT_CHECK_LAUNCH();
-      last_fallbacks() = read_back(fb.data(), s);
+      unsigned long long st[2];
+      CSPT_CUDA_TRY(cudaMemcpyAsync(st, fb.data(), sizeof(st), cudaMemcpyDeviceToHost, s));
+      CSPT_CUDA_TRY(cudaStreamSynchronize(s));
+      last_fallbacks()     = st[0];
+      last_group_scans()   = st[1];
       return;
     }
   }
@@ -522,8 +826,8 @@ void run(uint32_t const* pair_ls, uint32_t const* pair_quad, size_t npairs,
   {
     KernelTimer timer("nearest", s);
     nearest_kernel<T, false><<<grid_for(ng * 32, 256, sm_grid(32u)), 256, 0, s>>>(
-      gs, ng, npairs, pair_ls, pair_quad, tree->length, qoff, point_indices, npi, x, y, lso,
-      nls, lx, ly, opt, ols, od);
+      gs, ng, npairs, pair_ls, pair_quad, tree->length, qoff, src, npi, lso, nls, lx, ly, opt,
+      ols, od);
     CSPT_CHECK_LAUNCH();
   }
 }
@@ -537,17 +841,18 @@ void quadtree_point_to_nearest_linestring(uint32_t const* pair_ls, uint32_t cons
                                           size_t nlso, void const* lx, void const* ly,
                                           cspt_dtype dtype, cspt_method method,
                                           Allocator const& alloc, uint32_t* opt, uint32_t* ols,
-                                          void* od)
+                                          void* od, void const* ordered)
 {
   if (dtype == CSPT_FLOAT64)
     run<double>(pair_ls, pair_quad, npairs, tree, point_indices, npi,
                 static_cast<double const*>(x), static_cast<double const*>(y), lso, nlso,
                 static_cast<double const*>(lx), static_cast<double const*>(ly), method, alloc,
-                opt, ols, static_cast<double*>(od));
+                opt, ols, static_cast<double*>(od), static_cast<double const*>(ordered));
   else
     run<float>(pair_ls, pair_quad, npairs, tree, point_indices, npi, static_cast<float const*>(x),
                static_cast<float const*>(y), lso, nlso, static_cast<float const*>(lx),
-               static_cast<float const*>(ly), method, alloc, opt, ols, static_cast<float*>(od));
+               static_cast<float const*>(ly), method, alloc, opt, ols, static_cast<float*>(od),
+               static_cast<float const*>(ordered));
 }
 
 }  // namespace cspt

@@ -100,8 +100,7 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
   pip_pair_kernel(uint32_t const* __restrict__ pair_poly, uint32_t const* __restrict__ pair_quad,
                   uint32_t const* __restrict__ pair_group, size_t npairs,
                   uint32_t const* __restrict__ qlen, uint32_t const* __restrict__ qoff,
-                  uint32_t const* __restrict__ point_indices, size_t npi,
-                  double const* __restrict__ x, double const* __restrict__ y,
+                  PointSource<double> const src, size_t npi,
                   float2 const* __restrict__ u, LeafFrame const* __restrict__ frames,
                   PolygonIndexView<double> ix, uint64_t const* __restrict__ word_off,
                   uint32_t* __restrict__ bits, uint32_t* __restrict__ counts,
@@ -339,10 +338,8 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
             double px64 = 0.0, py64 = 0.0;
             auto load = [&] {
               if (!have64) {
-                uint32_t const pi = point_indices[pos];
-                px64              = x[pi];
-                py64              = y[pi];
-                have64            = true;
+                src.load(pos, px64, py64);
+                have64 = true;
               }
             };
             auto exact_at = [&](uint32_t kk) {
@@ -414,16 +411,13 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
             float2 const uv = u[pos];
             hit = filtered_test<Ordered>(
               ix, poly, uv.x - dx, uv.y - dy, mp, lf.m, bx, invh, invw, ns, slab0, vb, ve,
-              [&](double& px, double& py) {
-                uint32_t const pi = point_indices[pos];
-                px                = x[pi];
-                py                = y[pi];
-              },
+              [&](double& px, double& py) { src.load(pos, px, py); },
               nref);
           } else {
             ++nref;
-            uint32_t const pi = point_indices[pos];
-            hit               = pip_exact<double>(x[pi], y[pi], ix, poly);
+            double px, py;
+            src.load(pos, px, py);
+            hit = pip_exact<double>(px, py, ix, poly);
           }
         }
         unsigned const w = __ballot_sync(0xFFFFFFFFu, hit);
@@ -435,8 +429,9 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
         uint64_t const pos = off + c + lane;
         bool hit           = false;
         if (c + lane < len && pos < npi) {
-          uint32_t const pi = point_indices[pos];
-          hit               = pip_exact<double>(x[pi], y[pi], ix, poly);
+          double px, py;
+          src.load(pos, px, py);
+          hit = pip_exact<double>(px, py, ix, poly);
         }
         unsigned const w = __ballot_sync(0xFFFFFFFFu, hit);
         if (lane == 0) bits[wb + (c >> 5)] = w;
@@ -456,9 +451,7 @@ __global__ void __launch_bounds__(256)
   pip_pair_kernel_f32(uint32_t const* __restrict__ pair_poly,
                       uint32_t const* __restrict__ pair_quad, size_t npairs,
                       uint32_t const* __restrict__ qlen, uint32_t const* __restrict__ qoff,
-                      uint32_t const* __restrict__ point_indices, size_t npi,
-                      float const* __restrict__ x, float const* __restrict__ y,
-                      PolygonIndexView<float> ix, uint64_t const* __restrict__ word_off,
+                      PointSource<float> const src, size_t npi, PolygonIndexView<float> ix, uint64_t const* __restrict__ word_off,
                       uint32_t* __restrict__ bits, uint32_t* __restrict__ counts)
 {
   int const lane     = threadIdx.x & 31;
@@ -475,8 +468,9 @@ __global__ void __launch_bounds__(256)
       uint64_t const pos = off + c + lane;
       bool hit           = false;
       if (c + lane < len && pos < npi && poly < ix.num_polygons) {
-        uint32_t const pi = point_indices[pos];
-        hit               = pip_exact<float>(x[pi], y[pi], ix, poly);
+        float px, py;
+        src.load(pos, px, py);
+        hit = pip_exact<float>(px, py, ix, poly);
       }
       unsigned const w = __ballot_sync(0xFFFFFFFFu, hit);
       if (lane == 0) bits[wb + (c >> 5)] = w;
@@ -525,9 +519,10 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
          T const* y, uint32_t const* po, size_t npo, uint32_t const* ro, size_t nro,
          T const* vx, T const* vy, size_t nv, cspt_method method, Allocator const& alloc,
          uint32_t** out_poly, uint32_t** out_point, size_t* out_n, uint64_t* out_refined,
-         HostRows const* host)
+         HostRows const* host, T const* ordered)
 {
   cudaStream_t const s = alloc.stream();
+  PointSource<T> const src{point_indices, x, y, ordered};
   bool const filtered  = method == CSPT_METHOD_FILTERED && std::is_same<T, double>::value;
   uint32_t const* qlen = tree->length;
   uint32_t const* qoff = tree->offset;
@@ -540,8 +535,6 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
       return static_cast<uint64_t>((qlen[pair_quad[k]] + 31u) >> 5);
     },
     [wo] __device__(size_t k, uint64_t e, uint64_t) { wo[k] = e; }, npairs, wo + npairs, alloc);
-  size_t const nwords = read_back(wo + npairs, s);
-  Buffer<uint32_t> bits(alloc, nwords);
   Buffer<uint32_t> counts(alloc, npairs);
   Buffer<unsigned long long> refined(alloc, 2);  // [0] refined candidates, [1] next pair
   CSPT_CUDA_TRY(cudaMemsetAsync(refined.data(), 0, 2 * sizeof(unsigned long long), s));
@@ -569,25 +562,31 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
     u      = Buffer<float2>(alloc, npi);
     frames = Buffer<LeafFrame>(alloc, npairs);
   }
-  // The leaf frames (a gather of the points, bound by HBM) run on a second
-  // stream while the index writes its slab entries: the sizing pass below
-  // synchronises the stream, so everything above is complete when the frames
-  // start, and `join` (destroyed before the index and the buffers above, also
-  // on an exception) orders the rest of the call after them.
+  // The leaf frames (bound by HBM) run on a second stream while the index
+  // writes its slab entries: they start once everything enqueued above,
+  // the index's sizing pass and anchor grid included, is complete, and `join`
+  // (destroyed before the index and the buffers above, also on an
+  // exception) orders the rest of the call after them.  Nothing here waits
+  // on the host.
   PolygonIndex<T> index(po, npo, ro, nro, vx, vy, nv, filtered, alloc, false, filtered);
   cudaStream_t const side = filtered ? side_stream() : nullptr;
   StreamJoin join(s, side);
   if constexpr (std::is_same<T, double>::value) {
     if (filtered) {
+      stream_wait(side, s);
       KernelTimer timer("leaf_frames", side);
       leaf_frame_kernel<<<leaf_frame_grid(npairs), blk, 0, side>>>(
-        gstart.data(), gstart.data() + npairs, pair_quad, qlen, qoff, point_indices, npi, x, y,
-        index.grid(), u.data(), frames.data());
+        gstart.data(), gstart.data() + npairs, pair_quad, qlen, qoff, src, npi, index.grid(),
+        u.data(), frames.data());
       CSPT_CHECK_LAUNCH();
     }
   }
   index.fill();
   join.join();
+  // the bitmask's size: the one read-back before the evaluation, taken once
+  // the index and the frames are queued, so the device stays busy meanwhile
+  size_t const nwords = read_back(wo + npairs, s);
+  Buffer<uint32_t> bits(alloc, nwords);
   // hit bitmask and per-pair counts of pairs [k0, k0 + n) (the pair
   // arrays are offset; word offsets and group ids stay absolute)
   auto evaluate = [&](size_t k0, size_t n) {
@@ -596,18 +595,18 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
       CSPT_CUDA_TRY(cudaMemsetAsync(refined.data() + 1, 0, sizeof(unsigned long long), s));
       if (filtered)
         pip_pair_kernel<true><<<pair_grid(pip_pair_kernel<true>, kPipBlock, n), kPipBlock, 0, s>>>(
-          pair_poly + k0, pair_quad + k0, pgroup.data() + k0, n, qlen, qoff, point_indices, npi,
-          x, y, u.data(), frames.data(), index.view(), word_off.data() + k0, bits.data(),
-          counts.data() + k0, refined.data(), refined.data() + 1);
+          pair_poly + k0, pair_quad + k0, pgroup.data() + k0, n, qlen, qoff, src, npi, u.data(),
+          frames.data(), index.view(), word_off.data() + k0, bits.data(), counts.data() + k0,
+          refined.data(), refined.data() + 1);
       else
         pip_pair_kernel<false>
           <<<pair_grid(pip_pair_kernel<false>, kPipBlock, n), kPipBlock, 0, s>>>(
-            pair_poly + k0, pair_quad + k0, nullptr, n, qlen, qoff, point_indices, npi, x, y,
-            nullptr, nullptr, index.view(), word_off.data() + k0, bits.data(), counts.data() + k0,
-            nullptr, refined.data() + 1);
+            pair_poly + k0, pair_quad + k0, nullptr, n, qlen, qoff, src, npi, nullptr, nullptr,
+            index.view(), word_off.data() + k0, bits.data(), counts.data() + k0, nullptr,
+            refined.data() + 1);
     } else {
       pip_pair_kernel_f32<<<grid_for(n * 32, blk, sm_grid(8u * 4u)), blk, 0, s>>>(
-        pair_poly + k0, pair_quad + k0, n, qlen, qoff, point_indices, npi, x, y, index.view(),
+        pair_poly + k0, pair_quad + k0, n, qlen, qoff, src, npi, index.view(),
         word_off.data() + k0, bits.data(), counts.data() + k0);
     }
     CSPT_CHECK_LAUNCH();
@@ -780,22 +779,22 @@ class PipExec::Impl {
     CSPT_CUDA_TRY(cudaMemsetAsync(refined_.data(), 0, 2 * sizeof(unsigned long long), s));
     if (filtered_) {
       leaf_frame_kernel<<<grd, blk, 0, s>>>(gstart_.data(), gstart_.data() + np_, pq_, qlen_,
-                                            qoff_, pi_, npi_, x_, y_, ix_.grid, u_.data(),
+                                            qoff_, src(), npi_, ix_.grid, u_.data(),
                                             frames_.data());
       CSPT_CHECK_LAUNCH();
       if (ix_.slab_nfull)
         pip_pair_kernel<true, true><<<grid_ordered_, blk, 0, s>>>(
-          pp_, pq_, pgroup_.data(), np_, qlen_, qoff_, pi_, npi_, x_, y_, u_.data(),
-          frames_.data(), ix_, word_off_.data(), bits_.data(), counts_.data(), refined_.data(),
+          pp_, pq_, pgroup_.data(), np_, qlen_, qoff_, src(), npi_, u_.data(), frames_.data(),
+          ix_, word_off_.data(), bits_.data(), counts_.data(), refined_.data(),
           refined_.data() + 1);
       else
         pip_pair_kernel<true><<<grid_true_, blk, 0, s>>>(
-          pp_, pq_, pgroup_.data(), np_, qlen_, qoff_, pi_, npi_, x_, y_, u_.data(),
-          frames_.data(), ix_, word_off_.data(), bits_.data(), counts_.data(), refined_.data(),
+          pp_, pq_, pgroup_.data(), np_, qlen_, qoff_, src(), npi_, u_.data(), frames_.data(),
+          ix_, word_off_.data(), bits_.data(), counts_.data(), refined_.data(),
           refined_.data() + 1);
     } else {
       pip_pair_kernel<false><<<grid_false_, blk, 0, s>>>(
-        pp_, pq_, nullptr, np_, qlen_, qoff_, pi_, npi_, x_, y_, nullptr, nullptr, ix_,
+        pp_, pq_, nullptr, np_, qlen_, qoff_, src(), npi_, nullptr, nullptr, ix_,
         word_off_.data(), bits_.data(), counts_.data(), nullptr, refined_.data() + 1);
     }
     CSPT_CHECK_LAUNCH();
@@ -822,6 +821,7 @@ class PipExec::Impl {
   }
 
   uint64_t const* total() const { return out_off_.data() + np_; }
+  PointSource<double> src() const { return PointSource<double>{pi_, x_, y_, nullptr}; }
   uint64_t const* pair_out_offsets() const { return out_off_.data(); }
   int const* overflow() const { return flag_.data(); }
   unsigned long long const* refined() const { return refined_.data(); }
@@ -875,18 +875,19 @@ void quadtree_point_in_polygon(uint32_t const* pair_poly, uint32_t const* pair_q
                                size_t nro, void const* vx, void const* vy, size_t nv,
                                cspt_dtype dtype, cspt_method method, Allocator const& alloc,
                                uint32_t** out_poly, uint32_t** out_point, size_t* out_n,
-                               uint64_t* out_refined, HostRows const* host)
+                               uint64_t* out_refined, HostRows const* host, void const* ordered)
 {
   if (dtype == CSPT_FLOAT64)
     run<double>(pair_poly, pair_quad, npairs, tree, point_indices, npi,
                 static_cast<double const*>(x), static_cast<double const*>(y), po, npo, ro, nro,
                 static_cast<double const*>(vx), static_cast<double const*>(vy), nv, method, alloc,
-                out_poly, out_point, out_n, out_refined, host);
+                out_poly, out_point, out_n, out_refined, host,
+                static_cast<double const*>(ordered));
   else
     run<float>(pair_poly, pair_quad, npairs, tree, point_indices, npi,
                static_cast<float const*>(x), static_cast<float const*>(y), po, npo, ro, nro,
                static_cast<float const*>(vx), static_cast<float const*>(vy), nv, method, alloc,
-               out_poly, out_point, out_n, out_refined, host);
+               out_poly, out_point, out_n, out_refined, host, static_cast<float const*>(ordered));
 }
 
 }  // namespace cspt

@@ -7,6 +7,8 @@
 //   (scans of slab counts, entries and vertical counts over polygons)
 //   fill:  grid-rounded anchors, float32 box and edges, slab offsets, slab
 //          entries (vertex index and float32 edge), sorted vertical x.
+#include <cmath>
+
 #include "polygon_index.cuh"
 #include "scan.cuh"
 
@@ -749,18 +751,17 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
   prev_      = Buffer<uint32_t>(alloc, nv);
   if (build_float32) edge32_ = Buffer<float4>(alloc, nv);
   Buffer<uint32_t> nent(alloc, np + 1), ebase(alloc, np + 1), nvert(alloc, np + 1);
-  Buffer<uint32_t> totals(alloc, 3);
   Buffer<uint32_t> spans(alloc, nv);
   Buffer<float> yslab(alloc, nv);
 
+  double const density = build_float32 ? (order_slabs ? kSlabDensityOrdered : kSlabDensityFloat32)
+                                       : kSlabDensityFloat64;
   unsigned const grd = static_cast<unsigned>(np < sm_grid(64u) ? (np ? np : 1) : sm_grid(64u));
   if (np > 0) {
     index_count_kernel<T><<<grd, kIdxBlock, 0, s>>>(
       po, ro, vx, vy, np, pminx_.data(), pminy_.data(), pmaxx_.data(), pmaxy_.data(),
       invh_.data(), nslab_.data(), nent.data(), nvert.data(), exact_.data(), prev_.data(),
-      spans.data(), yslab.data(),
-      build_float32 ? (order_slabs ? kSlabDensityOrdered : kSlabDensityFloat32)
-                    : kSlabDensityFloat64);
+      spans.data(), yslab.data(), density);
     CSPT_CHECK_LAUNCH();
   }
   grid_kernel<T><<<1, 1024, 0, s>>>(pminx_.data(), pminy_.data(), pmaxx_.data(), pmaxy_.data(),
@@ -769,25 +770,47 @@ PolygonIndex<T>::PolygonIndex(uint32_t const* po, size_t npo, uint32_t const* ro
   exclusive_scan<uint32_t>(nslab_.data(), slab_base_.data(), np, slab_base_.data() + np, alloc);
   exclusive_scan<uint32_t>(nent.data(), ebase.data(), np, ebase.data() + np, alloc);
   exclusive_scan<uint32_t>(nvert.data(), vbeg_.data(), np, vbeg_.data() + np, alloc);
-  copy_totals_kernel<<<1, 1, 0, s>>>(slab_base_.data() + np, ebase.data() + np,
-                                     vbeg_.data() + np, totals.data());
-  CSPT_CHECK_LAUNCH();
-  Buffer<unsigned long long> wide(alloc, 2);
-  CSPT_CUDA_TRY(cudaMemsetAsync(wide.data(), 0, 2 * sizeof(unsigned long long), s));
-  if (np > 0) {
-    wide_totals_kernel<<<grid_for(np, 256, sm_grid(4u)), 256, 0, s>>>(nslab_.data(), nent.data(),
-                                                                     np, wide.data());
+  // Sizes of the slab arrays.  A polygon of V vertices gets
+  // ns <= max(1, density V / 2) slabs, and its edges' slab spans add up to
+  // at most (density + 1.07) V entries: with ns = s <= density V H / sum|rise|
+  // slabs of height H / ns, an edge of rise r spans at most
+  // r ns / H (1 + 2^-35) + 1 + 1/16 slabs (its range widened by 2^-36 of
+  // itself plus 1/32 slab at each end, float32 slab coordinates within
+  // 2^-12 slab), and the sum over edges of r ns / H is at most density V
+  // (with one slab every edge spans one).  So (density + 2) entries per
+  // vertex, 1 + density / 2 slabs per polygon and one vertical edge per
+  // vertex bound the arrays without reading the counts back: no host
+  // synchronisation.  Only where those bounds reach 2^32 (the 32-bit
+  // offsets' limit) are the exact totals read back and checked.
+  size_t const slab_bound  = np + static_cast<size_t>(std::ceil(density * 0.5 * nv)) + 1;
+  size_t const entry_bound = static_cast<size_t>(std::ceil((density + 2.0) * nv)) + 1;
+  size_t nslabs_total = slab_bound, nentries = entry_bound, nvertical = nv;
+  if (slab_bound >= (size_t{1} << 32) || entry_bound >= (size_t{1} << 32)) {
+    Buffer<uint32_t> totals(alloc, 3);
+    copy_totals_kernel<<<1, 1, 0, s>>>(slab_base_.data() + np, ebase.data() + np,
+                                       vbeg_.data() + np, totals.data());
     CSPT_CHECK_LAUNCH();
+    Buffer<unsigned long long> wide(alloc, 2);
+    CSPT_CUDA_TRY(cudaMemsetAsync(wide.data(), 0, 2 * sizeof(unsigned long long), s));
+    if (np > 0) {
+      wide_totals_kernel<<<grid_for(np, 256, sm_grid(4u)), 256, 0, s>>>(nslab_.data(),
+                                                                       nent.data(), np,
+                                                                       wide.data());
+      CSPT_CHECK_LAUNCH();
+    }
+    uint32_t tot[3];
+    unsigned long long wtot[2];
+    CSPT_CUDA_TRY(cudaMemcpyAsync(tot, totals.data(), sizeof(tot), cudaMemcpyDeviceToHost, s));
+    CSPT_CUDA_TRY(cudaMemcpyAsync(wtot, wide.data(), sizeof(wtot), cudaMemcpyDeviceToHost, s));
+    CSPT_CUDA_TRY(cudaStreamSynchronize(s));
+    CSPT_EXPECTS(wtot[0] < (1ull << 32) && wtot[1] < (1ull << 32),
+                 "polygon set too large for the slab index (2^32 slab entries)");
+    nslabs_total = tot[0];
+    nentries     = tot[1];
+    nvertical    = tot[2];
   }
-  uint32_t tot[3];
-  unsigned long long wtot[2];
-  CSPT_CUDA_TRY(cudaMemcpyAsync(tot, totals.data(), sizeof(tot), cudaMemcpyDeviceToHost, s));
-  CSPT_CUDA_TRY(cudaMemcpyAsync(wtot, wide.data(), sizeof(wtot), cudaMemcpyDeviceToHost, s));
-  CSPT_CUDA_TRY(cudaStreamSynchronize(s));
-  CSPT_EXPECTS(wtot[0] < (1ull << 32) && wtot[1] < (1ull << 32),
-               "polygon set too large for the slab index (2^32 slab entries)");
-  sizing_.reset(new Sizing{po, ro, vx, vy, np, tot[0], tot[1], tot[2], build_float32, order_slabs,
-                           grd, std::move(ebase), std::move(nvert), std::move(spans),
+  sizing_.reset(new Sizing{po, ro, vx, vy, np, nslabs_total, nentries, nvertical, build_float32,
+                           order_slabs, grd, std::move(ebase), std::move(nvert), std::move(spans),
                            std::move(yslab), &alloc});
   if (!defer_fill) fill();
 }
@@ -815,8 +838,7 @@ void PolygonIndex<T>::fill()
   if (build_float32) slab_e32_ = Buffer<float4>(alloc, nentries);
   vert_x_ = Buffer<T>(alloc, nvertical);
   if (build_float32) vert_x32_ = Buffer<float>(alloc, nvertical);
-  if (nslabs_total == 0)
-    CSPT_CUDA_TRY(cudaMemsetAsync(slab_start_.data(), 0, sizeof(uint32_t), s));
+  if (np == 0) CSPT_CUDA_TRY(cudaMemsetAsync(slab_start_.data(), 0, sizeof(uint32_t), s));
   Buffer<float2> vxy32(alloc, build_float32 ? nv : 0);
   if (np > 0) {
     index_fill_kernel<T><<<grd, kIdxBlock, 0, s>>>(

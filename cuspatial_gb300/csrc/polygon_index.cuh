@@ -103,9 +103,10 @@ class PolygonIndex {
   // entries and pays off where the index is evaluated many times (batched
   // plans, resident polygon sets).
   // defer_fill: return once the per-polygon boxes, slab counts and the anchor
-  // grid are on the device and the sizes are known (the call synchronises
-  // the stream for them); fill() then writes the slab entries.  Work that
-  // needs only grid() can run on another stream meanwhile.
+  // grid are enqueued (array sizes come from bounds on the host, so the call
+  // does not wait for the device); fill() then writes the slab entries.  Work
+  // that needs only grid() can run on another stream meanwhile, once it waits
+  // for the calling stream.
   PolygonIndex(uint32_t const* poly_offsets, size_t num_poly_offsets,
                uint32_t const* ring_offsets, size_t num_ring_offsets, T const* vx, T const* vy,
                size_t num_vertices, bool build_float32, Allocator const& alloc,

@@ -15,6 +15,7 @@
 // remove_unqualified_quads rule (phase_2.cuh:206-236).  Leaves keep the first
 // sorted position they cover, which is what the reference's flattened-key
 // scan (phase_2.cuh:98-141) produces.
+#include <limits>
 #include <vector>
 
 #include "common.cuh"
@@ -31,11 +32,17 @@ constexpr uint8_t kNoStart = 0xFF;
 template <typename T>
 __global__ void morton_keys_kernel(T const* __restrict__ x, T const* __restrict__ y, size_t n,
                                    T minx, T miny, T maxx, T maxy, T scale, T rscale, int d,
-                                   uint32_t* __restrict__ keys)
+                                   uint32_t* __restrict__ keys, T* __restrict__ xy)
 {
   for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<size_t>(gridDim.x) * blockDim.x) {
     T const px = x[i], py = y[i];
+    if (xy) {  // the points interleaved, in input order (for the ordered copy)
+      if constexpr (sizeof(T) == 8)
+        reinterpret_cast<double2*>(xy)[i] = make_double2(px, py);
+      else
+        reinterpret_cast<float2*>(xy)[i] = make_float2(px, py);
+    }
     uint32_t k;
     if (px < minx || px > maxx || py < miny || py > maxy) {
       k = static_cast<uint32_t>((1 << (2 * d)) - 1);
@@ -202,6 +209,38 @@ __global__ void internal_offset_kernel(uint8_t const* __restrict__ internal,
   }
 }
 
+// rows of an interleaved point array in quadtree order: dst[p] = src[pi[p]]
+// (pi a permutation of [0, n)), four independent 16-byte (float64) or 8-byte
+// (float32) gathers in flight per thread.
+template <typename V>
+__global__ void __launch_bounds__(256)
+  gather_rows_kernel(uint32_t const* __restrict__ pi, size_t n, V const* __restrict__ src,
+                     V* __restrict__ dst)
+{
+  constexpr int kPer = 4;
+  size_t const step  = static_cast<size_t>(gridDim.x) * blockDim.x * kPer;
+  for (size_t b = static_cast<size_t>(blockIdx.x) * blockDim.x * kPer + threadIdx.x; b < n;
+       b += step) {
+    uint32_t i[kPer];
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      size_t const p = b + static_cast<size_t>(j) * blockDim.x;
+      i[j]           = p < n ? pi[p] : 0u;
+    }
+    V v[kPer];
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      size_t const p = b + static_cast<size_t>(j) * blockDim.x;
+      if (p < n && i[j] < n) v[j] = src[i[j]];
+    }
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      size_t const p = b + static_cast<size_t>(j) * blockDim.x;
+      if (p < n && i[j] < n) dst[p] = v[j];
+    }
+  }
+}
+
 // Host input: the points are copied from host memory (hx, hy) into the
 // caller's device arrays (dx, dy, which build() then reads as x and y) in
 // chunks on a second stream, and the Morton keys of each chunk are computed
@@ -218,7 +257,8 @@ constexpr size_t kHostChunks = 8;
 template <typename T>
 void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d, double y2d,
            double scaled, int max_depth_in, int32_t max_size_in, Allocator const& alloc,
-           uint32_t** out_point_indices, cspt_quadtree* out, HostInput<T> const* host = nullptr)
+           uint32_t** out_point_indices, cspt_quadtree* out, HostInput<T> const* host = nullptr,
+           T* ordered = nullptr)
 {
   cudaStream_t const s = alloc.stream();
   *out                 = cspt_quadtree{nullptr, nullptr, nullptr, nullptr, nullptr, 0};
@@ -245,10 +285,14 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
 
   Buffer<uint32_t> keys(alloc, n), keys_alt(alloc, n);
   Buffer<uint32_t> idx(alloc, n), idx_alt(alloc, n);
+  // ordered copy requested: the key pass also writes the points interleaved
+  // (input order), so the gather after the sort reads one vector per point
+  Buffer<T> xy_in(alloc, ordered ? 2 * n : 0);
+  T* const xy0 = ordered ? xy_in.data() : nullptr;
   if (!host) {
     KernelTimer kt("quadtree_keys", s);
     morton_keys_kernel<T><<<grd, blk, 0, s>>>(x, y, n, minx, miny, maxx, maxy, scale,
-                                              T{1} / scale, d, keys.data());
+                                              T{1} / scale, d, keys.data(), xy0);
     CSPT_CHECK_LAUNCH();
   } else {
     cudaStream_t const copy = side_stream();
@@ -263,7 +307,8 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
                                     cudaMemcpyHostToDevice, copy));
       stream_wait(s, copy);
       morton_keys_kernel<T><<<grid_for(m, blk, sm_grid(16u)), blk, 0, s>>>(
-        x + i0, y + i0, m, minx, miny, maxx, maxy, scale, T{1} / scale, d, keys.data() + i0);
+        x + i0, y + i0, m, minx, miny, maxx, maxy, scale, T{1} / scale, d, keys.data() + i0,
+        xy0 ? xy0 + 2 * i0 : nullptr);
       CSPT_CHECK_LAUNCH();
     }
     copies.join();
@@ -279,7 +324,20 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
   Buffer<uint32_t>& skeys = alt ? keys_alt : keys;
   Buffer<uint32_t>& sidx  = alt ? idx_alt : idx;
   (alt ? keys : keys_alt).reset();
+  if (ordered) {
+    KernelTimer kt("quadtree_order", s);
+    unsigned const og = grid_for((n + 3) / 4, 256, sm_grid(8u));
+    if constexpr (sizeof(T) == 8)
+      gather_rows_kernel<double2><<<og, 256, 0, s>>>(
+        sidx.data(), n, reinterpret_cast<double2 const*>(xy0), reinterpret_cast<double2*>(ordered));
+    else
+      gather_rows_kernel<float2><<<og, 256, 0, s>>>(
+        sidx.data(), n, reinterpret_cast<float2 const*>(xy0), reinterpret_cast<float2*>(ordered));
+    CSPT_CHECK_LAUNCH();
+    xy_in.reset();
+  }
 
+  KernelTimer levels_timer("quadtree_levels", s);
   Buffer<uint8_t> lvl(alloc, n);
   start_level_kernel<<<grd, blk, 0, s>>>(skeys.data(), n, d, lvl.data());
   CSPT_CHECK_LAUNCH();
@@ -430,38 +488,93 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
                        ooff.release(), q};
 }
 
+// The points in quadtree order, interleaved: xy[pos] = (x[pi[pos]],
+// y[pi[pos]]).  Each thread keeps four independent gathers in flight; the
+// index reads and the 16-byte (float64) or 8-byte (float32) stores are
+// coalesced.  An index at or beyond npts is never read through: its point
+// becomes (NaN, NaN).
+template <typename T, typename V>
+__global__ void __launch_bounds__(256)
+  ordered_points_kernel(uint32_t const* __restrict__ pi, size_t n, T const* __restrict__ x,
+                        T const* __restrict__ y, size_t npts, V* __restrict__ xy)
+{
+  constexpr int kPer = 4;
+  size_t const step  = static_cast<size_t>(gridDim.x) * blockDim.x * kPer;
+  for (size_t b = static_cast<size_t>(blockIdx.x) * blockDim.x * kPer + threadIdx.x; b < n;
+       b += step) {
+    uint32_t i[kPer];
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      size_t const p = b + static_cast<size_t>(j) * blockDim.x;
+      i[j]           = p < n ? pi[p] : 0xFFFFFFFFu;
+    }
+    V v[kPer];
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      bool const ok = i[j] < npts;
+      v[j].x        = ok ? x[i[j]] : std::numeric_limits<T>::quiet_NaN();
+      v[j].y        = ok ? y[i[j]] : std::numeric_limits<T>::quiet_NaN();
+    }
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      size_t const p = b + static_cast<size_t>(j) * blockDim.x;
+      if (p < n) xy[p] = v[j];
+    }
+  }
+}
+
 }  // namespace
+
+void points_in_quadtree_order(uint32_t const* point_indices, size_t n, void const* x,
+                              void const* y, size_t npts, cspt_dtype dtype, void* out_xy,
+                              cudaStream_t s)
+{
+  if (n == 0) return;
+  unsigned const grd = grid_for((n + 3) / 4, 256, sm_grid(8u));
+  if (dtype == CSPT_FLOAT64)
+    ordered_points_kernel<double, double2><<<grd, 256, 0, s>>>(
+      point_indices, n, static_cast<double const*>(x), static_cast<double const*>(y), npts,
+      static_cast<double2*>(out_xy));
+  else
+    ordered_points_kernel<float, float2><<<grd, 256, 0, s>>>(
+      point_indices, n, static_cast<float const*>(x), static_cast<float const*>(y), npts,
+      static_cast<float2*>(out_xy));
+  CSPT_CHECK_LAUNCH();
+}
 
 void quadtree_on_points(void const* x, void const* y, size_t n, cspt_dtype dtype, double x_min,
                         double x_max, double y_min, double y_max, double scale, int max_depth,
                         int32_t max_size, Allocator const& alloc, uint32_t** out_point_indices,
-                        cspt_quadtree* out_tree)
+                        cspt_quadtree* out_tree, void* ordered)
 {
   if (dtype == CSPT_FLOAT64)
     build<double>(static_cast<double const*>(x), static_cast<double const*>(y), n, x_min, x_max,
-                  y_min, y_max, scale, max_depth, max_size, alloc, out_point_indices, out_tree);
+                  y_min, y_max, scale, max_depth, max_size, alloc, out_point_indices, out_tree,
+                  nullptr, static_cast<double*>(ordered));
   else
     build<float>(static_cast<float const*>(x), static_cast<float const*>(y), n, x_min, x_max,
-                 y_min, y_max, scale, max_depth, max_size, alloc, out_point_indices, out_tree);
+                 y_min, y_max, scale, max_depth, max_size, alloc, out_point_indices, out_tree,
+                 nullptr, static_cast<float*>(ordered));
 }
 
 void quadtree_on_points_from_host(void const* host_x, void const* host_y, void* dev_x,
                                   void* dev_y, size_t n, cspt_dtype dtype, double x_min,
                                   double x_max, double y_min, double y_max, double scale,
                                   int max_depth, int32_t max_size, Allocator const& alloc,
-                                  uint32_t** out_point_indices, cspt_quadtree* out_tree)
+                                  uint32_t** out_point_indices, cspt_quadtree* out_tree,
+                                  void* ordered)
 {
   if (dtype == CSPT_FLOAT64) {
     HostInput<double> const h{static_cast<double const*>(host_x),
                               static_cast<double const*>(host_y), static_cast<double*>(dev_x),
                               static_cast<double*>(dev_y)};
     build<double>(h.dx, h.dy, n, x_min, x_max, y_min, y_max, scale, max_depth, max_size, alloc,
-                  out_point_indices, out_tree, &h);
+                  out_point_indices, out_tree, &h, static_cast<double*>(ordered));
   } else {
     HostInput<float> const h{static_cast<float const*>(host_x), static_cast<float const*>(host_y),
                              static_cast<float*>(dev_x), static_cast<float*>(dev_y)};
     build<float>(h.dx, h.dy, n, x_min, x_max, y_min, y_max, scale, max_depth, max_size, alloc,
-                 out_point_indices, out_tree, &h);
+                 out_point_indices, out_tree, &h, static_cast<float*>(ordered));
   }
 }
 

@@ -80,6 +80,14 @@ const char* cspt_version(void);
  * counterpart in the reference. */
 uint64_t cspt_last_refined_count(void);
 
+/* Paths taken by the last CSPT_METHOD_FILTERED float64 nearest-linestring
+ * call on this thread: points whose fold ran over every candidate in
+ * float64 (their listed candidates reached only zero distances, or none),
+ * and groups of pairs sharing a quadrant that were scanned point by point
+ * instead of through their leaf's segment list.  Either pointer may be NULL.
+ * Diagnostic with no counterpart in the reference. */
+void cspt_last_nearest_stats(uint64_t* points_folded_whole, uint64_t* groups_scanned);
+
 /* Number of kernels this library has launched since load.  Diagnostic with
  * no counterpart in the reference. */
 uint64_t cspt_launch_count(void);
@@ -127,6 +135,47 @@ cspt_status cspt_quadtree_on_points_host(const void* host_x, const void* host_y,
                                          int8_t max_depth, int32_t max_size, void* device_x,
                                          void* device_y, const cspt_allocator* mr, void* stream,
                                          uint32_t** out_point_indices, cspt_quadtree* out_tree);
+
+/*
+ * The points in quadtree order: writes out_xy[2 i] = x[point_indices[i]] and
+ * out_xy[2 i + 1] = y[point_indices[i]] for i < num_point_indices (out_xy is
+ * the caller's device array of 2 * num_point_indices elements of dtype,
+ * starting on a 16-byte boundary for float64, 8-byte for float32).  An index
+ * at or beyond num_points gives NaN coordinates.  Asynchronous.
+ * No counterpart in the reference: its quadtree_point_in_polygon and
+ * quadtree_point_to_nearest_linestring read every point through
+ * point_indices on every call (an index read and two random reads per
+ * point).  A caller that keeps a quadtree for one or more joins pays that
+ * gather once here and passes the result to the *_ordered entry points,
+ * which then read each leaf's points contiguously.
+ */
+cspt_status cspt_points_in_quadtree_order(const uint32_t* point_indices,
+                                          size_t num_point_indices, const void* x, const void* y,
+                                          size_t num_points, cspt_dtype dtype, void* out_xy,
+                                          void* stream);
+
+/*
+ * cspt_quadtree_on_points and cspt_quadtree_on_points_host that also write
+ * the points in quadtree order to out_ordered_xy (what
+ * cspt_points_in_quadtree_order writes; the caller's device array of
+ * 2 * num_points elements of dtype, 16-byte aligned for float64, 8-byte for
+ * float32).  The key pass writes the points interleaved as it reads them,
+ * so the gather after the sort reads one vector per point.  Tree and
+ * point_indices are those of the calls they stand beside.  No counterpart in
+ * the reference (see cspt_points_in_quadtree_order).
+ */
+cspt_status cspt_quadtree_on_points_ordered(const void* x, const void* y, size_t num_points,
+                                            cspt_dtype dtype, double x_min, double x_max,
+                                            double y_min, double y_max, double scale,
+                                            int8_t max_depth, int32_t max_size,
+                                            const cspt_allocator* mr, void* stream,
+                                            uint32_t** out_point_indices,
+                                            cspt_quadtree* out_tree, void* out_ordered_xy);
+cspt_status cspt_quadtree_on_points_host_ordered(
+  const void* host_x, const void* host_y, size_t num_points, cspt_dtype dtype, double x_min,
+  double x_max, double y_min, double y_max, double scale, int8_t max_depth, int32_t max_size,
+  void* device_x, void* device_y, const cspt_allocator* mr, void* stream,
+  uint32_t** out_point_indices, cspt_quadtree* out_tree, void* out_ordered_xy);
 
 /*
  * Replaces cuspatial::polygon_bounding_boxes
@@ -246,6 +295,39 @@ cspt_status cspt_quadtree_point_to_nearest_linestring(
   cspt_dtype dtype, cspt_method method, const cspt_allocator* mr, void* stream,
   uint32_t* out_point_index, uint32_t* out_linestring_index, void* out_distance,
   size_t* out_num_rows);
+
+/*
+ * cspt_quadtree_point_in_polygon, cspt_quadtree_point_in_polygon_host and
+ * cspt_quadtree_point_to_nearest_linestring with the points given in
+ * quadtree order (ordered_xy: num_points interleaved (x, y) pairs from
+ * cspt_points_in_quadtree_order) in place of point_indices, x and y.  The
+ * results, row order, validation and empty-input rules are those of the
+ * calls they stand beside (point_index is still a position in
+ * point_indices).  No counterpart in the reference (see
+ * cspt_points_in_quadtree_order).
+ */
+cspt_status cspt_quadtree_point_in_polygon_ordered(
+  const uint32_t* pair_polygon, const uint32_t* pair_quad, size_t num_pairs,
+  const cspt_quadtree* tree, const void* ordered_xy, size_t num_points,
+  const uint32_t* poly_offsets, size_t num_poly_offsets, const uint32_t* ring_offsets,
+  size_t num_ring_offsets, const void* poly_x, const void* poly_y, size_t num_poly_vertices,
+  cspt_dtype dtype, cspt_method method, const cspt_allocator* mr, void* stream,
+  uint32_t** out_polygon_index, uint32_t** out_point_index, size_t* out_num_pairs);
+cspt_status cspt_quadtree_point_in_polygon_host_ordered(
+  const uint32_t* pair_polygon, const uint32_t* pair_quad, size_t num_pairs,
+  const cspt_quadtree* tree, const void* ordered_xy, size_t num_points,
+  const uint32_t* poly_offsets, size_t num_poly_offsets, const uint32_t* ring_offsets,
+  size_t num_ring_offsets, const void* poly_x, const void* poly_y, size_t num_poly_vertices,
+  cspt_dtype dtype, cspt_method method, const cspt_allocator* mr, void* stream,
+  uint32_t* host_polygon_index, uint32_t* host_point_index, size_t host_capacity,
+  size_t* out_num_pairs);
+cspt_status cspt_quadtree_point_to_nearest_linestring_ordered(
+  const uint32_t* pair_linestring, const uint32_t* pair_quad, size_t num_pairs,
+  const cspt_quadtree* tree, const void* ordered_xy, size_t num_points,
+  const uint32_t* linestring_offsets, size_t num_linestring_offsets, const void* ls_x,
+  const void* ls_y, size_t num_ls_vertices, cspt_dtype dtype, cspt_method method,
+  const cspt_allocator* mr, void* stream, uint32_t* out_point_index,
+  uint32_t* out_linestring_index, void* out_distance, size_t* out_num_rows);
 
 /*
  * Replaces cuspatial::point_in_polygon

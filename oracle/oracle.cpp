@@ -470,19 +470,17 @@ void quadtree_point_in_polygon(uint32_t const* pair_poly, uint32_t const* pair_q
 {
   out_poly.clear();
   out_point.clear();
-  int nthreads = 1;
-#ifdef _OPENMP
-  nthreads = omp_get_max_threads();
-#endif
-  // contiguous chunks of pairs per thread keep the output order
-  std::vector<std::vector<uint32_t>> tp(nthreads), tq(nthreads);
-#pragma omp parallel num_threads(nthreads)
-  {
-    int tid = 0;
-#ifdef _OPENMP
-    tid = omp_get_thread_num();
-#endif
-    size_t const lo = np * tid / nthreads, hi = np * (tid + 1) / nthreads;
+  // blocks of consecutive pairs, handed out dynamically (pairs differ widely
+  // in cost); each block's rows are kept apart and concatenated in block
+  // order, which keeps the output order
+  size_t const kBlock  = 64;
+  size_t const nblocks = (np + kBlock - 1) / kBlock;
+  std::vector<std::vector<uint32_t>> tp(nblocks), tq(nblocks);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (size_t b = 0; b < nblocks; ++b) {
+    size_t const lo = b * kBlock, hi = std::min(np, lo + kBlock);
+    std::vector<uint32_t>& bp = tp[b];
+    std::vector<uint32_t>& bq = tq[b];
     for (size_t k = lo; k < hi; ++k) {
       uint32_t const poly = pair_poly[k];
       uint32_t const quad = pair_quad[k];
@@ -493,15 +491,19 @@ void quadtree_point_in_polygon(uint32_t const* pair_poly, uint32_t const* pair_q
         uint32_t const pi = point_indices[pos];
         if (is_point_in_polygon<T, Off>(x[pi], y[pi], ring_offsets, poly_offsets[poly],
                                         poly_offsets[poly + 1], vx, vy)) {
-          tp[tid].push_back(poly);
-          tq[tid].push_back(static_cast<uint32_t>(pos));
+          bp.push_back(poly);
+          bq.push_back(static_cast<uint32_t>(pos));
         }
       }
     }
   }
-  for (int t = 0; t < nthreads; ++t) {
-    out_poly.insert(out_poly.end(), tp[t].begin(), tp[t].end());
-    out_point.insert(out_point.end(), tq[t].begin(), tq[t].end());
+  size_t total = 0;
+  for (auto const& v : tp) total += v.size();
+  out_poly.reserve(total);
+  out_point.reserve(total);
+  for (size_t b = 0; b < nblocks; ++b) {
+    out_poly.insert(out_poly.end(), tp[b].begin(), tp[b].end());
+    out_point.insert(out_point.end(), tq[b].begin(), tq[b].end());
   }
 }
 
