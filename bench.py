@@ -7,10 +7,16 @@ max_size 256 (cuspatial_gb300.datasets.precision_at_scale).
 
 A step is one pass of the join over the resident point set:
 polygon_bounding_boxes + join_quadtree_and_bounding_boxes +
-quadtree_point_in_polygon (float32 filter + float64 refine).  The quadtree is
-built once and reported separately (build_ms).  value = points / step time;
-e2e repeats the whole chain through the public API from pinned host buffers
-(host->device copies, quadtree build, join, device->host copy of the pairs).
+quadtree_point_in_polygon (float32 filter + float64 refine).  The quadtree and
+the points in its order are built once and reported separately (build_ms).
+value = points / step time; e2e repeats the whole chain through the public
+API from pinned host buffers (host->device copies, quadtree build, join,
+device->host copy of the pairs), beside the host link's measured rates.
+
+The default run also measures the other configurations at their shapes
+(other_configs: the 1M-point plain drop-in case against the CPU oracle in
+full, the nearest-linestring join, the serving loop and the batched form),
+each a short run; --no-configs skips them, --workload runs one alone.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -44,6 +50,8 @@ def parse_args():
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the other configurations' sub-results in the default run")
     ap.add_argument("--workload", choices=["precision", "batched", "serving", "nearest",
                                            "unindexed"],
                     default="precision",
@@ -56,6 +64,13 @@ def parse_args():
     ap.add_argument("--rate", type=float, default=2000.0)
     ap.add_argument("--streams", type=int, default=4)
     ap.add_argument("--nearest-points", type=int, default=50_000_000)
+    ap.add_argument("--nearest-linestrings", type=int, default=200_000)
+    ap.add_argument("--nearest-extent", type=float, default=10000.0,
+                    help="side of the nearest-linestring domain (a smaller side with "
+                         "proportionally fewer points and linestrings keeps the density)")
+    ap.add_argument("--nearest-plain-every", type=int, default=64,
+                    help="time the plain float64 nearest method on every k-th leaf "
+                         "(0: skip)")
     ap.add_argument("--instances", type=int, default=4096)
     ap.add_argument("--sides", type=int, default=100,
                     help="polygon sides of the unindexed workload (reference: 4, 10, 100)")
@@ -422,6 +437,7 @@ def run_ours(args, dist):
         kern[name] = (ms.value, int(cnt.value))
     lib.cspt_profile_enable(0)
     refined = cs.last_refined_count()
+    edge_free = cs.last_edge_free_pairs()
 
     ms_per_step = total_ms / args.steps
     value = n * args.gpus / (ms_per_step / 1e3)
@@ -577,6 +593,7 @@ def run_ours(args, dist):
                    "parallelism": "replicas" if args.gpus > 1 else "single GPU"},
         "pairs": K, "candidates": cand, "hits": M,
         "refined_candidates": refined, "refine_fraction": refined / max(cand, 1),
+        "edge_free_pairs": edge_free,
         "build_ms": min(build_ms), "tree_only_build_ms": min(tree_ms),
         "generation_s": gen_s,
         "kernels_ms_per_step": {k: v[0] / max(args.steps, 1) for k, v in kern.items()},
@@ -585,8 +602,7 @@ def run_ours(args, dist):
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
         "clocks": clock_info,
     }
-    if dist.rank == 0:
-        print(json.dumps(line), flush=True)
+    return line
 
 
 # --------------------------------------------------------------------------
@@ -639,7 +655,122 @@ def run_reference(args, dist):
                 "d2h_bytes_per_step": 0},
         "build_s": build_s,
     }
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def run_plain_small(args, dist):
+    """The plain drop-in configuration: 1,000,000 uniform points in
+    [0,1000)^2, 256 star polygons (8-64 vertices), max_depth 7, scale
+    1000/128, max_size 128.  A step is polygon_bounding_boxes +
+    join_quadtree_and_bounding_boxes + quadtree_point_in_polygon; the whole
+    configuration is small enough for the CPU oracle to run in full, so its
+    pairs are compared with the GPU's exactly and its time is measured, not
+    scaled."""
+    import torch
+
+    import cuspatial_gb300 as cs
+    from cuspatial_gb300 import datasets
+    from oracle import oracle as O
+
+    torch.cuda.set_device(dist.local)
+    dist.init("nccl")
+    w = datasets.plain_small()
+    P = w.polygons
+    n = len(w.x)
+    pts = cs.GeoSeries.from_points(w.x, w.y)
+    polys = cs.GeoSeries.from_polygons_xy(polygons_xy(P), P.ring_offset, P.part_offset,
+                                          P.geometry_offset)
+    stream = torch.cuda.current_stream()
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    pi, tree, xy = cs.quadtree_on_points_ordered(pts, w.x_min, w.x_max, w.y_min, w.y_max,
+                                                 w.scale, w.max_depth, w.max_size)
+
+    def step(method):
+        bb = cs.polygon_bounding_boxes(polys)
+        pairs = cs.join_quadtree_and_bounding_boxes(tree, bb, w.x_min, w.x_max, w.y_min,
+                                                    w.y_max, w.scale, w.max_depth)
+        return cs.quadtree_point_in_polygon(pairs, tree, pi, pts, polys, method=method,
+                                            ordered_points=xy)
+
+    res, times = {}, {}
+    for method in ("exact", "filtered"):
+        for _ in range(max(3, args.warmup)):
+            res[method] = step(method)
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(max(10, args.steps)):
+            a, b = ev(), ev()
+            a.record(stream)
+            step(method)
+            b.record(stream)
+            ms.append((a, b))
+        torch.cuda.synchronize()
+        times[method] = [a.elapsed_time(b) for a, b in ms]
+    # the CPU oracle on the whole configuration (tree, boxes, join, PiP)
+    t0 = time.perf_counter()
+    opi, ot = O.quadtree_on_points(w.x, w.y, w.x_min, w.x_max, w.y_min, w.y_max, w.scale,
+                                   w.max_depth, w.max_size)
+    t1 = time.perf_counter()
+    obb = O.polygon_bounding_boxes(P.part_offset, P.ring_offset, P.x, P.y)
+    oj = O.join_quadtree_and_bounding_boxes(ot, obb, w.x_min, w.x_max, w.y_min, w.y_max,
+                                            w.scale, w.max_depth)
+    orr = O.quadtree_point_in_polygon(oj, ot, opi, w.x, w.y, P.part_offset, P.ring_offset,
+                                      P.x, P.y)
+    t2 = time.perf_counter()
+    exact_ms = statistics.mean(times["exact"])
+    filt_ms = statistics.mean(times["filtered"])
+    same = {m: bool(np.array_equal(r["polygon_index"].cpu().numpy().view(np.uint32),
+                                   orr["polygon_index"]) and
+                    np.array_equal(r["point_index"].cpu().numpy().view(np.uint32),
+                                   orr["point_index"])) for m, r in res.items()}
+    return {
+        "workload": "plain_small: 1,000,000 uniform points in [0,1000)^2, 256 star polygons "
+                    "(8-64 vertices), max_depth 7, scale 1000/128, max_size 128",
+        "metric": METRIC, "unit": "points/s", "steps": max(10, args.steps),
+        "value": n / (exact_ms / 1e3), "method": "exact (the drop-in)", "ms_per_step": exact_ms,
+        "p50_ms": percentile(times["exact"], 0.5), "p99_ms": percentile(times["exact"], 0.99),
+        "filtered": {"points_per_s": n / (filt_ms / 1e3), "ms_per_step": filt_ms,
+                     "p99_ms": percentile(times["filtered"], 0.99)},
+        "pairs_identical_to_oracle": same, "pairs": int(len(oj["bbox_offset"])),
+        "hits": int(len(orr["polygon_index"])),
+        "cpu_baseline": {"value": n / (t2 - t1), "unit": "points/s", "cores": O.num_threads(),
+                         "kind": "port", "sample": "the whole configuration: boxes, join and "
+                                                   "point-in-polygon timed (tree build %.2f s "
+                                                   "apart)" % (t1 - t0)},
+    }
+
+
+def other_configs(args, dist):
+    """The other configurations at their shapes, each a short run whose
+    result rides in the default line (an error is recorded, not raised):
+    the plain drop-in case (1M points), the nearest-linestring join (50M
+    points, 200k linestrings), the serving form (250k resident polygons,
+    4000 Poisson requests) and the batched form (4096 instances)."""
+    import argparse
+    import gc
+    out = {}
+    runs = [
+        ("plain_small", run_plain_small, {}),
+        ("nearest", run_nearest, {"steps": 3, "warmup": 1, "nearest_plain_every": 0,
+                                  "nearest_points": 50_000_000,
+                                  "nearest_linestrings": 200_000, "nearest_extent": 10000.0}),
+        ("serving", run_serving, {}),
+        ("batched", run_batched, {"steps": 5, "warmup": 2, "plain_steps": 1,
+                                  "single_sample": 8, "e2e_steps": 1}),
+    ]
+    for name, fn, over in runs:
+        sub = argparse.Namespace(**vars(args))
+        for k, v in over.items():
+            setattr(sub, k, v)
+        t0 = time.time()
+        try:
+            out[name] = fn(sub, dist)
+        except Exception as e:  # noqa: BLE001 - recorded in the line
+            out[name] = {"error": "%s: %s" % (type(e).__name__, e)}
+        if isinstance(out[name], dict):
+            out[name]["wall_s"] = time.time() - t0
+        gc.collect()
+    return out
 
 
 def run_batched(args, dist):
@@ -838,8 +969,7 @@ def run_batched(args, dist):
         "e2e": e2e, "gpu_launches": launches, "clocks": clock_info, "generation_s": gen_s,
     }
     pl.close()
-    if dist.rank == 0:
-        print(json.dumps(line), flush=True)
+    return line
 
 
 def run_serving(args, dist):
@@ -923,8 +1053,7 @@ def run_serving(args, dist):
         "gpu_launches": f["launches_live"], "clocks": f["clocks"], "generation_s": gen_s,
     }
     pset.close()
-    if dist.rank == 0:
-        print(json.dumps(line), flush=True)
+    return line
 
 
 def run_nearest(args, dist):
@@ -932,10 +1061,12 @@ def run_nearest(args, dist):
     random-walk linestrings (2-256 segments); a step is
     linestring_bounding_boxes (radius 25) + join_quadtree_and_bounding_boxes +
     quadtree_point_to_nearest_linestring with the float32 filter.  The plain
-    float64 method is timed on the pairs of every 64th leaf (about 5e11
-    float64 segment distances per full step would take hours on this
+    float64 method is timed on the pairs of every k-th leaf (about 5e11
+    float64 segment distances per full step would take minutes on this
     part's float64 unit) and scaled by the candidate fraction; its rows are
-    compared with the filtered rows of the same points."""
+    compared with the filtered rows of the same points.  The CPU oracle runs
+    on every 4096th leaf: its rows are compared with the GPU's and its time,
+    scaled by candidates, is the CPU baseline."""
     import torch
 
     import cuspatial_gb300 as cs
@@ -945,11 +1076,17 @@ def run_nearest(args, dist):
     dist.init("nccl")
     lib = _lib.load()
     lib.cspt_launch_count.restype = ctypes.c_uint64
+    lib.cspt_profile_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(ctypes.c_uint64)]
+    lib.cspt_profile_enable.argtypes = [ctypes.c_int]
     t0 = time.time()
-    w = datasets.nearest_linestring(n_points=args.nearest_points)
+    w = datasets.nearest_linestring(n_points=args.nearest_points,
+                                    n_linestrings=args.nearest_linestrings,
+                                    extent=args.nearest_extent)
     gen_s = time.time() - t0
     L = w.linestrings
     n = len(w.x)
+    nls = len(L.part_offset) - 1
     pts = cs.GeoSeries.from_points(w.x, w.y)
     xy = np.empty(2 * len(L.x))
     xy[0::2], xy[1::2] = L.x, L.y
@@ -958,9 +1095,8 @@ def run_nearest(args, dist):
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
     a, b = ev(), ev()
     a.record(stream)
-    pi, tree = cs.quadtree_on_points(pts, w.x_min, w.x_max, w.y_min, w.y_max, w.scale,
-                                     w.max_depth, w.max_size)
-    oxy = cs.points_in_quadtree_order(pi, pts)
+    pi, tree, oxy = cs.quadtree_on_points_ordered(pts, w.x_min, w.x_max, w.y_min, w.y_max,
+                                                  w.scale, w.max_depth, w.max_size)
     b.record(stream)
     b.synchronize()
     build_ms = a.elapsed_time(b)
@@ -978,6 +1114,7 @@ def run_nearest(args, dist):
     torch.cuda.synchronize()
     clocks = ClockSampler(dist.local)
     clocks.start()
+    lib.cspt_profile_enable(1)
     l0 = lib.cspt_launch_count()
     times = []
     for _ in range(args.steps):
@@ -987,34 +1124,47 @@ def run_nearest(args, dist):
         b.record(stream)
         times.append((a, b))
     torch.cuda.synchronize()
+    kern = {}
+    for name in ("bounding_boxes", "join_count", "join_write", "nearest_index", "leaf_frames",
+                 "nearest"):
+        kms, cnt = ctypes.c_double(), ctypes.c_uint64()
+        lib.cspt_profile_read(name.encode(), ctypes.byref(kms), ctypes.byref(cnt))
+        kern[name] = kms.value / max(args.steps, 1)
+    lib.cspt_profile_enable(0)
     launches = int(lib.cspt_launch_count() - l0)
     clock_info = clocks.stop()
     ms = [x.elapsed_time(y) for x, y in times]
     f_ms = dist.max(statistics.mean(ms))
     paths = cs.last_nearest_stats()
 
-    # plain float64 on every 64th leaf's pairs
+    # plain float64 on every k-th leaf's pairs
     pq = pairs["quad_offset"].long()
-    sel = (pq % 64) == 0
-    sub = {"bbox_offset": pairs["bbox_offset"][sel].contiguous(),
-           "quad_offset": pairs["quad_offset"][sel].contiguous()}
     qlen = tree["length"].long()
     cand_all = int(qlen[pq].sum().item())
-    cand_sub = int(qlen[pq[sel]].sum().item())
-    a, b = ev(), ev()
-    a.record(stream)
-    ex = cs.quadtree_point_to_nearest_linestring(sub, tree, pi, pts, lines, method="exact")
-    b.record(stream)
-    b.synchronize()
-    sub_ms = a.elapsed_time(b)
-    fi = cs.quadtree_point_to_nearest_linestring(sub, tree, pi, pts, lines, method="filtered")
-    same = bool(torch.equal(fi["linestring_index"], ex["linestring_index"]) and
-                torch.equal(fi["distance"], ex["distance"]) and
-                torch.equal(fi["point_index"], ex["point_index"]))
-    plain_ms = sub_ms * cand_all / max(cand_sub, 1)
+    plain = None
+    if args.nearest_plain_every > 0:
+        sel = (pq % args.nearest_plain_every) == 0
+        sub = {"bbox_offset": pairs["bbox_offset"][sel].contiguous(),
+               "quad_offset": pairs["quad_offset"][sel].contiguous()}
+        cand_sub = int(qlen[pq[sel]].sum().item())
+        a, b = ev(), ev()
+        a.record(stream)
+        ex = cs.quadtree_point_to_nearest_linestring(sub, tree, pi, pts, lines, method="exact")
+        b.record(stream)
+        b.synchronize()
+        sub_ms = a.elapsed_time(b)
+        fi = cs.quadtree_point_to_nearest_linestring(sub, tree, pi, pts, lines,
+                                                     method="filtered")
+        same = bool(torch.equal(fi["linestring_index"], ex["linestring_index"]) and
+                    torch.equal(fi["distance"], ex["distance"]) and
+                    torch.equal(fi["point_index"], ex["point_index"]))
+        plain_ms = sub_ms * cand_all / max(cand_sub, 1)
+        plain = {"leaves": "every %dth" % args.nearest_plain_every,
+                 "candidate_fraction": cand_sub / max(cand_all, 1), "sample_ms": sub_ms,
+                 "ms_per_step_scaled": plain_ms, "rows_identical_to_filtered": same}
 
     # the oracle on the pairs of every 4096th leaf (rows of those leaves' points)
-    oracle_check = None
+    oracle_check = cpu = None
     if dist.rank == 0 and not args.no_cpu:
         from oracle import oracle as O
         osel = (pq % 4096) == 0
@@ -1030,34 +1180,52 @@ def run_nearest(args, dist):
         rows = orr["linestring_index"] != 0xFFFFFFFF
         g_ls = res["linestring_index"].cpu().numpy().view(np.uint32)
         g_d = res["distance"].cpu().numpy()
+        o_cand = int(qlen[pq[osel]].sum().item())
         oracle_check = {"leaves": "every 4096th", "rows": int(rows.sum()),
                         "oracle_s": o_s, "cores": O.num_threads(),
+                        "candidate_fraction": o_cand / max(cand_all, 1),
                         "rows_identical": bool(np.array_equal(g_ls[rows],
                                                               orr["linestring_index"][rows]) and
                                                np.array_equal(g_d[rows], orr["distance"][rows]))}
-    line = {
+        full_s = o_s * cand_all / max(o_cand, 1)
+        cpu = {"value": n / full_s, "unit": "points/s", "cores": O.num_threads(),
+               "kind": "port",
+               "sample": "the oracle on the pairs of every 4096th leaf (%.3f%% of candidates, "
+                         "%d rows): %.2f s, scaled by candidates to %.0f s for the full join"
+                         % (100.0 * o_cand / max(cand_all, 1), int(rows.sum()), o_s, full_s),
+               "sample_s": o_s}
+    # roofline of the nearest kernel: 20 N + 16 V + 32 L + 8 K + 16 N (points
+    # and their index, linestring vertices and boxes, pairs, rows)
+    nb_alg = 20 * n + 16 * len(L.x) + 32 * nls + 8 * int(pairs["bbox_offset"].numel()) + 16 * n
+    peak, peak_kind = measured_peak_hbm()
+    nk_ms = kern.get("nearest") or 0.0
+    achieved = nb_alg / (nk_ms / 1e3) / 1e9 if nk_ms else None
+    roofline = {"bound": "hbm", "kernel": "nearest_filtered_kernel", "achieved": achieved,
+                "peak": peak, "unit": "GB/s", "frac": achieved / peak if achieved else None,
+                "peak_source": peak_kind, "algorithmic_bytes_per_launch": nb_alg,
+                "kernel_ms_per_launch": nk_ms,
+                "note": "bound by instruction issue and the float64 pipe, not HBM "
+                        "(profiles/nearest_filtered_kernel_5M_points_20k_linestrings.md)"}
+    return {
         "metric": METRIC, "workload": "nearest", "value": n * args.gpus / (f_ms / 1e3),
         "unit": "points/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": f_ms, "p50_ms": percentile(ms, 0.5), "p99_ms": percentile(ms, 0.99),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded numpy PCG64; shapes of the nearest-linestring config)",
-        "config": {"workload": "nearest_linestring: %d uniform points, 200k random-walk "
-                               "linestrings (2-256 segments), max_depth 14, max_size 256, "
-                               "expansion radius 25" % n,
-                   "points": n, "linestrings": len(L.part_offset) - 1, "vertices": len(L.x),
+        "config": {"workload": "nearest_linestring: %d uniform points in [0,%g)^2, %d "
+                               "random-walk linestrings (2-256 segments), max_depth 14, "
+                               "max_size 256, expansion radius 25" % (n, args.nearest_extent, nls),
+                   "points": n, "linestrings": nls, "vertices": len(L.x),
                    "step": "linestring_bounding_boxes + join_quadtree_and_bounding_boxes + "
-                           "quadtree_point_to_nearest_linestring (float32 filter)"},
+                           "quadtree_point_to_nearest_linestring (float32 filter, points in "
+                           "quadtree order built with the tree)"},
         "pairs": int(pairs["bbox_offset"].numel()), "candidates": cand_all,
-        "build_ms": build_ms,
-        "plain_fp64_sampled": {"leaves": "every 64th", "candidate_fraction": cand_sub /
-                               max(cand_all, 1), "sample_ms": sub_ms,
-                               "ms_per_step_scaled": plain_ms,
-                               "rows_identical_to_filtered": same},
-        "speedup_vs_plain": plain_ms / f_ms, "gpu_launches": launches, "clocks": clock_info,
-        "generation_s": gen_s, "paths": paths, "oracle_sample": oracle_check,
+        "build_ms": build_ms, "plain_fp64_sampled": plain,
+        "speedup_vs_plain": plain["ms_per_step_scaled"] / f_ms if plain else None,
+        "gpu_launches": launches, "clocks": clock_info, "generation_s": gen_s,
+        "paths": paths, "oracle_sample": oracle_check, "kernels_ms_per_step": kern,
+        "roofline": roofline, "cpu_baseline": cpu,
     }
-    if dist.rank == 0:
-        print(json.dumps(line), flush=True)
 
 
 def run_unindexed(args, dist):
@@ -1185,25 +1353,28 @@ def run_unindexed(args, dist):
                          "sample": "first %d points, all 31 polygons" % k},
         "gpu_launches": launches, "clocks": clock_info,
     }
-    if dist.rank == 0:
-        print(json.dumps(line), flush=True)
+    return line
 
 
 def main():
     args = parse_args()
     dist = Dist()
     if args.impl == "reference":
-        run_reference(args, dist)
+        line = run_reference(args, dist)
     elif args.workload == "batched":
-        run_batched(args, dist)
+        line = run_batched(args, dist)
     elif args.workload == "serving":
-        run_serving(args, dist)
+        line = run_serving(args, dist)
     elif args.workload == "nearest":
-        run_nearest(args, dist)
+        line = run_nearest(args, dist)
     elif args.workload == "unindexed":
-        run_unindexed(args, dist)
+        line = run_unindexed(args, dist)
     else:
-        run_ours(args, dist)
+        line = run_ours(args, dist)
+        if not args.no_configs:
+            line["other_configs"] = other_configs(args, dist)
+    if line is not None and dist.rank == 0:
+        print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

@@ -8,7 +8,8 @@ the pairwise point-linestring distance and nearest points;
 they run hand-written CUDA kernels in libcuspatial_gb300.so through its C ABI.
 """
 
-from .api import (HostRowsTooFew, join_quadtree_and_bounding_boxes, last_nearest_stats,
+from .api import (HostRowsTooFew, join_quadtree_and_bounding_boxes, last_edge_free_pairs,
+                  last_nearest_stats,
                   last_refined_count,
                   linestring_bounding_boxes, pairwise_point_in_polygon,
                   pairwise_point_linestring_distance, pairwise_point_linestring_nearest_points,
@@ -25,6 +26,7 @@ __all__ = [
     "Table",
     "contains_properly",
     "join_quadtree_and_bounding_boxes",
+    "last_edge_free_pairs",
     "last_nearest_stats",
     "last_refined_count",
     "linestring_bounding_boxes",

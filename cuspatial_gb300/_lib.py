@@ -85,7 +85,9 @@ def _declare(lib):
     lib.cspt_last_error_message.restype = ctypes.c_char_p
     lib.cspt_version.restype = ctypes.c_char_p
     lib.cspt_last_refined_count.restype = ctypes.c_uint64
+    lib.cspt_last_edge_free_pairs.restype = ctypes.c_uint64
     lib.cspt_last_nearest_stats.argtypes = [ctypes.POINTER(ctypes.c_uint64),
+                                            ctypes.POINTER(ctypes.c_uint64),
                                             ctypes.POINTER(ctypes.c_uint64)]
     lib.cspt_last_nearest_stats.restype = None
     lib.cspt_free.argtypes = [ctypes.POINTER(CsptAllocator), _vp, _sz, _vp]

@@ -563,11 +563,19 @@ def last_refined_count():
     return int(_lib.load().cspt_last_refined_count())
 
 
+def last_edge_free_pairs():
+    """(polygon, quadrant) pairs the last filtered PiP call decided whole
+    (no edge near the quadrant's points)."""
+    return int(_lib.load().cspt_last_edge_free_pairs())
+
+
 def last_nearest_stats():
     """Paths of the last filtered float64 nearest-linestring call on this
     thread: {"points_folded_whole": points folded over every candidate in
     float64, "groups_scanned": quadrant groups scanned point by point instead
-    of through their segment list}."""
-    a, b = ctypes.c_uint64(), ctypes.c_uint64()
-    _lib.load().cspt_last_nearest_stats(ctypes.byref(a), ctypes.byref(b))
-    return {"points_folded_whole": int(a.value), "groups_scanned": int(b.value)}
+    of through their segment list, "float64_segments": listed segments whose
+    distance was evaluated in float64}."""
+    a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+    _lib.load().cspt_last_nearest_stats(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+    return {"points_folded_whole": int(a.value), "groups_scanned": int(b.value),
+            "float64_segments": int(c.value)}

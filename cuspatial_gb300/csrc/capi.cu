@@ -24,6 +24,8 @@ void quadtree_on_points_from_host(void const* host_x, void const* host_y, void* 
                                   void* ordered = nullptr);
 uint64_t& last_fallbacks();
 uint64_t& last_group_scans();
+uint64_t& last_f64_segments();
+uint64_t& last_edge_free_pairs();
 void points_in_quadtree_order(uint32_t const* point_indices, size_t n, void const* x,
                               void const* y, size_t npts, cspt_dtype dtype, void* out_xy,
                               cudaStream_t s);
@@ -274,10 +276,14 @@ int cspt_profile_read(const char* name, double* total_ms, uint64_t* launches)
 // call on this thread (diagnostic; not part of the reference interface).
 uint64_t cspt_last_refined_count(void) { return t_last_refined; }
 
-void cspt_last_nearest_stats(uint64_t* points_folded_whole, uint64_t* groups_scanned)
+uint64_t cspt_last_edge_free_pairs(void) { return last_edge_free_pairs(); }
+
+void cspt_last_nearest_stats(uint64_t* points_folded_whole, uint64_t* groups_scanned,
+                             uint64_t* float64_segments)
 {
   if (points_folded_whole) *points_folded_whole = last_fallbacks();
   if (groups_scanned) *groups_scanned = last_group_scans();
+  if (float64_segments) *float64_segments = last_f64_segments();
 }
 
 void cspt_free(const cspt_allocator* mr, void* ptr, size_t bytes, void* stream)

@@ -20,6 +20,8 @@
 // with a forward error bound; only segments whose lower bound can still beat
 // the best upper bound of the point are evaluated with the float64
 // expression, so the winner and its distance are the exact ones.
+#include <memory>
+
 #include "common.cuh"
 #include "leaf_frame.cuh"
 #include "scan.cuh"
@@ -36,6 +38,11 @@ uint64_t& last_group_scans()
   static thread_local uint64_t n = 0;
   return n;
 }
+uint64_t& last_f64_segments()
+{
+  static thread_local uint64_t n = 0;
+  return n;
+}
 
 namespace {
 
@@ -45,6 +52,8 @@ __device__ inline T dot_fma(T ax, T ay, T bx, T by)
   return fma_rn(ax, bx, ay * by);
 }
 
+// (the quotient r is only formed where the result depends on it: when
+// d3 <= 0 the reference's expression yields fmin(d0, d1) whatever r is)
 template <typename T>
 __device__ inline T segment_dist2(T px, T py, T ax, T ay, T bx, T by)
 {
@@ -53,10 +62,11 @@ __device__ inline T segment_dist2(T px, T py, T ax, T ay, T bx, T by)
   T const d0  = dot_fma(v1x, v1y, v1x, v1y);
   T const d1  = dot_fma(v2x, v2y, v2x, v2y);
   T const ex = bx - ax, ey = by - ay;
-  T const d2  = dot_fma(ex, ey, ex, ey);
   T const d3  = dot_fma(px - ax, py - ay, ex, ey);
-  T const r   = d3 * d3 / d2;
-  return (d3 <= T{0} || r >= d2) ? fmin(d0, d1) : d0 - r;
+  if (d3 <= T{0}) return fmin(d0, d1);
+  T const d2 = dot_fma(ex, ey, ex, ey);
+  T const r  = d3 * d3 / d2;
+  return r >= d2 ? fmin(d0, d1) : d0 - r;
 }
 
 // point_linestring_distance.cuh:32-51
@@ -145,6 +155,18 @@ __global__ void __launch_bounds__(256)
 // ---------------------------------------------------------------------------
 constexpr int kSegChunk = 8;  // segments per pruning box
 
+// Per linestring, what the segment listing needs in one 64-byte record.
+struct __align__(16) LsRec {
+  long long aix, aiy;  // anchor in grid steps
+  float4 box;          // box of its float32 segments, anchor frame
+  float maxoff;        // largest |float32 offset|
+  uint32_t v0, nseg;   // first vertex, segments
+  uint32_t cb;         // first chunk
+  uint32_t exact;      // non-finite coordinates: exact path only
+  uint32_t pad[3];
+};
+static_assert(sizeof(LsRec) == 64, "one 64-byte record per linestring");
+
 struct LinestringIndexView {
   long long const* aix;  // anchors in grid steps
   long long const* aiy;
@@ -153,6 +175,7 @@ struct LinestringIndexView {
   float4 const* chunk_box;  // (minx, miny, maxx, maxy) of 8 segments, anchor frame
   float4 const* seg32;      // per segment start vertex: (ax, ay, bx, by), anchor frame
   uint8_t const* exact;     // non-finite coordinates: exact path only
+  LsRec const* rec;
 };
 
 // per linestring: box, anchor, float32 segments, chunk boxes (one warp each)
@@ -221,7 +244,8 @@ __global__ void __launch_bounds__(256)
   ls_fill_kernel(uint32_t const* __restrict__ lso, size_t nls, double const* __restrict__ lx,
                  double const* __restrict__ ly, double4_16a const* __restrict__ box,
                  double const* __restrict__ gridp, uint32_t const* __restrict__ chunk_base,
-                 long long* aix, long long* aiy, float* maxoff, float4* chunk_box, float4* seg32)
+                 uint8_t const* __restrict__ exact, long long* aix, long long* aiy,
+                 float* maxoff, float4* chunk_box, float4* seg32, LsRec* rec)
 {
   int const lane      = threadIdx.x & 31;
   size_t const nwarps = (static_cast<size_t>(gridDim.x) * blockDim.x) >> 5;
@@ -239,6 +263,7 @@ __global__ void __launch_bounds__(256)
     uint32_t const nch  = (nseg + kSegChunk - 1) / kSegChunk;
     uint32_t const cb   = chunk_base[l];
     float m             = 0.0f;
+    float4 lbx          = make_float4(INFINITY, INFINITY, -INFINITY, -INFINITY);
     // lane per chunk
     for (uint32_t c = lane; c < nch; c += 32) {
       float4 cbx = make_float4(INFINITY, INFINITY, -INFINITY, -INFINITY);
@@ -258,12 +283,28 @@ __global__ void __launch_bounds__(256)
         m = fmaxf(m, fmaxf(fmaxf(fabsf(e.x), fabsf(e.y)), fmaxf(fabsf(e.z), fabsf(e.w))));
       }
       chunk_box[cb + c] = cbx;
+      lbx = make_float4(fminf(lbx.x, cbx.x), fminf(lbx.y, cbx.y), fmaxf(lbx.z, cbx.z),
+                        fmaxf(lbx.w, cbx.w));
     }
-    m = warp_max(m);
+    m     = warp_max(m);
+    lbx.x = warp_min(lbx.x);
+    lbx.y = warp_min(lbx.y);
+    lbx.z = warp_max(lbx.z);
+    lbx.w = warp_max(lbx.w);
     if (lane == 0) {
       aix[l]    = static_cast<long long>(rx);
       aiy[l]    = static_cast<long long>(ry);
       maxoff[l] = m;
+      LsRec r{};
+      r.aix    = static_cast<long long>(rx);
+      r.aiy    = static_cast<long long>(ry);
+      r.box    = lbx;
+      r.maxoff = m;
+      r.v0     = v0;
+      r.nseg   = nseg;
+      r.cb     = cb;
+      r.exact  = exact[l];
+      rec[l]   = r;
     }
   }
 }
@@ -465,79 +506,139 @@ __device__ inline void nearest_point_scan(NearestArgs const& a, uint32_t k0, uin
 
 // The group's segment list (per warp, in shared memory): the candidate
 // segments whose box lies within a radius of the leaf's point box, each in
-// the leaf's float32 frame, with its global start vertex and its pair (the
-// pair gives the linestring and the fold order).
+// the leaf's float32 frame, with its global start vertex and its
+// linestring, in no particular order.
 constexpr int kNearWarps    = 4;    // warps per block
 constexpr uint32_t kNearCap = 384;  // listed segments per warp
 struct NearList {
   float4 e[kNearCap];
   uint32_t seg[kNearCap];
-  uint32_t pair[kNearCap];
+  uint32_t lid[kNearCap];
 };
 constexpr uint32_t kListOverflow = 0xFFFFFFFEu;  // more than kNearCap segments
 constexpr uint32_t kListFrame    = 0xFFFFFFFFu;  // a linestring outside the float32 frames
 
-// Lists, in pair order, the segments of the group's linestrings whose box
-// is within squared distance r2 of the leaf's point box (box-to-box lower
-// bound with the filter's margin tol, computed in each linestring's frame;
-// the leaf box maps into that frame monotonically, so it holds every point's
-// mapped offset and the bound is below each point's own box_lb).  Chunk
-// boxes are tested first; four near chunks are expanded per round, eight
-// lanes per chunk, one segment each.  mg receives the largest magnitude the
-// listed segments involve (their linestrings' offsets and their leaf-frame
-// coordinates).  Returns the count, kListOverflow or kListFrame.
+// Lists the segments of the group's linestrings whose box is within squared
+// distance r2 of the leaf's point box (box-to-box lower bound with the
+// filter's margin tol, computed in each linestring's frame; the leaf box
+// maps into that frame monotonically, so it holds every point's mapped
+// offset and the bound is below each point's own box_lb).  Three filters,
+// each on every lane: 32 candidate linestrings at a time, each lane loading
+// one linestring's 64-byte record and testing its whole box; the chunks of
+// the linestrings that pass, flattened over the lanes (a lane finds its
+// chunk's linestring by a binary search over the lanes' running chunk
+// counts); four near chunks at a time, eight lanes per chunk, one segment
+// each.  Listed segments are stored in the leaf frame, rounded once from the
+// float64 vertices; mg receives the largest magnitude of the leaf frame (its
+// points' and the listed segments' offsets), which bounds their errors.
+// Returns the count, kListOverflow or kListFrame.
 __device__ uint32_t list_segments(NearestArgs const& a, NearList& L, uint32_t k0, uint32_t k1,
                                   LeafFrame const& lf, float r2, float& mg)
 {
   LinestringIndexView const& li = a.li;
-  int const lane    = threadIdx.x & 31;
-  unsigned const lt = (1u << lane) - 1u;
-  uint32_t n        = 0;
-  float m           = lf.m;
-  for (uint32_t k = k0; k < k1; ++k) {
-    uint32_t const lid = a.pair_ls[k];
-    if (lid >= a.nls) continue;
-    long long const dix = li.aix[lid] - lf.ix, diy = li.aiy[lid] - lf.iy;
-    if (li.exact[lid] || dix <= -16777216LL || dix >= 16777216LL || diy <= -16777216LL ||
-        diy >= 16777216LL)
-      return kListFrame;
-    float const sx  = static_cast<float>(static_cast<int>(dix)) * a.gf;
-    float const sy  = static_cast<float>(static_cast<int>(diy)) * a.gf;
-    float4 const lb = make_float4(lf.uxmin - sx, lf.uymin - sy, lf.uxmax - sx, lf.uymax - sy);
-    float const mk  = fmaxf(fmaxf(li.maxoff[lid], lf.m),
-                            fmaxf(fmaxf(fabsf(lb.x), fabsf(lb.y)), fmaxf(fabsf(lb.z), fabsf(lb.w))));
-    float const tol = 4.76837158203125e-07f * mk;
-    uint32_t const v0 = a.lso[lid], v1 = a.lso[lid + 1];
-    uint32_t const nseg = v1 > v0 + 1 ? v1 - v0 - 1 : 0;
-    uint32_t const nch  = (nseg + kSegChunk - 1) / kSegChunk;
-    uint32_t const cb   = li.chunk_base[lid];
-    for (uint32_t c0 = 0; c0 < nch; c0 += 32) {
-      bool const near = c0 + lane < nch && boxbox_lb(lb, li.chunk_box[cb + c0 + lane], tol) <= r2;
-      unsigned cm     = __ballot_sync(0xFFFFFFFFu, near);
+  constexpr unsigned kAll       = 0xFFFFFFFFu;
+  int const lane                = threadIdx.x & 31;
+  unsigned const lt             = (1u << lane) - 1u;
+  uint32_t n                    = 0;
+  float m                       = lf.m;
+  for (uint32_t kb = k0; kb < k1; kb += 32) {
+    // this lane's linestring: its frame relative to the leaf and whether its
+    // whole box is near the leaf box
+    uint32_t const k = kb + static_cast<uint32_t>(lane);
+    uint32_t lid     = 0;
+    bool valid       = k < k1;
+    if (valid) {
+      lid   = a.pair_ls[k];
+      valid = lid < a.nls;
+    }
+    LsRec r{};
+    if (valid) r = li.rec[lid];
+    bool bad = false;
+    float4 lb{};
+    float tol    = 0.0f;
+    uint32_t nch = 0;
+    if (valid) {
+      long long const dix = r.aix - lf.ix, diy = r.aiy - lf.iy;
+      bad = r.exact || dix <= -16777216LL || dix >= 16777216LL || diy <= -16777216LL ||
+            diy >= 16777216LL;
+      if (!bad) {
+        float const sx = static_cast<float>(static_cast<int>(dix)) * a.gf;
+        float const sy = static_cast<float>(static_cast<int>(diy)) * a.gf;
+        lb             = make_float4(lf.uxmin - sx, lf.uymin - sy, lf.uxmax - sx, lf.uymax - sy);
+        float const mk = fmaxf(fmaxf(r.maxoff, lf.m), fmaxf(fmaxf(fabsf(lb.x), fabsf(lb.y)),
+                                                            fmaxf(fabsf(lb.z), fabsf(lb.w))));
+        tol            = 4.76837158203125e-07f * mk;
+        if (boxbox_lb(lb, r.box, tol) <= r2) nch = (r.nseg + kSegChunk - 1) / kSegChunk;
+      }
+    }
+    if (__any_sync(kAll, bad)) return kListFrame;
+    // running chunk counts over the lanes
+    uint32_t incl = nch;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t const t = __shfl_up_sync(kAll, incl, o);
+      if (lane >= o) incl += t;
+    }
+    uint32_t const total = __shfl_sync(kAll, incl, 31);
+    for (uint32_t c0 = 0; c0 < total; c0 += 32) {
+      uint32_t const c = c0 + static_cast<uint32_t>(lane);
+      // the chunk's linestring: the first lane whose running count exceeds c
+      int ow = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        uint32_t const v = __shfl_sync(kAll, incl, ow + step - 1);
+        if (v <= c) ow += step;
+      }
+      ow = ow < 31 ? ow : 31;
+      float4 const olb     = make_float4(__shfl_sync(kAll, lb.x, ow), __shfl_sync(kAll, lb.y, ow),
+                                         __shfl_sync(kAll, lb.z, ow), __shfl_sync(kAll, lb.w, ow));
+      float const otol     = __shfl_sync(kAll, tol, ow);
+      uint32_t const olid  = __shfl_sync(kAll, lid, ow);
+      uint32_t const ov0   = __shfl_sync(kAll, r.v0, ow);
+      uint32_t const onseg = __shfl_sync(kAll, r.nseg, ow);
+      uint32_t const ocb   = __shfl_sync(kAll, r.cb, ow);
+      uint32_t const oinc  = __shfl_sync(kAll, incl, ow);
+      uint32_t const onch  = __shfl_sync(kAll, nch, ow);
+      uint32_t const ch    = c - (oinc - onch);  // the chunk within its linestring
+      bool const near      = c < total && boxbox_lb(olb, li.chunk_box[ocb + ch], otol) <= r2;
+      unsigned cm          = __ballot_sync(kAll, near);
       while (cm) {
-        // lane l expands the (l / 8)-th remaining near chunk, segment l % 8
+        // lane l expands the (l / 8)-th remaining near chunk, segment l % 8;
+        // that chunk's linestring fields are held by lane src
         unsigned mm = cm;
         for (int t = 0; t < (lane >> 3); ++t) mm &= mm - 1u;
-        uint32_t const ch = c0 + static_cast<uint32_t>(__ffs(mm) - 1);
-        uint32_t const sg = v0 + ch * kSegChunk + static_cast<uint32_t>(lane & 7);
-        bool keep         = false;
-        float4 e{};
-        if (mm && ch < nch && sg < v0 + nseg) {
-          e                = li.seg32[sg];
+        int const src       = mm ? __ffs(mm) - 1 : 0;
+        float4 const slb    = make_float4(__shfl_sync(kAll, olb.x, src), __shfl_sync(kAll, olb.y, src),
+                                          __shfl_sync(kAll, olb.z, src), __shfl_sync(kAll, olb.w, src));
+        float const stol    = __shfl_sync(kAll, otol, src);
+        uint32_t const slid = __shfl_sync(kAll, olid, src);
+        uint32_t const sv0  = __shfl_sync(kAll, ov0, src);
+        uint32_t const snsg = __shfl_sync(kAll, onseg, src);
+        uint32_t const sch  = __shfl_sync(kAll, ch, src);
+        uint32_t const sg   = sv0 + sch * kSegChunk + static_cast<uint32_t>(lane & 7);
+        bool keep           = false;
+        if (mm && sg < sv0 + snsg) {
+          float4 const e   = li.seg32[sg];
           float4 const sbx = make_float4(fminf(e.x, e.z), fminf(e.y, e.w), fmaxf(e.x, e.z),
                                          fmaxf(e.y, e.w));
-          keep             = boxbox_lb(lb, sbx, tol) <= r2;
+          keep             = boxbox_lb(slb, sbx, stol) <= r2;
         }
-        unsigned const km = __ballot_sync(0xFFFFFFFFu, keep);
+        unsigned const km = __ballot_sync(kAll, keep);
         if (n + __popc(km) > kNearCap) return kListOverflow;
         if (keep) {
+          // the segment in the leaf frame, rounded once from the float64
+          // vertices: its error is a float32 rounding of a leaf-local value,
+          // not of the linestring-frame offset (which grows with the
+          // linestring's extent), so the estimates' bound stays tight
           uint32_t const slot = n + __popc(km & lt);
-          float4 const el = make_float4(e.x + sx, e.y + sy, e.z + sx, e.w + sy);
-          L.e[slot]       = el;
-          L.seg[slot]     = sg;
-          L.pair[slot]    = k;
-          m = fmaxf(fmaxf(m, mk), fmaxf(fmaxf(fabsf(el.x), fabsf(el.y)),
-                                        fmaxf(fabsf(el.z), fabsf(el.w))));
+          float4 const el     = make_float4(static_cast<float>(a.lx[sg] - lf.ax),
+                                            static_cast<float>(a.ly[sg] - lf.ay),
+                                            static_cast<float>(a.lx[sg + 1] - lf.ax),
+                                            static_cast<float>(a.ly[sg + 1] - lf.ay));
+          L.e[slot]   = el;
+          L.seg[slot] = sg;
+          L.lid[slot] = slid;
+          m = fmaxf(m, fmaxf(fmaxf(fabsf(el.x), fabsf(el.y)), fmaxf(fabsf(el.z), fabsf(el.w))));
         }
         n += __popc(km);
         for (int t = 0; t < 4 && cm; ++t) cm &= cm - 1u;
@@ -591,13 +692,20 @@ __device__ float group_upper(NearestArgs const& a, uint32_t k0, uint32_t k1, Lea
 }
 
 // Smallest float32 upper bound (estimate + error) of the squared distance
-// from point offset (qx, qy) to the listed segments.
-__device__ inline float list_upper(NearList const& L, uint32_t n, float qx, float qy, float dm)
+// from point offset (qx, qy) to the listed segments.  A segment whose box is
+// farther than the running bound (box_lb, a lower bound of its distance) is
+// passed over without its estimate.
+__device__ inline float list_upper(NearList const& L, uint32_t n, float qx, float qy, float dm,
+                                   float tol)
 {
   float U = INFINITY;
   for (uint32_t t = 0; t < n; ++t) {
+    float4 const e  = L.e[t];
+    float4 const sb = make_float4(fminf(e.x, e.z), fminf(e.y, e.w), fmaxf(e.x, e.z),
+                                  fmaxf(e.y, e.w));
+    if (box_lb(qx, qy, sb, tol) > U) continue;
     float est, err;
-    seg_estimate(qx, qy, L.e[t], dm, est, err);
+    seg_estimate(qx, qy, e, dm, est, err);
     U = fminf(U, est + err);
   }
   return U;
@@ -613,10 +721,12 @@ __device__ inline float list_upper(NearList const& L, uint32_t n, float qx, floa
 //      a float64 distance above r2 >= U for every point, so it can neither
 //      win nor tie;
 //   4. per point: U over the list, then float64 (the reference's expression)
-//      on every listed segment whose estimate can reach U, folded per
-//      linestring in pair order with the reference's rule.  A point that
-//      reaches only zero distances (the winner is then the nearest non-zero
-//      candidate, possibly unlisted) or none is folded over every candidate.
+//      on every listed segment whose estimate can reach U; the winner is the
+//      smallest (distance, linestring id) among them, which is the
+//      reference's fold (:279-294) whenever no distance is exactly 0.  A
+//      point that reaches a zero distance (the reference then passes over
+//      that linestring, whose other segments may be unlisted) or none is
+//      folded over every candidate.
 // A group whose list overflows, or that meets a linestring outside the
 // float32 frames, a non-finite point or an unusable grid, is scanned whole
 // per point (nearest_point_scan).
@@ -628,7 +738,7 @@ __global__ void __launch_bounds__(kNearWarps * 32)
   NearList& L       = s_list[threadIdx.x >> 5];
   uint32_t const ng = *a.ngroups_p;
   bool const gok    = a.gf >= 1.17549435e-38f && a.gf < 1.0e30f;
-  uint32_t nfb = 0, nscan = 0;
+  uint32_t nfb = 0, nscan = 0, nf64 = 0;
   for (;;) {
     unsigned long long gg = 0;
     if (lane == 0) gg = atomicAdd(a.next_group, 1ull);
@@ -657,13 +767,14 @@ __global__ void __launch_bounds__(kNearWarps * 32)
       }
     }
     if (listed) {
-      float const dm = 1.1920928955078125e-07f * mg;
-      float r2       = 0.0f;
+      float const dm  = 1.1920928955078125e-07f * mg;
+      float const tol = 4.76837158203125e-07f * mg;
+      float r2        = 0.0f;
       for (uint32_t c = lane; c < len; c += 32) {
         uint64_t const pos = off + c;
         if (pos >= a.npi) continue;
         float2 const uv = a.u[pos];
-        r2              = fmaxf(r2, list_upper(L, n, uv.x, uv.y, dm));
+        r2              = fmaxf(r2, list_upper(L, n, uv.x, uv.y, dm, tol));
       }
       r2 = warp_max(r2);
       __syncwarp();  // every lane is done with the first list
@@ -683,42 +794,58 @@ __global__ void __launch_bounds__(kNearWarps * 32)
       __syncwarp();
       continue;
     }
-    float const dm = 1.1920928955078125e-07f * mg;
+    float const dm  = 1.1920928955078125e-07f * mg;
+    float const tol = 4.76837158203125e-07f * mg;
     for (uint32_t c = lane; c < len; c += 32) {
       uint64_t const pos = off + c;
       if (pos >= a.npi) continue;
       float2 const uv = a.u[pos];
-      float const U   = list_upper(L, n, uv.x, uv.y, dm);
+      float const U   = list_upper(L, n, uv.x, uv.y, dm, tol);
       float const Uw  = U * 1.0000000009313226f + 7.52316384526264e-37f;
       double px = 0.0, py = 0.0;
       a.src.load(pos, px, py);
-      bool have = false, nonzero = false;
+      // the float64 distance of every listed segment whose estimate can
+      // reach U; per segment, since a linestring's distance is the smallest
+      // of its segments' (square roots are monotone) and the reference's
+      // winner is the smallest non-zero (distance, id): the fold needs no
+      // order.  A segment at distance exactly 0 makes its linestring's
+      // distance 0, which the reference passes over; such a point is folded
+      // over every candidate instead.
+      bool have = false, zero = false;
       uint32_t bid = 0;
       double bd    = 0.0;
-      for (uint32_t t = 0; t < n;) {
-        // the run of entries of one pair (one linestring)
-        uint32_t const k = L.pair[t];
-        double dmin      = std::numeric_limits<double>::max();
-        bool evaluated   = false;
-        for (; t < n && L.pair[t] == k; ++t) {
-          float est, err;
-          seg_estimate(uv.x, uv.y, L.e[t], dm, est, err);
-          if (est - err > Uw) continue;
-          uint32_t const sg = L.seg[t];
-          dmin = fmin(dmin, segment_dist2<double>(px, py, a.lx[sg], a.ly[sg], a.lx[sg + 1],
-                                                  a.ly[sg + 1]));
-          evaluated = true;
+      double bd2   = 0.0;  // smallest squared distance so far (its root is bd)
+      for (uint32_t t = 0; t < n; ++t) {
+        float4 const e  = L.e[t];
+        float4 const sb = make_float4(fminf(e.x, e.z), fminf(e.y, e.w), fmaxf(e.x, e.z),
+                                      fmaxf(e.y, e.w));
+        if (box_lb(uv.x, uv.y, sb, tol) > Uw) continue;
+        float est, err;
+        seg_estimate(uv.x, uv.y, e, dm, est, err);
+        if (est - err > Uw) continue;
+        uint32_t const sg = L.seg[t];
+        ++nf64;
+        double const d2 =
+          segment_dist2<double>(px, py, a.lx[sg], a.ly[sg], a.lx[sg + 1], a.ly[sg + 1]);
+        if (!(d2 <= static_cast<double>(Uw))) continue;
+        if (d2 == 0.0) {
+          zero = true;
+          break;
         }
-        if (!evaluated || !(dmin <= static_cast<double>(Uw))) continue;
-        uint32_t const lid = a.pair_ls[k];
-        double const d     = sqrt(dmin);
-        if (!have || take_rhs<double>(bd, bid, d, lid)) {
-          bid = lid;
+        // a squared distance more than 2^-48 above the smallest so far has a
+        // larger (rounded) square root: it can neither win nor tie, so its
+        // root is not needed
+        if (have && d2 > bd2 * 1.0000000000000036) continue;
+        double const d     = sqrt(d2);
+        uint32_t const lid = L.lid[t];
+        if (!have || d < bd || (d == bd && lid < bid)) {
           bd  = d;
+          bid = lid;
         }
+        bd2  = have ? fmin(bd2, d2) : d2;
         have = true;
-        nonzero |= d != 0.0;
       }
+      bool const nonzero = !zero;
       if (!have || !nonzero) {
         ++nfb;
         fold_all(a, k0, k1, px, py, have, bid, bd);
@@ -734,9 +861,11 @@ __global__ void __launch_bounds__(kNearWarps * 32)
   if (a.stats) {
     for (int o = 16; o > 0; o >>= 1) {
       nfb += __shfl_xor_sync(0xFFFFFFFFu, nfb, o);
+      nf64 += __shfl_xor_sync(0xFFFFFFFFu, nf64, o);
     }
     if (lane == 0 && nfb) atomicAdd(a.stats, static_cast<unsigned long long>(nfb));
     if (lane == 0 && nscan) atomicAdd(a.stats + 1, static_cast<unsigned long long>(nscan));
+    if (lane == 0 && nf64) atomicAdd(a.stats + 3, static_cast<unsigned long long>(nf64));
   }
 }
 
@@ -767,6 +896,7 @@ void run(uint32_t const* pair_ls, uint32_t const* pair_quad, size_t npairs,
   if constexpr (std::is_same<T, double>::value) {
     if (method == CSPT_METHOD_FILTERED) {
       // linestring index
+      std::unique_ptr<KernelTimer> index_timer(new KernelTimer("nearest_index", s));
       Buffer<double4_16a> box(alloc, nls);
       Buffer<uint8_t> lexact(alloc, nls);
       Buffer<uint32_t> nch(alloc, nls + 1), cbase(alloc, nls + 1);
@@ -781,22 +911,27 @@ void run(uint32_t const* pair_ls, uint32_t const* pair_quad, size_t npairs,
       Buffer<long long> aix(alloc, nls), aiy(alloc, nls);
       Buffer<float> maxoff(alloc, nls);
       Buffer<float4> cbox(alloc, nv / kSegChunk + nls + 1), seg32(alloc, nv);
+      Buffer<LsRec> lrec(alloc, nls);
       ls_fill_kernel<<<lgrd, 256, 0, s>>>(lso, nls, lx, ly, box.data(), grid.data(),
-                                          cbase.data(), aix.data(), aiy.data(), maxoff.data(),
-                                          cbox.data(), seg32.data());
+                                          cbase.data(), lexact.data(), aix.data(), aiy.data(),
+                                          maxoff.data(), cbox.data(), seg32.data(), lrec.data());
       CSPT_CHECK_LAUNCH();
       double const g = read_back(grid.data(), s);
+      index_timer.reset();
       // leaf frames of the groups
       Buffer<float2> u(alloc, npi);
       Buffer<LeafFrame> frames(alloc, npairs);
+      std::unique_ptr<KernelTimer> frames_timer(new KernelTimer("leaf_frames", s));
       leaf_frame_kernel<<<grid_for(npairs * 32, 256, sm_grid(32u)), 256, 0, s>>>(
         gs, gs + npairs, pair_quad, tree->length, qoff, src, npi, grid.data(), u.data(),
         frames.data());
       CSPT_CHECK_LAUNCH();
-      LinestringIndexView liv{aix.data(),   aiy.data(),  maxoff.data(), cbase.data(),
-                              cbox.data(),  seg32.data(), lexact.data()};
-      Buffer<unsigned long long> fb(alloc, 3);  // points folded whole, groups scanned, next group
-      CSPT_CUDA_TRY(cudaMemsetAsync(fb.data(), 0, 3 * sizeof(unsigned long long), s));
+      frames_timer.reset();
+      LinestringIndexView liv{aix.data(),  aiy.data(),   maxoff.data(), cbase.data(),
+                              cbox.data(), seg32.data(), lexact.data(), lrec.data()};
+      // points folded whole, groups scanned, next group, float64 segment distances
+      Buffer<unsigned long long> fb(alloc, 4);
+      CSPT_CUDA_TRY(cudaMemsetAsync(fb.data(), 0, 4 * sizeof(unsigned long long), s));
       NearestArgs const na{gs,          gs + npairs,  npairs,     pair_ls,   pair_quad,
                            tree->length, qoff,        src,        npi,       lso,
                            nls,          lx,          ly,         u.data(),  frames.data(),
@@ -814,11 +949,12 @@ void run(uint32_t const* pair_ls, uint32_t const* pair_quad, size_t npairs,
                                          sm_grid(static_cast<unsigned>(per_sm))),
                                 kNearWarps * 32, 0, s>>>(na);
       CSPT_CHECK_LAUNCH();
-      unsigned long long st[2];
+      unsigned long long st[4];
       CSPT_CUDA_TRY(cudaMemcpyAsync(st, fb.data(), sizeof(st), cudaMemcpyDeviceToHost, s));
       CSPT_CUDA_TRY(cudaStreamSynchronize(s));
       last_fallbacks()     = st[0];
       last_group_scans()   = st[1];
+      last_f64_segments()  = st[3];
       return;
     }
   }

@@ -26,6 +26,13 @@
 #include "scan.cuh"
 
 namespace cspt {
+
+uint64_t& last_edge_free_pairs()
+{
+  static thread_local uint64_t n = 0;
+  return n;
+}
+
 namespace {
 
 constexpr int kPipBlock = 256;
@@ -42,6 +49,8 @@ constexpr size_t kHostChunks = CSPT_HOST_CHUNKS;
 #endif
 constexpr uint32_t kFastPool  = CSPT_FAST_POOL;
 constexpr uint32_t kFastSlabs = 31;
+// the edge-free quadrant test streams at most this many slab entries
+constexpr uint32_t kFreeScan = 1024;
 
 // The float32 slab of offset y (the lookup of filtered_test).
 __device__ inline uint32_t slab_lookup(float qy, float y0, float invh, uint32_t ns)
@@ -105,7 +114,8 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
                   PolygonIndexView<double> ix, uint64_t const* __restrict__ word_off,
                   uint32_t* __restrict__ bits, uint32_t* __restrict__ counts,
                   unsigned long long* __restrict__ refined,
-                  unsigned long long* __restrict__ next_pair)
+                  unsigned long long* __restrict__ next_pair,
+                  unsigned long long* __restrict__ stats)
 {
   int const lane      = threadIdx.x & 31;
   int const wid       = threadIdx.x >> 5;
@@ -121,6 +131,7 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
   float const gf      = Filtered ? static_cast<float>(*ix.grid) : 0.0f;
   bool const gok      = gf >= 1.17549435e-38f && gf < 1.0e30f;  // normal float grid step
   uint32_t nref       = 0;
+  uint32_t nfree      = 0;  // pairs decided by the edge-free test
   for (;;) {
     unsigned long long kk = 0;
     if (lane == 0) kk = atomicAdd(next_pair, 1ull);
@@ -193,6 +204,105 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
           j0                  = slab_lookup(qymin, bx.y, invh, ns);
           uint32_t const j1   = slab_lookup(qymax, bx.y, invh, ns);
           jspan               = j1 - j0;
+          // Edge-free quadrant.  When no edge's box, widened by tol, meets
+          // the quadrant's point box [qxmin, qxmax] x [qymin, qymax] and no
+          // exactly vertical edge lies within tol of its x-range, every
+          // point of the quadrant gets the reference's result of any one of
+          // them: no point can be on an edge (each edge is more than tol
+          // from it in x or in y); edges left of, above or below the box
+          // never toggle; an edge right of the box toggles exactly when its
+          // y-range holds the point's y, and as y moves through the box that
+          // changes only at a vertex right of the box, whose two ring
+          // neighbours are then both right of the box (an edge through such
+          // a vertex and within the box's y-range can be neither left,
+          // above, below nor meeting the box) and flip together.  So the
+          // crossing parity is the same for the whole box: the quadrant's
+          // first point is tested over its slab (float32 per edge, the
+          // reference's float64 for undecided edges) and its result fills
+          // every word.
+          {
+            uint32_t const E0 = ix.slab_start[slab0 + j0];
+            uint32_t const E1 = ix.slab_start[slab0 + j1 + 1];
+            bool meets        = E1 - E0 > kFreeScan || len == 0 || off >= npi;
+            for (uint32_t t0 = E0; t0 < E1 && !meets; t0 += 32) {
+              uint32_t const kk = t0 + lane;
+              bool m            = false;
+              if (kk < E1) {
+                float4 const e = ix.slab_e32[kk];
+                m = !(fmaxf(e.x, e.z) < qxmin - tol || fminf(e.x, e.z) > qxmax + tol ||
+                      fmaxf(e.y, e.w) < qymin - tol || fminf(e.y, e.w) > qymax + tol);
+              }
+              meets = __any_sync(0xFFFFFFFFu, m);
+            }
+            if (!meets && vb < ve) {
+              uint32_t lo = vb, hi = ve;
+              float const key = qxmin - tol;
+              while (lo < hi) {
+                uint32_t const mid = (lo + hi) >> 1;
+                if (ix.vert_x32[mid] < key)
+                  lo = mid + 1;
+                else
+                  hi = mid;
+              }
+              meets = lo < ve && ix.vert_x32[lo] <= qxmax + tol;
+            }
+            if (!meets) {
+              float2 const uv   = u[off];
+              float const qx    = uv.x - dx, qy = uv.y - dy;
+              float const eb    = __fmaf_rn(7.62939453125e-06f * mall, mall, 7.52316384526264e-37f);
+              uint32_t const jr = slab_lookup(qy, bx.y, invh, ns);
+              uint32_t const R0 = ix.slab_start[slab0 + jr];
+              uint32_t const R1 = ix.slab_start[slab0 + jr + 1];
+              unsigned par      = 0u;
+              bool on           = false;
+              for (uint32_t t0 = R0; t0 < R1; t0 += 32) {
+                uint32_t const kk = t0 + lane;
+                bool tg = false, oe = false;
+                if (kk < R1) {
+                  float4 const e = ix.slab_e32[kk];
+                  float const ya = e.y - qy, yb = e.w - qy;
+                  bool const y1  = ya > 0.0f;
+                  bool const y0  = yb > 0.0f;
+                  float const cr = __fmaf_rn(qx - e.x, e.w - e.y, -((e.z - e.x) * (qy - e.y)));
+                  bool const undecided =
+                    fabsf(ya) <= tol || fabsf(yb) <= tol ||
+                    (fabsf(cr) <= eb &&
+                     (y1 != y0 || !(qx < fminf(e.x, e.z) - tol || qx > fmaxf(e.x, e.z) + tol)));
+                  if (!undecided) {
+                    tg = y1 != y0 && ((cr < 0.0f) != y1);
+                  } else {
+                    ++nref;
+                    double px64, py64;
+                    src.load(off, px64, py64);
+                    uint32_t const v  = ix.slab_edges[kk] & kEntryVertex;
+                    uint32_t const pv = ix.prev_vertex[v];
+                    int const ee =
+                      exact_edge<double>(px64, py64, ix.vx[v], ix.vy[v], ix.vx[pv], ix.vy[pv]);
+                    oe = ee == 2;
+                    tg = ee == 1;
+                  }
+                }
+                par ^= __ballot_sync(0xFFFFFFFFu, tg);
+                on = __any_sync(0xFFFFFFFFu, oe) || on;
+              }
+              if (!on) {
+                // (an on-edge representative contradicts the premise; such a
+                // pair takes the paths below)
+                bool const all      = (__popc(par) & 1u) != 0u;
+                uint64_t const vmax = npi - off < len ? npi - off : len;
+                for (uint32_t w = lane; w < nw; w += 32) {
+                  uint64_t const b0 = static_cast<uint64_t>(w) * 32u;
+                  uint32_t word     = 0u;
+                  if (all && vmax > b0)
+                    word = vmax - b0 >= 32 ? 0xFFFFFFFFu : (1u << (vmax - b0)) - 1u;
+                  bits[wb + w] = word;
+                }
+                if (lane == 0) counts[k] = all ? static_cast<uint32_t>(vmax) : 0u;
+                ++nfree;
+                continue;
+              }
+            }
+          }
           if (jspan < kFastSlabs) {
             fast              = true;
             float const hs    = invh > 0.0f ? 1.0f / invh : 0.0f;
@@ -443,6 +553,7 @@ __global__ void __launch_bounds__(kPipBlock, Filtered ? kPipMinBlocksFiltered : 
   if (Filtered && refined) {
     for (int o = 16; o > 0; o >>= 1) nref += __shfl_xor_sync(0xFFFFFFFFu, nref, o);
     if (lane == 0 && nref) atomicAdd(refined, static_cast<unsigned long long>(nref));
+    if (lane == 0 && nfree) atomicAdd(stats, static_cast<unsigned long long>(nfree));
   }
 }
 
@@ -536,8 +647,10 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
     },
     [wo] __device__(size_t k, uint64_t e, uint64_t) { wo[k] = e; }, npairs, wo + npairs, alloc);
   Buffer<uint32_t> counts(alloc, npairs);
-  Buffer<unsigned long long> refined(alloc, 2);  // [0] refined candidates, [1] next pair
-  CSPT_CUDA_TRY(cudaMemsetAsync(refined.data(), 0, 2 * sizeof(unsigned long long), s));
+  // [0] refined candidates, [1] next pair, [2] pairs decided by the
+  // edge-free test
+  Buffer<unsigned long long> refined(alloc, 3);
+  CSPT_CUDA_TRY(cudaMemsetAsync(refined.data(), 0, 3 * sizeof(unsigned long long), s));
   unsigned const blk = 256;
   // filtered: groups of consecutive pairs sharing a quadrant, each pair's
   // group, and the leaf frames (float32 point offsets from the quadrant's
@@ -597,13 +710,13 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
         pip_pair_kernel<true><<<pair_grid(pip_pair_kernel<true>, kPipBlock, n), kPipBlock, 0, s>>>(
           pair_poly + k0, pair_quad + k0, pgroup.data() + k0, n, qlen, qoff, src, npi, u.data(),
           frames.data(), index.view(), word_off.data() + k0, bits.data(), counts.data() + k0,
-          refined.data(), refined.data() + 1);
+          refined.data(), refined.data() + 1, refined.data() + 2);
       else
         pip_pair_kernel<false>
           <<<pair_grid(pip_pair_kernel<false>, kPipBlock, n), kPipBlock, 0, s>>>(
             pair_poly + k0, pair_quad + k0, nullptr, n, qlen, qoff, src, npi, nullptr, nullptr,
             index.view(), word_off.data() + k0, bits.data(), counts.data() + k0, nullptr,
-            refined.data() + 1);
+            refined.data() + 1, refined.data() + 2);
     } else {
       pip_pair_kernel_f32<<<grid_for(n * 32, blk, sm_grid(8u * 4u)), blk, 0, s>>>(
         pair_poly + k0, pair_quad + k0, n, qlen, qoff, src, npi, index.view(),
@@ -630,11 +743,19 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
     CSPT_CHECK_LAUNCH();
   };
 
+  // the kernel's counters (read once the stream is idle)
+  auto finish_counts = [&] {
+    unsigned long long h[3] = {0, 0, 0};
+    CSPT_CUDA_TRY(cudaMemcpyAsync(h, refined.data(), sizeof(h), cudaMemcpyDeviceToHost, s));
+    CSPT_CUDA_TRY(cudaStreamSynchronize(s));
+    if (out_refined) *out_refined = filtered ? h[0] : 0;
+    last_edge_free_pairs() = filtered ? h[2] : 0;
+  };
   if (!host) {
     evaluate(0, npairs);
     Buffer<uint64_t> out_off;
     size_t const m = row_offsets(0, npairs, out_off);
-    if (out_refined) *out_refined = filtered ? read_back(refined.data(), s) : 0;
+    finish_counts();
     *out_n = m;
     if (m == 0) return;
     Buffer<uint32_t> op(alloc, m), oq(alloc, m);
@@ -681,8 +802,7 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
     rows += m;
   }
   copies.join();
-  if (out_refined) *out_refined = filtered ? read_back(refined.data(), s) : 0;
-  CSPT_CUDA_TRY(cudaStreamSynchronize(s));
+  finish_counts();
   *out_n = rows;
   CSPT_EXPECTS(rows <= host->capacity,
                "the host buffers hold " + std::to_string(host->capacity) +
@@ -758,7 +878,7 @@ class PipExec::Impl {
     pgroup_   = Buffer<uint32_t>(alloc, npairs);
     frames_   = Buffer<LeafFrame>(alloc, npairs);
     u_        = Buffer<float2>(alloc, filtered ? npi : 0);
-    refined_  = Buffer<unsigned long long>(alloc, 2);  // [0] refined, [1] next pair
+    refined_  = Buffer<unsigned long long>(alloc, 3);  // refined, next pair, edge-free pairs
     flag_     = Buffer<int>(alloc, 1);
     grid_true_    = pair_grid(pip_pair_kernel<true>, blk_, npairs);
     grid_ordered_ = pair_grid(pip_pair_kernel<true, true>, blk_, npairs);
@@ -776,7 +896,7 @@ class PipExec::Impl {
   {
     unsigned const blk = blk_;
     unsigned const grd = grid_for(np_ * 32, blk, sm_grid(8u * 1024u / blk));
-    CSPT_CUDA_TRY(cudaMemsetAsync(refined_.data(), 0, 2 * sizeof(unsigned long long), s));
+    CSPT_CUDA_TRY(cudaMemsetAsync(refined_.data(), 0, 3 * sizeof(unsigned long long), s));
     if (filtered_) {
       leaf_frame_kernel<<<grd, blk, 0, s>>>(gstart_.data(), gstart_.data() + np_, pq_, qlen_,
                                             qoff_, src(), npi_, ix_.grid, u_.data(),
@@ -786,16 +906,17 @@ class PipExec::Impl {
         pip_pair_kernel<true, true><<<grid_ordered_, blk, 0, s>>>(
           pp_, pq_, pgroup_.data(), np_, qlen_, qoff_, src(), npi_, u_.data(), frames_.data(),
           ix_, word_off_.data(), bits_.data(), counts_.data(), refined_.data(),
-          refined_.data() + 1);
+          refined_.data() + 1, refined_.data() + 2);
       else
         pip_pair_kernel<true><<<grid_true_, blk, 0, s>>>(
           pp_, pq_, pgroup_.data(), np_, qlen_, qoff_, src(), npi_, u_.data(), frames_.data(),
           ix_, word_off_.data(), bits_.data(), counts_.data(), refined_.data(),
-          refined_.data() + 1);
+          refined_.data() + 1, refined_.data() + 2);
     } else {
       pip_pair_kernel<false><<<grid_false_, blk, 0, s>>>(
         pp_, pq_, nullptr, np_, qlen_, qoff_, src(), npi_, nullptr, nullptr, ix_,
-        word_off_.data(), bits_.data(), counts_.data(), nullptr, refined_.data() + 1);
+        word_off_.data(), bits_.data(), counts_.data(), nullptr, refined_.data() + 1,
+        refined_.data() + 2);
     }
     CSPT_CHECK_LAUNCH();
     scan_apply_prealloc<uint64_t>(CountsOf{counts_.data()}, Store64{out_off_.data()}, np_,

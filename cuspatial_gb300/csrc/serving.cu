@@ -543,7 +543,19 @@ class Server {
     budget_.limit = o.memory_budget_bytes;
     CSPT_CUDA_TRY(cudaGetDevice(&device_));
     int const nw = std::max(1, o.num_streams);
-    for (int w = 0; w < nw; ++w) workers_.emplace_back([this] { worker(); });
+    // every worker's stream exists before any worker starts: a failure is
+    // reported here, to the caller creating the server
+    streams_.resize(nw, nullptr);
+    for (int w = 0; w < nw; ++w) {
+      cudaError_t const e = cudaStreamCreateWithFlags(&streams_[w], cudaStreamNonBlocking);
+      if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        for (int v = 0; v < w; ++v) cudaStreamDestroy(streams_[v]);
+        throw Error{CSPT_CUDA_ERROR, std::string("cannot create a serving stream: ") +
+                                       cudaGetErrorString(e)};
+      }
+    }
+    for (int w = 0; w < nw; ++w) workers_.emplace_back([this, w] { worker(streams_[w]); });
   }
 
   ~Server()
@@ -554,6 +566,7 @@ class Server {
     }
     cv_.notify_all();
     for (auto& t : workers_) t.join();
+    for (cudaStream_t st : streams_) cudaStreamDestroy(st);
   }
 
   double now() const
@@ -690,14 +703,9 @@ class Server {
     done_cv_.notify_all();
   }
 
-  void worker()
+  void worker(cudaStream_t s)
   {
     cudaSetDevice(device_);
-    cudaStream_t s = nullptr;
-    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
-      (void)cudaGetLastError();
-      return;
-    }
     cspt_allocator mr{&budget_, &Budget::allocate, &Budget::deallocate};
     Allocator alloc(&mr, s);
     for (;;) {
@@ -749,7 +757,6 @@ class Server {
       }
       cv_.notify_all();
     }
-    cudaStreamDestroy(s);
   }
 
   void run_batch(std::vector<Request*>& b, Allocator const& alloc, cudaStream_t s,
@@ -813,6 +820,7 @@ class Server {
   uint64_t max_batch_seen_ = 0;
   bool stop_ = false;
   std::vector<std::thread> workers_;
+  std::vector<cudaStream_t> streams_;
 };
 
 }  // namespace cspt

@@ -80,13 +80,22 @@ const char* cspt_version(void);
  * counterpart in the reference. */
 uint64_t cspt_last_refined_count(void);
 
+/* Number of (polygon, quadrant) pairs that the last CSPT_METHOD_FILTERED
+ * float64 point-in-polygon call on this thread decided whole: no edge comes
+ * within the filter's margin of the quadrant's points, so one point's
+ * result holds for all of them.  Diagnostic with no counterpart in the
+ * reference. */
+uint64_t cspt_last_edge_free_pairs(void);
+
 /* Paths taken by the last CSPT_METHOD_FILTERED float64 nearest-linestring
  * call on this thread: points whose fold ran over every candidate in
- * float64 (their listed candidates reached only zero distances, or none),
- * and groups of pairs sharing a quadrant that were scanned point by point
- * instead of through their leaf's segment list.  Either pointer may be NULL.
- * Diagnostic with no counterpart in the reference. */
-void cspt_last_nearest_stats(uint64_t* points_folded_whole, uint64_t* groups_scanned);
+ * float64 (their listed candidates reached a zero distance, or none),
+ * groups of pairs sharing a quadrant that were scanned point by point
+ * instead of through their leaf's segment list, and listed segments whose
+ * distance was evaluated in float64.  Any pointer may be NULL.  Diagnostic
+ * with no counterpart in the reference. */
+void cspt_last_nearest_stats(uint64_t* points_folded_whole, uint64_t* groups_scanned,
+                             uint64_t* float64_segments);
 
 /* Number of kernels this library has launched since load.  Diagnostic with
  * no counterpart in the reference. */
@@ -204,7 +213,10 @@ cspt_status cspt_polygon_bounding_boxes(const uint32_t* poly_offsets, size_t num
  * library keeps until exit, so inputs are limited to 1,048,576 polygons;
  * larger inputs are rejected with CSPT_INVALID_ARGUMENT.  The first call on a
  * device looks up the array's device address (cudaGetSymbolAddress) with
- * that device current: make that first call before any stream capture.  All
+ * that device current: make that first call before any stream capture.  The
+ * address is kept per device ordinal for the life of the process; it does
+ * not survive cudaDeviceReset (or another reset of the device's primary
+ * context), after which this entry point must not be called again.  All
  * calls on a device share the one array (each call rewrites what it reads),
  * so calls whose work overlaps on the GPU (different streams, no ordering
  * between them) race and must not be issued.

@@ -4,8 +4,8 @@ cspt_polygon_bounding_boxes_noalloc serves callers that must not allocate
 device memory (stream capture, latency-bound loops, hosts that own all device
 memory): it keeps its scratch in a fixed device array.  Two calls in a row
 with different inputs must each equal cspt_polygon_bounding_boxes bit for bit
-(the second call reuses the array the first one wrote), and oversize inputs
-are refused before any GPU work.
+(each call reuses the array the previous one wrote), for float64 and float32
+coordinates, and oversize inputs are refused before any GPU work.
 """
 
 import ctypes
@@ -32,7 +32,7 @@ def _boxes(fn, po, ro, x, y, r):
     return status, out
 
 
-def _polygon_set(n_polygons, seed, with_empty):
+def _polygon_set(n_polygons, seed, with_empty, dtype=torch.float64):
     w = D.precision_at_scale(n_points=1000, n_polygons=n_polygons, extent=5000.0,
                              max_vertices=200, seed_offset=seed)
     P = w.polygons
@@ -40,8 +40,8 @@ def _polygon_set(n_polygons, seed, with_empty):
     if with_empty:  # polygons without rings: rows move up, trailing rows are NaN
         po = np.insert(po, [3, 3, 10], [po[3], po[3], po[10]])
     dev = lambda a, t: torch.from_numpy(np.ascontiguousarray(a)).to(t).cuda()  # noqa: E731
-    return (dev(po, torch.int32), dev(P.ring_offset, torch.int32), dev(P.x, torch.float64),
-            dev(P.y, torch.float64))
+    return (dev(po, torch.int32), dev(P.ring_offset, torch.int32), dev(P.x, dtype),
+            dev(P.y, dtype))
 
 
 def test_noalloc_matches_allocating_entry_point_twice():
@@ -49,8 +49,12 @@ def test_noalloc_matches_allocating_entry_point_twice():
     lib.cspt_polygon_bounding_boxes.argtypes = ARGS
     lib.cspt_polygon_bounding_boxes_noalloc.argtypes = ARGS
     lib.cspt_polygon_bounding_boxes_noalloc.restype = ctypes.c_int
-    inputs = [(_polygon_set(5000, 11, False), 0.0), (_polygon_set(700, 12, True), 0.25)]
-    for (po, ro, x, y), r in inputs:  # two calls in a row
+    # float64 and float32 coordinates (the float32 branch has its own box
+    # kernel and NaN tail), with and without empty polygons and expansion
+    inputs = [(_polygon_set(5000, 11, False), 0.0), (_polygon_set(700, 12, True), 0.25),
+              (_polygon_set(3000, 13, True, torch.float32), 0.5),
+              (_polygon_set(900, 14, False, torch.float32), 0.0)]
+    for (po, ro, x, y), r in inputs:  # calls in a row
         s_ref, ref = _boxes(lib.cspt_polygon_bounding_boxes, po, ro, x, y, r)
         s_new, got = _boxes(lib.cspt_polygon_bounding_boxes_noalloc, po, ro, x, y, r)
         torch.cuda.synchronize()
