@@ -827,7 +827,17 @@ def run_batched(args, dist):
 
     pl, _ = plan(args.method)  # warms the allocator
     pl.close()
+    lib.cspt_profile_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(ctypes.c_uint64)]
+    lib.cspt_profile_enable.argtypes = [ctypes.c_int]
+    lib.cspt_profile_enable(1)
     pl, plan_ms = plan(args.method)
+    plan_stages = {}
+    for name in ("batched_tree", "batched_join", "polygon_index"):
+        sms, cnt = ctypes.c_double(), ctypes.c_uint64()
+        lib.cspt_profile_read(name.encode(), ctypes.byref(sms), ctypes.byref(cnt))
+        plan_stages[name] = sms.value
+    lib.cspt_profile_enable(0)
     clocks = ClockSampler(dist.local)
     clocks.start()
     counted = []
@@ -954,7 +964,8 @@ def run_batched(args, dist):
                               "device": table.meta.get("device", "untuned defaults")},
                    "step": "one replay of the captured evaluation graph (all instances)",
                    "l2": "inputs larger than L2 (%.1f GB of points resident)" % (16 * n / 1e9)},
-        "plan_ms": plan_ms, "plan_plus_step_points_per_s": n / ((plan_ms + ms) / 1e3),
+        "plan_ms": plan_ms, "plan_stages_ms": plan_stages,
+        "plan_plus_step_points_per_s": n / ((plan_ms + ms) / 1e3),
         "nodes": inf.num_nodes, "pairs": inf.num_pairs, "rows": inf.num_rows,
         "refined_candidates": refined, "kernels_per_step": inf.kernels_per_run,
         "plain_fp64": plain,
