@@ -510,6 +510,10 @@ __device__ inline void nearest_point_scan(NearestArgs const& a, uint32_t k0, uin
 // linestring, in no particular order.
 constexpr int kNearWarps    = 4;    // warps per block
 constexpr uint32_t kNearCap = 384;  // listed segments per warp
+static_assert(kNearCap <= 65536, "candidate slots hold 16-bit list positions");
+// float64 candidates per point evaluated in lockstep rounds (more are taken
+// one lane at a time)
+constexpr uint32_t kNearCand = 4;
 struct NearList {
   float4 e[kNearCap];
   uint32_t seg[kNearCap];
@@ -711,6 +715,20 @@ __device__ inline float list_upper(NearList const& L, uint32_t n, float qx, floa
   return U;
 }
 
+// Whether listed segment t can reach the bound Uw from point offset
+// (qx, qy): its box and then its float32 estimate (minus the estimate's
+// error) are within Uw.
+__device__ inline bool seg_can_reach(NearList const& L, uint32_t t, float qx, float qy, float dm,
+                                     float tol, float Uw)
+{
+  float4 const e  = L.e[t];
+  float4 const sb = make_float4(fminf(e.x, e.z), fminf(e.y, e.w), fmaxf(e.x, e.z), fmaxf(e.y, e.w));
+  if (box_lb(qx, qy, sb, tol) > Uw) return false;
+  float est, err;
+  seg_estimate(qx, qy, e, dm, est, err);
+  return !(est - err > Uw);
+}
+
 // One warp per group of pairs sharing a quadrant (handed out from a device
 // counter), one lane per point.
 //   1. list the segments whose box meets the leaf's point box (radius 0);
@@ -730,10 +748,11 @@ __device__ inline float list_upper(NearList const& L, uint32_t n, float qx, floa
 // A group whose list overflows, or that meets a linestring outside the
 // float32 frames, a non-finite point or an unusable grid, is scanned whole
 // per point (nearest_point_scan).
-__global__ void __launch_bounds__(kNearWarps * 32)
+__global__ void __launch_bounds__(kNearWarps * 32, 6)
   nearest_filtered_kernel(NearestArgs const a)
 {
   __shared__ NearList s_list[kNearWarps];
+  __shared__ uint16_t s_cand[kNearWarps][kNearCand][32];
   int const lane    = threadIdx.x & 31;
   NearList& L       = s_list[threadIdx.x >> 5];
   uint32_t const ng = *a.ngroups_p;
@@ -796,46 +815,53 @@ __global__ void __launch_bounds__(kNearWarps * 32)
     }
     float const dm  = 1.1920928955078125e-07f * mg;
     float const tol = 4.76837158203125e-07f * mg;
-    for (uint32_t c = lane; c < len; c += 32) {
-      uint64_t const pos = off + c;
-      if (pos >= a.npi) continue;
-      float2 const uv = a.u[pos];
-      float const U   = list_upper(L, n, uv.x, uv.y, dm, tol);
-      float const Uw  = U * 1.0000000009313226f + 7.52316384526264e-37f;
+    uint16_t(&cand)[kNearCand][32] = s_cand[threadIdx.x >> 5];
+    for (uint32_t c0 = 0; c0 < len; c0 += 32) {
+      uint64_t const pos = off + c0 + static_cast<uint32_t>(lane);
+      bool const act     = c0 + static_cast<uint32_t>(lane) < len && pos < a.npi;
+      // this point's candidates: the listed segments whose estimate can
+      // reach U (the smallest upper bound over the list), the first
+      // kNearCand of them kept in list order
+      float2 const uv = act ? a.u[pos] : make_float2(0.0f, 0.0f);
+      float Uw        = 0.0f;
+      uint32_t nc     = 0;
+      if (act) {
+        float const U = list_upper(L, n, uv.x, uv.y, dm, tol);
+        Uw            = U * 1.0000000009313226f + 7.52316384526264e-37f;
+        for (uint32_t t = 0; t < n; ++t) {
+          if (!seg_can_reach(L, t, uv.x, uv.y, dm, tol, Uw)) continue;
+          if (nc < kNearCand) cand[nc][lane] = static_cast<uint16_t>(t);
+          ++nc;
+        }
+      }
       double px = 0.0, py = 0.0;
-      a.src.load(pos, px, py);
-      // the float64 distance of every listed segment whose estimate can
-      // reach U; per segment, since a linestring's distance is the smallest
-      // of its segments' (square roots are monotone) and the reference's
-      // winner is the smallest non-zero (distance, id): the fold needs no
-      // order.  A segment at distance exactly 0 makes its linestring's
-      // distance 0, which the reference passes over; such a point is folded
-      // over every candidate instead.
+      if (act) a.src.load(pos, px, py);
+      // The float64 distance of every candidate; per segment, since a
+      // linestring's distance is the smallest of its segments' (square
+      // roots are monotone) and the reference's winner is the smallest
+      // non-zero (distance, id): the fold needs no order.  The lanes take
+      // their r-th candidates together, so each float64 instruction serves
+      // every lane that has one.  A segment at distance exactly 0 makes its
+      // linestring's distance 0, which the reference passes over; such a
+      // point is folded over every candidate instead.
       bool have = false, zero = false;
       uint32_t bid = 0;
       double bd    = 0.0;
       double bd2   = 0.0;  // smallest squared distance so far (its root is bd)
-      for (uint32_t t = 0; t < n; ++t) {
-        float4 const e  = L.e[t];
-        float4 const sb = make_float4(fminf(e.x, e.z), fminf(e.y, e.w), fmaxf(e.x, e.z),
-                                      fmaxf(e.y, e.w));
-        if (box_lb(uv.x, uv.y, sb, tol) > Uw) continue;
-        float est, err;
-        seg_estimate(uv.x, uv.y, e, dm, est, err);
-        if (est - err > Uw) continue;
+      auto fold_seg = [&](uint32_t t) {
         uint32_t const sg = L.seg[t];
         ++nf64;
         double const d2 =
           segment_dist2<double>(px, py, a.lx[sg], a.ly[sg], a.lx[sg + 1], a.ly[sg + 1]);
-        if (!(d2 <= static_cast<double>(Uw))) continue;
+        if (!(d2 <= static_cast<double>(Uw))) return;
         if (d2 == 0.0) {
           zero = true;
-          break;
+          return;
         }
         // a squared distance more than 2^-48 above the smallest so far has a
         // larger (rounded) square root: it can neither win nor tie, so its
         // root is not needed
-        if (have && d2 > bd2 * 1.0000000000000036) continue;
+        if (have && d2 > bd2 * 1.0000000000000036) return;
         double const d     = sqrt(d2);
         uint32_t const lid = L.lid[t];
         if (!have || d < bd || (d == bd && lid < bid)) {
@@ -844,16 +870,32 @@ __global__ void __launch_bounds__(kNearWarps * 32)
         }
         bd2  = have ? fmin(bd2, d2) : d2;
         have = true;
+      };
+      uint32_t const mine   = nc < kNearCand ? nc : kNearCand;
+      uint32_t const rounds = __reduce_max_sync(0xFFFFFFFFu, mine);
+      __syncwarp();  // every lane's candidates are stored
+      for (uint32_t r = 0; r < rounds; ++r)
+        if (r < mine && !zero) fold_seg(cand[r][lane]);
+      if (nc > kNearCand && !zero) {
+        // more candidates than kept: the rest in list order, this lane alone
+        uint32_t seen = 0;
+        for (uint32_t t = 0; t < n && !zero; ++t) {
+          if (!seg_can_reach(L, t, uv.x, uv.y, dm, tol, Uw)) continue;
+          if (seen++ < kNearCand) continue;
+          fold_seg(t);
+        }
       }
-      bool const nonzero = !zero;
-      if (!have || !nonzero) {
-        ++nfb;
-        fold_all(a, k0, k1, px, py, have, bid, bd);
-      }
-      if (have) {
-        a.opt[pos] = static_cast<uint32_t>(pos);
-        a.ols[pos] = bid;
-        a.od[pos]  = bd;
+      __syncwarp();  // the candidate slots are reused by the next chunk
+      if (act) {
+        if (!have || zero) {
+          ++nfb;
+          fold_all(a, k0, k1, px, py, have, bid, bd);
+        }
+        if (have) {
+          a.opt[pos] = static_cast<uint32_t>(pos);
+          a.ols[pos] = bid;
+          a.od[pos]  = bd;
+        }
       }
     }
     __syncwarp();  // the next group rewrites this warp's list
