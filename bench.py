@@ -801,11 +801,12 @@ def run_batched(args, dist):
     stream = torch.cuda.current_stream()
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
 
-    def plan(method):
+    def plan(method, ordered=True):
         torch.cuda.synchronize()
         t = time.perf_counter()
         pl = BatchedPointInPolygon(x, y, wl.point_offsets, polys, wl.polygon_offsets, params,
-                                   method=method, block_threads=table.block_threads)
+                                   method=method, block_threads=table.block_threads,
+                                   ordered_index=ordered)
         torch.cuda.synchronize()
         return pl, (time.perf_counter() - t) * 1e3
 
@@ -865,6 +866,18 @@ def run_batched(args, dist):
                      torch.equal(er[0], rows[2]))}
         pe.close()
 
+    # the one-shot index (no slab ordering): the shortest plan + one run
+    pu, pu_plan_ms = plan(args.method, ordered=False)
+    ums = replays(pu, args.steps, args.warmup)
+    ur = pu.rows()
+    pu_ms = statistics.mean(ums)
+    one_shot = {"plan_ms": pu_plan_ms, "ms_per_step": pu_ms,
+                "plan_plus_step_points_per_s": n / ((pu_plan_ms + pu_ms) / 1e3),
+                "rows_identical_to_ordered": bool(
+                    torch.equal(ur[1], rows[0]) and torch.equal(ur[2], rows[1]) and
+                    torch.equal(ur[0], rows[2]))}
+    pu.close()
+
     # the same instances one by one through the single-instance calls
     # (sample, time scaled by points)
     rng = np.random.default_rng(7)
@@ -907,7 +920,7 @@ def run_batched(args, dist):
         got_q = rows[1][ro_h[i]:ro_h[i + 1]]
         if not (torch.equal(got_p, ir["polygon_index"]) and torch.equal(got_q, ir["point_index"])):
             mismatches += 1
-    single_pps = single_pts / single_s
+    single_pps = single_pts / single_s if single_s > 0 else None
 
     # end to end from pinned host buffers: copies, plan, one evaluation, rows back
     e2e = None
@@ -966,6 +979,7 @@ def run_batched(args, dist):
                    "l2": "inputs larger than L2 (%.1f GB of points resident)" % (16 * n / 1e9)},
         "plan_ms": plan_ms, "plan_stages_ms": plan_stages,
         "plan_plus_step_points_per_s": n / ((plan_ms + ms) / 1e3),
+        "one_shot_index": one_shot,
         "nodes": inf.num_nodes, "pairs": inf.num_pairs, "rows": inf.num_rows,
         "refined_candidates": refined, "kernels_per_step": inf.kernels_per_run,
         "plain_fp64": plain,

@@ -157,7 +157,7 @@ def _declare(lib):
     _u64p = ctypes.POINTER(ctypes.c_uint64)
     lib.cspt_batched_pip_plan.argtypes = [
         _sz, _u64p, _vp, _vp, _u64p, _vp, _sz, _vp, _sz, _vp, _vp, _sz,
-        ctypes.POINTER(CsptInstanceParams), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+        ctypes.POINTER(CsptInstanceParams), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
         ctypes.POINTER(CsptAllocator), _vp, ctypes.POINTER(_vp)]
     lib.cspt_batched_pip_run.argtypes = [_vp, ctypes.c_int, _vp]
     lib.cspt_batched_pip_get_info.argtypes = [_vp, ctypes.POINTER(CsptBatchedPipInfo)]

@@ -48,12 +48,16 @@ class BatchedPointInPolygon:
     params: per instance x_min, x_max, y_min, y_max, scale, max_depth,
     max_size (dicts or tuples), the arguments of quadtree_on_points.
     method: "exact" (float64) or "filtered" (float32 filter, float64
-    refinement; same rows).  block_threads: block size of the per-pair kernels.
+    refinement; same rows).  ordered_index: sort each slab's crossing edges
+    into per-(slab, x-bin) windows — a longer plan and faster runs, for plans
+    run many times; False keeps the one-shot index (shortest plan + run).
+    block_threads: block size of the per-pair kernels with the ordered index.
     budget_bytes: optional cap on the device memory the plan may take.
     """
 
     def __init__(self, points_x, points_y, point_offsets, polygons: GeoSeries, polygon_offsets,
-                 params, method="filtered", block_threads=256, budget_bytes=None):
+                 params, method="filtered", block_threads=256, budget_bytes=None,
+                 ordered_index=True):
         if len(polygons) and not contains_only_polygons(polygons):
             raise ValueError("`polygons` Geoseries must contains only polygons geometries.")
         self._lib = lib = _lib.load()
@@ -79,7 +83,8 @@ class BatchedPointInPolygon:
             _lib.ptr(poly.part_offset), int(poly.part_offset.numel()), _lib.ptr(poly.ring_offset),
             int(poly.ring_offset.numel()), _lib.ptr(poly.x), _lib.ptr(poly.y),
             int(poly.x.numel()), self._params, _lib.FLOAT64, _METHODS[method],
-            int(block_threads), self._alloc.ref, _lib.stream_ptr(), ctypes.byref(h)), lib)
+            1 if ordered_index else 0, int(block_threads), self._alloc.ref, _lib.stream_ptr(),
+            ctypes.byref(h)), lib)
         self._h = h
         self._row_offsets_host = None
 

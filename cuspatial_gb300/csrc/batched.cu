@@ -76,12 +76,13 @@ class BatchedPip {
   BatchedPip(size_t ni, uint64_t const* h_pt_off, double const* x, double const* y,
              uint64_t const* h_poly_off, uint32_t const* po, size_t npo, uint32_t const* ro,
              size_t nro, double const* vx, double const* vy, size_t nv,
-             cspt_instance_params const* params, cspt_method method, int block,
+             cspt_instance_params const* params, cspt_method method, bool ordered, int block,
              cspt_allocator const* mr, cudaStream_t stream)
     : mr_copy_(mr ? *mr : cspt_allocator{}), alloc_(mr ? &mr_copy_ : nullptr, stream), ni_(ni),
       f_(alloc_)
   {
-    plan(h_pt_off, x, y, h_poly_off, po, npo, ro, nro, vx, vy, nv, params, method, block);
+    plan(h_pt_off, x, y, h_poly_off, po, npo, ro, nro, vx, vy, nv, params, method, ordered,
+         block);
   }
   ~BatchedPip()
   {
@@ -167,7 +168,7 @@ class BatchedPip {
   void plan(uint64_t const* h_pt_off, double const* x, double const* y,
             uint64_t const* h_poly_off, uint32_t const* po, size_t npo, uint32_t const* ro,
             size_t nro, double const* vx, double const* vy, size_t nv,
-            cspt_instance_params const* params, cspt_method method, int block)
+            cspt_instance_params const* params, cspt_method method, bool ordered, int block)
   {
     cudaStream_t const s = alloc_.stream();
     Allocator const& a   = alloc_;
@@ -205,11 +206,15 @@ class BatchedPip {
       return;
     }
     bool const filtered = method == CSPT_METHOD_FILTERED;
+    // the ordered index's windows serve small blocks; the one-shot index's
+    // quadrant fast path keeps per-warp lists sized for blocks of 256
+    bool const order_slabs = filtered && ordered;
     index_.reset(new PolygonIndex<double>(po, np_ + 1, ro, nro, vx, vy, nv, filtered, a,
-                                          /*order_slabs=*/true));
+                                          order_slabs));
+    unsigned const pair_block = order_slabs || !filtered ? static_cast<unsigned>(block) : 256u;
     pip_.reset(new PipExec(pair_poly_.data(), pair_quad_.data(), k_, f_.length_.data(),
                            f_.goff_.data(), f_.sidx_.data(), f_.n_, x, y, index_->view(),
-                           filtered, static_cast<unsigned>(block), a));
+                           filtered, pair_block, a));
     // one evaluation sizes the outputs
     pip_->evaluate(s);
     m_  = read_back(pip_->total(), s);
@@ -296,8 +301,8 @@ cspt_status cspt_batched_pip_plan(size_t num_instances, const uint64_t* point_of
                                   const uint32_t* ring_offsets, size_t num_ring_offsets,
                                   const void* poly_x, const void* poly_y,
                                   size_t num_poly_vertices, const cspt_instance_params* params,
-                                  cspt_dtype dtype, cspt_method method, int block_threads,
-                                  const cspt_allocator* mr, void* stream,
+                                  cspt_dtype dtype, cspt_method method, int ordered_index,
+                                  int block_threads, const cspt_allocator* mr, void* stream,
                                   cspt_batched_pip** out_plan)
 {
   return guarded([&] {
@@ -321,7 +326,8 @@ cspt_status cspt_batched_pip_plan(size_t num_instances, const uint64_t* point_of
       num_instances, point_offsets, static_cast<double const*>(x),
       static_cast<double const*>(y), polygon_offsets, poly_offsets, num_poly_offsets,
       ring_offsets, num_ring_offsets, static_cast<double const*>(poly_x),
-      static_cast<double const*>(poly_y), num_poly_vertices, params, method, block_threads, mr,
+      static_cast<double const*>(poly_y), num_poly_vertices, params, method, ordered_index != 0,
+      block_threads, mr,
       static_cast<cudaStream_t>(stream)));
   });
 }

@@ -588,17 +588,21 @@ typedef struct cspt_batched_pip_info {
 
 /* Builds the trees, joins the boxes, builds the polygon index and sizes the
  * outputs by one evaluation; synchronises `stream`.  method selects plain
- * float64 or float32-filtered evaluation (same rows).  block_threads (a
- * multiple of 32 up to 256; 256 is a good default) is the block size of the
- * per-pair kernels.  Device memory comes from mr on `stream`, which must stay
- * valid until cspt_batched_pip_free. */
+ * float64 or float32-filtered evaluation (same rows).  ordered_index != 0
+ * sorts each slab's crossing edges and keeps per-(slab, x-bin) windows: a
+ * longer plan and faster runs (for plans run many times); 0 keeps the
+ * one-shot index and its quadrant fast path (the shortest plan + run).
+ * block_threads (a multiple of 32 up to 256; 256 is a good default) is the
+ * block size of the per-pair kernels with the ordered index (the one-shot
+ * index's kernel takes 256).  Device memory comes from mr on `stream`, which
+ * must stay valid until cspt_batched_pip_free. */
 cspt_status cspt_batched_pip_plan(
   size_t num_instances, const uint64_t* point_offsets, const void* x, const void* y,
   const uint64_t* polygon_offsets, const uint32_t* poly_offsets, size_t num_poly_offsets,
   const uint32_t* ring_offsets, size_t num_ring_offsets, const void* poly_x, const void* poly_y,
   size_t num_poly_vertices, const cspt_instance_params* params, cspt_dtype dtype,
-  cspt_method method, int block_threads, const cspt_allocator* mr, void* stream,
-  cspt_batched_pip** out_plan);
+  cspt_method method, int ordered_index, int block_threads, const cspt_allocator* mr,
+  void* stream, cspt_batched_pip** out_plan);
 
 /* Evaluates all instances on `stream` (asynchronous; allocates nothing).
  * With use_graph != 0 the evaluation is recorded into a CUDA graph on the

@@ -104,12 +104,14 @@ def _check_plan(plan, wl, params, method, expect=None):
     return out
 
 
+@pytest.mark.parametrize("ordered", [True, False])
 @pytest.mark.parametrize("method", ["exact", "filtered"])
-def test_batched_matches_single_instance_calls(method):
+def test_batched_matches_single_instance_calls(method, ordered):
+    # ordered=False: the one-shot polygon index and its quadrant fast path
     wl, params = _workload(24, seed=1)
     plan = BatchedPointInPolygon(torch.from_numpy(wl.x).cuda(), torch.from_numpy(wl.y).cuda(),
                                  wl.point_offsets, _polygons(wl), wl.polygon_offsets, params,
-                                 method=method)
+                                 method=method, ordered_index=ordered)
     plan.run(graph=False)
     torch.cuda.synchronize()
     expect = _check_plan(plan, wl, params, method)
