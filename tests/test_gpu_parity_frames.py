@@ -202,3 +202,35 @@ def test_nearest_frames_beyond_float32_grid_range(method):
                    expansion_radius=3.0)
     orr = _nearest_vs_oracle(w, method, 3, 64)
     assert int((orr["linestring_index"] != 0xFFFFFFFF).sum()) > 10_000
+
+
+def _dense_quadrant_workload(n_points, depth, max_size, seed):
+    """Polygons of 1,000 to 4,000 vertices (per-vertex radius factor
+    U[0.5, 1]: deep spikes, dozens of entries per slab) under a coarse tree,
+    so a quadrant spans more than 31 slabs or lists more edges than one warp's
+    list pool holds: such quadrants leave the quadrant classification for the
+    per-point slab walk, beside quadrants that stay on it."""
+    rng = np.random.default_rng(seed)
+    n_poly = 40
+    centers = rng.uniform(100.0, 900.0, (n_poly, 2))
+    P = D.star_polygons(rng, centers, rng.integers(1000, 4000, n_poly),
+                        lambda g, pid: g.uniform(40.0, 120.0, len(pid)) * g.uniform(0.5, 1.0, len(pid)),
+                        hole_fraction=0.2)
+    x = rng.uniform(0.0, 1000.0, n_points)
+    y = rng.uniform(0.0, 1000.0, n_points)
+    nb = n_points // 100
+    sel = rng.choice(n_points, nb, replace=False)
+    bx, by = D._near_boundary(rng, P, nb)
+    x[sel], y[sel] = bx, by
+    return D.Workload("dense_quadrants", x, y, 0.0, 1000.0, 0.0, 1000.0, 1000.0 / 2 ** depth,
+                      depth, max_size, polygons=P)
+
+
+@pytest.mark.parametrize("method", METHODS)
+@pytest.mark.parametrize("depth,max_size", [(5, 1024), (4, 2048), (7, 256)])
+def test_dense_quadrants(method, depth, max_size):
+    w = _dense_quadrant_workload(400_000, depth, max_size, seed=47 + depth)
+    r, refined = _pip_vs_oracle(w, method)
+    assert int(r["polygon_index"].numel()) > 10_000
+    if method == "filtered":
+        assert refined > 0
