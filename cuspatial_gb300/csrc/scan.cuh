@@ -91,27 +91,49 @@ __global__ void __launch_bounds__(1024) scan_partials_kernel(T* partials, size_t
 }
 
 // Calls out(i, exclusive_prefix_of_i, in(i)) for every i in [0, n).
+// Items are read and handed to `out` in striped order (item j * 256 + t of
+// the tile by thread t: coalesced), and scanned in blocked order (thread t
+// owns items [8 t, 8 t + 8)) through a shared-memory transpose padded by one
+// word per 32 (no bank conflicts for 4-byte items).
 template <typename T, typename InF, typename OutF>
 __global__ void __launch_bounds__(kScanBlock)
   scan_down_kernel(InF in, OutF out, size_t n, T const* partials)
 {
+  __shared__ T s_items[kScanTile + kScanTile / 32];
   size_t const base = static_cast<size_t>(blockIdx.x) * kScanTile;
-  // blocked arrangement: thread t owns items [t*ITEMS, t*ITEMS+ITEMS)
+  T sv[kScanItems];  // this thread's items, striped
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    uint32_t const li = static_cast<uint32_t>(j) * kScanBlock + threadIdx.x;
+    size_t const i    = base + li;
+    sv[j]             = i < n ? in(i) : T{0};
+    s_items[li + (li >> 5)] = sv[j];
+  }
+  __syncthreads();
   T vals[kScanItems];
   T s = 0;
 #pragma unroll
   for (int j = 0; j < kScanItems; ++j) {
-    size_t const i = base + static_cast<size_t>(threadIdx.x) * kScanItems + j;
-    vals[j]        = i < n ? in(i) : T{0};
+    uint32_t const li = threadIdx.x * kScanItems + static_cast<uint32_t>(j);
+    vals[j]           = s_items[li + (li >> 5)];
     s += vals[j];
   }
   __shared__ T total;
   T run = block_exclusive_scan<T, kScanBlock>(s, &total) + partials[blockIdx.x];
+  // block_exclusive_scan ends with a barrier: every thread has read its
+  // items before the prefixes overwrite them
 #pragma unroll
   for (int j = 0; j < kScanItems; ++j) {
-    size_t const i = base + static_cast<size_t>(threadIdx.x) * kScanItems + j;
-    if (i < n) out(i, run, vals[j]);
+    uint32_t const li       = threadIdx.x * kScanItems + static_cast<uint32_t>(j);
+    s_items[li + (li >> 5)] = run;
     run += vals[j];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    uint32_t const li = static_cast<uint32_t>(j) * kScanBlock + threadIdx.x;
+    size_t const i    = base + li;
+    if (i < n) out(i, s_items[li + (li >> 5)], sv[j]);
   }
 }
 
