@@ -453,12 +453,15 @@ def test_host_rows(method):
         np.testing.assert_array_equal(hp[:n].numpy().view(np.uint32), orr["polygon_index"])
         np.testing.assert_array_equal(hq[:n].numpy().view(np.uint32), orr["point_index"])
         assert hp[n:].tolist() == [-1] * 5
-    # too few rows: the count comes back with the error
+    # too few rows: the count comes back with the error (page-locked and
+    # pageable arrays)
+    for pinned in (True, False):
+        small = torch.full((m - 1,), -1, dtype=torch.int32, pin_memory=pinned)
+        with pytest.raises(cs.HostRowsTooFew) as e:
+            cs.quadtree_point_in_polygon_host(j, t, pi, pts, polys, small, small.clone(),
+                                              method=method)
+        assert e.value.rows == m and str(m) in str(e.value)
     small = torch.empty(m - 1, dtype=torch.int32)
-    with pytest.raises(cs.HostRowsTooFew) as e:
-        cs.quadtree_point_in_polygon_host(j, t, pi, pts, polys, small, small.clone(),
-                                          method=method)
-    assert e.value.rows == m and str(m) in str(e.value)
     # no pairs: nothing is written
     none = {"bbox_offset": j["bbox_offset"][:0], "quad_offset": j["quad_offset"][:0]}
     assert cs.quadtree_point_in_polygon_host(none, t, pi, pts, polys, small, small.clone(),
