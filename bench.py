@@ -547,7 +547,35 @@ def run_ours(args, dist):
             h2d = (hx.numel() + hy.numel() + hpxy.numel()) * 8 + (hro.numel() + hpo.numel() +
                                                                    hgo.numel()) * 4
             d2h = 2 * m * 4
-        e2e_ms = dist.max(statistics.mean(ems))
+        sep_same = bool(m == M0 and torch.equal(o1[:m], res["polygon_index"].cpu()) and
+                        torch.equal(o2[:m], res["point_index"].cpu()))
+        # the same join through the one-call host entry point: the polygons'
+        # copy, boxes and index run beside the quadtree build
+        hpo32 = torch.from_numpy(P.part_offset.astype(np.int32)).pin_memory()
+        hro32 = torch.from_numpy(P.ring_offset.astype(np.int32)).pin_memory()
+        hpx = torch.from_numpy(np.ascontiguousarray(P.x)).pin_memory()
+        hpy = torch.from_numpy(np.ascontiguousarray(P.y)).pin_memory()
+        jms = []
+        for it in range(args.e2e_steps + 1):
+            a, b = ev(), ev()
+            a.record(stream)
+            mj = cs.point_in_polygon_join_host(hx, hy, w.x_min, w.x_max, w.y_min, w.y_max,
+                                               w.scale, w.max_depth, w.max_size, hpo32, hro32,
+                                               hpx, hpy, o1, o2, method=args.method)
+            b.record(stream)
+            b.synchronize()
+            if it > 0:
+                jms.append(a.elapsed_time(b))
+        # its point column holds input point ids: point_indices[point_index]
+        joined_same = bool(mj == M0 and torch.equal(o1[:mj], res["polygon_index"].cpu()) and
+                           torch.equal(o2[:mj], pi.long()[res["point_index"].long()].int().cpu()))
+        sep_ms = dist.max(statistics.mean(ems))
+        join_ms = dist.max(statistics.mean(jms))
+        e2e_ms = min(sep_ms, join_ms)
+        if join_ms <= sep_ms:  # the one call's own copies
+            h2d = (hx.numel() + hy.numel() + hpx.numel() + hpy.numel()) * 8 + (
+                hpo32.numel() + hro32.numel()) * 4
+            d2h = 2 * mj * 4
         # lower bounds of one e2e step: its copies at the link's measured
         # rates (the two directions do not overlap each other here), and its
         # device work (point index build + the step)
@@ -557,14 +585,15 @@ def run_ours(args, dist):
         e2e = {"value": n * args.gpus / (e2e_ms / 1e3), "unit": "points/s",
                "ms_per_step": e2e_ms, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "link": link,
-               "api": "quadtree_on_points_host (ordered), polygon_bounding_boxes, "
-                      "join_quadtree_and_bounding_boxes, quadtree_point_in_polygon_host",
-               "phases_ms": dict(zip(["polygons_h2d", "points_h2d_and_quadtree_build",
-                                      "boxes_join", "pip_and_d2h"],
-                                     [statistics.mean(p[k] for p in phases) for k in range(4)])),
-               "pairs_identical": bool(m == M0 and
-                                       torch.equal(o1[:m], res["polygon_index"].cpu()) and
-                                       torch.equal(o2[:m], res["point_index"].cpu()))}
+               "api": ("point_in_polygon_join_host (one call)" if join_ms <= sep_ms else
+                       "quadtree_on_points_host (ordered), polygon_bounding_boxes, "
+                       "join_quadtree_and_bounding_boxes, quadtree_point_in_polygon_host"),
+               "one_call_ms": join_ms, "one_call_rows_identical": joined_same,
+               "separate_calls_ms": sep_ms,
+               "separate_calls_phases_ms": dict(zip(
+                   ["polygons_h2d", "points_h2d_and_quadtree_build", "boxes_join",
+                    "pip_and_d2h"], [statistics.mean(p[k] for p in phases) for k in range(4)])),
+               "pairs_identical": joined_same and sep_same}
 
     cpu = None
     if dist.rank == 0 and args.gpus == 1 and not args.no_cpu:

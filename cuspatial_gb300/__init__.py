@@ -13,7 +13,8 @@ from .api import (HostRowsTooFew, join_quadtree_and_bounding_boxes, last_edge_fr
                   last_refined_count,
                   linestring_bounding_boxes, pairwise_point_in_polygon,
                   pairwise_point_linestring_distance, pairwise_point_linestring_nearest_points,
-                  point_in_polygon, point_in_polygon_bitmask, points_in_quadtree_order,
+                  point_in_polygon, point_in_polygon_bitmask, point_in_polygon_join_host,
+                  points_in_quadtree_order,
                   polygon_bounding_boxes, quadtree_on_points, quadtree_on_points_host, quadtree_on_points_ordered,
                   quadtree_point_in_polygon,
                   quadtree_point_in_polygon_host, quadtree_point_to_nearest_linestring)
@@ -35,6 +36,7 @@ __all__ = [
     "pairwise_point_linestring_nearest_points",
     "point_in_polygon",
     "point_in_polygon_bitmask",
+    "point_in_polygon_join_host",
     "points_in_quadtree_order",
     "polygon_bounding_boxes",
     "polygons_contains_properly",

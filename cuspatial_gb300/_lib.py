@@ -118,6 +118,11 @@ def _declare(lib):
         _vp, _vp, _sz, ctypes.POINTER(CsptQuadtree), _vp, _sz, _vp, _vp, _sz, _vp, _sz, _vp, _sz,
         _vp, _vp, _sz, ctypes.c_int, ctypes.c_int, ctypes.POINTER(CsptAllocator), _vp, _vp, _vp,
         _sz, ctypes.POINTER(_sz)]
+    lib.cspt_point_in_polygon_join_host.argtypes = [
+        _vp, _vp, _sz, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+        ctypes.c_double, ctypes.c_double, ctypes.c_int8, ctypes.c_int32, _vp, _sz, _vp, _sz, _vp,
+        _vp, _sz, ctypes.c_int, ctypes.POINTER(CsptAllocator), _vp, _vp, _vp, _sz,
+        ctypes.POINTER(_sz)]
     lib.cspt_quadtree_point_to_nearest_linestring.argtypes = [
         _vp, _vp, _sz, ctypes.POINTER(CsptQuadtree), _vp, _sz, _vp, _vp, _sz, _vp, _sz, _vp, _vp,
         _sz, ctypes.c_int, ctypes.c_int, ctypes.POINTER(CsptAllocator), _vp, _vp, _vp, _vp,
@@ -193,6 +198,7 @@ def _declare(lib):
                  "cspt_polygon_bounding_boxes",
                  "cspt_linestring_bounding_boxes", "cspt_join_quadtree_and_bounding_boxes",
                  "cspt_quadtree_point_in_polygon", "cspt_quadtree_point_in_polygon_host",
+                 "cspt_point_in_polygon_join_host",
                  "cspt_quadtree_point_to_nearest_linestring"):
         getattr(lib, name).restype = ctypes.c_int
     return lib
@@ -244,6 +250,7 @@ class TorchAllocator:
         self.in_use = 0
         self.peak = 0
         self.blocks = {}
+        self._streams = {}  # library streams other than torch's current one
         self._alloc_cb = ALLOC_FN(self._allocate)
         self._free_cb = FREE_FN(self._deallocate)
         self.struct = CsptAllocator(None, self._alloc_cb, self._free_cb)
@@ -253,7 +260,19 @@ class TorchAllocator:
         try:
             if self.budget is not None and self.in_use + nbytes > self.budget:
                 return None
-            t = torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=self.device)
+            # the block belongs to the stream the library will use it on:
+            # torch's caching allocator reuses a freed block only for later
+            # work on that same stream
+            cur = torch.cuda.current_stream(self.device)
+            if stream and int(stream) != cur.cuda_stream:
+                ext = self._streams.get(int(stream))
+                if ext is None:
+                    ext = torch.cuda.ExternalStream(int(stream), device=self.device)
+                    self._streams[int(stream)] = ext
+                with torch.cuda.stream(ext):
+                    t = torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=self.device)
+            else:
+                t = torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=self.device)
         except Exception:  # noqa: BLE001 - out of memory: report NULL to the library
             return None
         p = t.data_ptr()

@@ -376,6 +376,60 @@ def quadtree_point_in_polygon_host(poly_quad_pairs, quadtree, point_indices, poi
     return int(nn.value)
 
 
+def point_in_polygon_join_host(x, y, x_min, x_max, y_min, y_max, scale, max_depth, max_size,
+                               poly_offsets, ring_offsets, poly_x, poly_y, polygon_index_out,
+                               point_index_out, method="exact"):
+    """The whole quadtree point-in-polygon join from host columns to host rows
+    in one call (no counterpart in cuSpatial).
+
+    x, y: the points (float64 or float32 CPU tensors); poly_offsets,
+    ring_offsets (int32), poly_x, poly_y: single-ring-list polygons in the
+    layout quadtree_point_in_polygon reads (part and ring offsets), all on
+    the host, page-locked for the copies to overlap the work.  The rows are
+    those of quadtree_on_points -> polygon_bounding_boxes ->
+    join_quadtree_and_bounding_boxes -> quadtree_point_in_polygon, in that
+    order, with the point column holding each point's index in x / y
+    (point_indices[point_index] of the separate calls).  Corners are ordered
+    and the scale clamped as join_quadtree_and_bounding_boxes does.  Returns
+    the number of rows written; raises HostRowsTooFew when the outputs are
+    too short.
+    """
+    cols = (x, y, poly_offsets, ring_offsets, poly_x, poly_y, polygon_index_out,
+            point_index_out)
+    for t in cols:
+        if not isinstance(t, torch.Tensor) or t.device.type != "cpu" or not t.is_contiguous():
+            raise ValueError("inputs and outputs must be contiguous CPU tensors")
+    if x.dtype != y.dtype or poly_x.dtype != x.dtype or poly_y.dtype != x.dtype:
+        raise TypeError("point and polygon coordinates must share one floating-point dtype")
+    if x.numel() != y.numel() or poly_x.numel() != poly_y.numel():
+        raise ValueError("x and y columns must have the same length")
+    for t in (poly_offsets, ring_offsets, polygon_index_out, point_index_out):
+        if t.dtype != torch.int32:
+            raise TypeError("offsets and outputs must be int32")
+    x_min, x_max = min(x_min, x_max), max(x_min, x_max)
+    y_min, y_max = min(y_min, y_max), max(y_min, y_max)
+    min_scale = max(x_max - x_min, y_max - y_min) / ((1 << max_depth) + 2)
+    if scale < min_scale:
+        warnings.warn("scale {} is less than required minimum ".format(scale) +
+                      "scale {}. Clamping to minimum scale".format(min_scale))
+    cap = min(int(polygon_index_out.numel()), int(point_index_out.numel()))
+    lib = _lib.load()
+    alloc = _lib.TorchAllocator(torch.device("cuda", torch.cuda.current_device()))
+    nn = ctypes.c_size_t()
+    status = lib.cspt_point_in_polygon_join_host(
+        x.data_ptr(), y.data_ptr(), int(x.numel()), _dtype_code(x), float(x_min), float(x_max),
+        float(y_min), float(y_max), float(scale), int(max_depth), int(max_size),
+        poly_offsets.data_ptr(), int(poly_offsets.numel()), ring_offsets.data_ptr(),
+        int(ring_offsets.numel()), poly_x.data_ptr(), poly_y.data_ptr(), int(poly_x.numel()),
+        _METHODS[method], alloc.ref, _lib.stream_ptr(),
+        polygon_index_out.data_ptr() if cap else None,
+        point_index_out.data_ptr() if cap else None, cap, ctypes.byref(nn))
+    if status != _lib.OK and int(nn.value) > cap:
+        raise HostRowsTooFew(lib.cspt_last_error_message().decode(), int(nn.value))
+    _lib.check(status, lib)
+    return int(nn.value)
+
+
 def quadtree_point_to_nearest_linestring(linestring_quad_pairs, quadtree, point_indices,
                                          points: GeoSeries, linestrings: GeoSeries,
                                          method="exact", ordered_points=None):

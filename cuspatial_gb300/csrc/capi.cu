@@ -1,6 +1,7 @@
 // extern "C" entry points: argument validation and empty-input rules of the
 // libcuspatial column API, then dispatch to the kernels.
 #include <atomic>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -21,7 +22,15 @@ void quadtree_on_points_from_host(void const* host_x, void const* host_y, void* 
                                   double x_max, double y_min, double y_max, double scale,
                                   int max_depth, int32_t max_size, Allocator const& alloc,
                                   uint32_t** out_point_indices, cspt_quadtree* out_tree,
-                                  void* ordered = nullptr);
+                                  void* ordered                                    = nullptr,
+                                  std::function<void(cudaStream_t)> const* after_copies = nullptr);
+void point_in_polygon_join_host(void const* hx, void const* hy, size_t n, cspt_dtype dtype,
+                                double x_min, double x_max, double y_min, double y_max,
+                                double scale, int max_depth, int32_t max_size,
+                                uint32_t const* hpo, size_t npo, uint32_t const* hro,
+                                size_t nro, void const* hvx, void const* hvy, size_t nv,
+                                cspt_method method, cspt_allocator const* mr, cudaStream_t s,
+                                HostRows const& out, size_t* out_n, uint64_t* out_refined);
 uint64_t& last_fallbacks();
 uint64_t& last_group_scans();
 uint64_t& last_f64_segments();
@@ -129,10 +138,10 @@ int num_sms()
   return n;
 }
 
-cudaStream_t side_stream()
+cudaStream_t side_stream(int k)
 {
   struct Streams {
-    std::vector<cudaStream_t> by_device;
+    std::vector<cudaStream_t> by_device;  // kSideStreams per device
     ~Streams()
     {
       for (cudaStream_t st : by_device)
@@ -140,12 +149,14 @@ cudaStream_t side_stream()
     }
   };
   thread_local Streams t;
+  CSPT_EXPECTS(k >= 0 && k < kSideStreams, "side stream index out of range");
   int dev = 0;
   CSPT_CUDA_TRY(cudaGetDevice(&dev));
-  if (static_cast<size_t>(dev) >= t.by_device.size()) t.by_device.resize(dev + 1, nullptr);
-  if (!t.by_device[dev])
-    CSPT_CUDA_TRY(cudaStreamCreateWithFlags(&t.by_device[dev], cudaStreamNonBlocking));
-  return t.by_device[dev];
+  size_t const i = static_cast<size_t>(dev) * kSideStreams + static_cast<size_t>(k);
+  if (i >= t.by_device.size()) t.by_device.resize(i + 1, nullptr);
+  if (!t.by_device[i])
+    CSPT_CUDA_TRY(cudaStreamCreateWithFlags(&t.by_device[i], cudaStreamNonBlocking));
+  return t.by_device[i];
 }
 
 void stream_wait(cudaStream_t waiter, cudaStream_t on)
@@ -565,6 +576,51 @@ cspt_status cspt_quadtree_point_in_polygon_host(
                               ring_offsets, num_ring_offsets, poly_x, poly_y, num_poly_vertices,
                               dtype, method, alloc, nullptr, nullptr, out_num_pairs, &refined,
                               &host);
+    t_last_refined = refined;
+  });
+}
+
+cspt_status cspt_point_in_polygon_join_host(
+  const void* host_x, const void* host_y, size_t num_points, cspt_dtype dtype, double x_min,
+  double x_max, double y_min, double y_max, double scale, int8_t max_depth, int32_t max_size,
+  const uint32_t* host_poly_offsets, size_t num_poly_offsets, const uint32_t* host_ring_offsets,
+  size_t num_ring_offsets, const void* host_poly_x, const void* host_poly_y,
+  size_t num_poly_vertices, cspt_method method, const cspt_allocator* mr, void* stream,
+  uint32_t* host_polygon_index, uint32_t* host_point_index, size_t host_capacity,
+  size_t* out_num_rows)
+{
+  return guarded([&] {
+    CSPT_EXPECTS(out_num_rows, "output pointers must not be null");
+    *out_num_rows  = 0;
+    t_last_refined = 0;
+    check_dtype(dtype);
+    CSPT_EXPECTS(method == CSPT_METHOD_EXACT || method == CSPT_METHOD_FILTERED,
+                 "unknown point-in-polygon method");
+    CSPT_EXPECTS(host_capacity == 0 || (host_polygon_index && host_point_index),
+                 "host output arrays must not be null");
+    // join.py:163-180: corners ordered, scale clamped to the tree's minimum;
+    // then quadtree_bbox_filtering.cu:100-106
+    double const x0 = x_min < x_max ? x_min : x_max, x1 = x_min < x_max ? x_max : x_min;
+    double const y0 = y_min < y_max ? y_min : y_max, y1 = y_min < y_max ? y_max : y_min;
+    CSPT_EXPECTS(max_depth > 0 && max_depth < 16,
+                 "maximum depth must be positive and less than 16");
+    double const span      = (x1 - x0) > (y1 - y0) ? (x1 - x0) : (y1 - y0);
+    double const min_scale = span / static_cast<double>((1 << max_depth) + 2);
+    double const sc        = scale > min_scale ? scale : min_scale;
+    CSPT_EXPECTS(sc > 0, "scale must be positive");
+    CSPT_EXPECTS(x0 < x1 && y0 < y1, "invalid bounding box (x_min, x_max, y_min, y_max)");
+    if (num_points == 0 || num_poly_offsets < 2 || num_ring_offsets < 2 ||
+        num_poly_vertices == 0)
+      return;
+    CSPT_EXPECTS(host_x && host_y && host_poly_offsets && host_ring_offsets && host_poly_x &&
+                   host_poly_y,
+                 "input columns must not be null");
+    uint64_t refined = 0;
+    HostRows const host{host_polygon_index, host_point_index, host_capacity};
+    point_in_polygon_join_host(host_x, host_y, num_points, dtype, x0, x1, y0, y1, sc, max_depth,
+                               max_size, host_poly_offsets, num_poly_offsets, host_ring_offsets,
+                               num_ring_offsets, host_poly_x, host_poly_y, num_poly_vertices,
+                               method, mr, as_stream(stream), host, out_num_rows, &refined);
     t_last_refined = refined;
   });
 }

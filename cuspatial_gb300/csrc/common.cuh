@@ -176,6 +176,15 @@ class Buffer {
   }
   T* data() const { return p_; }
   size_t size() const { return n_; }
+  // takes ownership of n elements at p, allocated from a
+  static Buffer adopt(Allocator const& a, T* p, size_t n)
+  {
+    Buffer b;
+    b.a_ = &a;
+    b.p_ = p;
+    b.n_ = n;
+    return b;
+  }
 
  private:
   Allocator const* a_ = nullptr;
@@ -206,10 +215,13 @@ int num_sms();
 // Grid cap of `per_sm` blocks on every SM of the current device.
 inline unsigned sm_grid(unsigned per_sm) { return static_cast<unsigned>(num_sms()) * per_sm; }
 
-// A second stream of the calling thread on the current device, for work that
+// Extra streams of the calling thread on the current device, for work that
 // overlaps the caller's stream inside one call (created on first use;
-// non-blocking with respect to the legacy default stream).
-cudaStream_t side_stream();
+// non-blocking with respect to the legacy default stream).  Stream 0 serves
+// the copies and side kernels of a single call; stream 1 the polygon work a
+// combined call runs beside a single call's streams.
+constexpr int kSideStreams = 2;
+cudaStream_t side_stream(int k = 0);
 
 // Makes `waiter` wait for everything enqueued on `on` so far.
 void stream_wait(cudaStream_t waiter, cudaStream_t on);

@@ -19,6 +19,9 @@
 //   filtered : the same edges in float32 on anchored coordinates with a
 //              forward error bound; any undecided edge sends the candidate
 //              to the exact test.
+#include <functional>
+#include <memory>
+
 #include "common.cuh"
 #include "leaf_frame.cuh"
 #include "pip_test.cuh"
@@ -597,7 +600,7 @@ __global__ void __launch_bounds__(256)
                     uint32_t const* __restrict__ qoff, uint64_t const* __restrict__ word_off,
                     uint32_t const* __restrict__ bits, uint64_t const* __restrict__ out_off,
                     uint32_t* __restrict__ out_poly, uint32_t* __restrict__ out_point,
-                    uint64_t cap)
+                    uint64_t cap, uint32_t const* __restrict__ id_map)
 {
   int const lane     = threadIdx.x & 31;
   unsigned const lt  = (1u << lane) - 1u;
@@ -615,8 +618,9 @@ __global__ void __launch_bounds__(256)
       if (w & (1u << lane)) {
         uint64_t const d = o + __popc(w & lt);
         if (d < cap) {
-          out_poly[d]  = poly;
-          out_point[d] = off + c + lane;
+          uint32_t const pos = off + c + lane;
+          out_poly[d]        = poly;
+          out_point[d]       = id_map ? id_map[pos] : pos;
         }
       }
       o += __popc(w);
@@ -630,7 +634,8 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
          T const* y, uint32_t const* po, size_t npo, uint32_t const* ro, size_t nro,
          T const* vx, T const* vy, size_t nv, cspt_method method, Allocator const& alloc,
          uint32_t** out_poly, uint32_t** out_point, size_t* out_n, uint64_t* out_refined,
-         HostRows const* host, T const* ordered)
+         HostRows const* host, T const* ordered, PolygonIndex<T>* prebuilt = nullptr,
+         uint32_t const* id_map = nullptr)
 {
   cudaStream_t const s = alloc.stream();
   PointSource<T> const src{point_indices, x, y, ordered};
@@ -681,7 +686,11 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
   // (destroyed before the index and the buffers above, also on an
   // exception) orders the rest of the call after them.  Nothing here waits
   // on the host.
-  PolygonIndex<T> index(po, npo, ro, nro, vx, vy, nv, filtered, alloc, false, filtered);
+  // (a prebuilt index, filled, may come with the call)
+  std::unique_ptr<PolygonIndex<T>> own;
+  if (!prebuilt)
+    own.reset(new PolygonIndex<T>(po, npo, ro, nro, vx, vy, nv, filtered, alloc, false, filtered));
+  PolygonIndex<T>& index  = prebuilt ? *prebuilt : *own;
   cudaStream_t const side = filtered ? side_stream() : nullptr;
   StreamJoin join(s, side);
   if constexpr (std::is_same<T, double>::value) {
@@ -694,7 +703,7 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
       CSPT_CHECK_LAUNCH();
     }
   }
-  index.fill();
+  if (!prebuilt) index.fill();
   join.join();
   // the bitmask's size: the one read-back before the evaluation, taken once
   // the index and the frames are queued, so the device stays busy meanwhile
@@ -739,7 +748,7 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
     KernelTimer timer("pip_expand", s);
     pip_expand_kernel<<<grid_for(n * 32, blk, sm_grid(8u * 4u)), blk, 0, s>>>(
       pair_poly + k0, pair_quad + k0, n, qlen, qoff, word_off.data() + k0, bits.data(),
-      out_off.data(), op, oq, m);
+      out_off.data(), op, oq, m, id_map);
     CSPT_CHECK_LAUNCH();
   };
 
@@ -929,7 +938,7 @@ class PipExec::Impl {
     unsigned const blk = blk_;
     unsigned const grd = grid_for(np_ * 32, blk, sm_grid(8u * 1024u / blk));
     pip_expand_kernel<<<grd, blk, 0, s>>>(pp_, pq_, np_, qlen_, qoff_, word_off_.data(),
-                                          bits_.data(), out_off_.data(), op, oq, cap);
+                                          bits_.data(), out_off_.data(), op, oq, cap, nullptr);
     CSPT_CHECK_LAUNCH();
     overflow_kernel<<<1, 1, 0, s>>>(out_off_.data() + np_, cap, flag_.data());
     CSPT_CHECK_LAUNCH();
@@ -1009,6 +1018,120 @@ void quadtree_point_in_polygon(uint32_t const* pair_poly, uint32_t const* pair_q
                static_cast<float const*>(x), static_cast<float const*>(y), po, npo, ro, nro,
                static_cast<float const*>(vx), static_cast<float const*>(vy), nv, method, alloc,
                out_poly, out_point, out_n, out_refined, host, static_cast<float const*>(ordered));
+}
+
+// defined in the other kernel translation units
+void quadtree_on_points_from_host(void const* host_x, void const* host_y, void* dev_x,
+                                  void* dev_y, size_t n, cspt_dtype dtype, double x_min,
+                                  double x_max, double y_min, double y_max, double scale,
+                                  int max_depth, int32_t max_size, Allocator const& alloc,
+                                  uint32_t** out_point_indices, cspt_quadtree* out_tree,
+                                  void* ordered,
+                                  std::function<void(cudaStream_t)> const* after_copies);
+void polygon_bounding_boxes(uint32_t const* poly_offsets, size_t npo,
+                            uint32_t const* ring_offsets, size_t nro, void const* x,
+                            void const* y, size_t nv, cspt_dtype dtype, double r, void* ominx,
+                            void* ominy, void* omaxx, void* omaxy, Allocator const& alloc);
+void join_quadtree_and_bounding_boxes(cspt_quadtree const* tree, void const* bminx,
+                                      void const* bminy, void const* bmaxx, void const* bmaxy,
+                                      size_t nb, cspt_dtype dtype, double x_min, double y_min,
+                                      double scale, int max_depth, Allocator const& alloc,
+                                      uint32_t** out_box, uint32_t** out_node, size_t* out_n);
+
+namespace {
+
+// The whole join from host columns to host rows on stream s.  The points go
+// to the device in chunks, each chunk's Morton keys computed as it lands
+// (quadtree_on_points from host); the polygons follow them on the link, and
+// their boxes and index are built on a second stream while the quadtree is
+// built; then the box join and the point-in-polygon test with its rows
+// copied to the host chunk by chunk.  Rows carry input point ids.
+template <typename T>
+void join_host(T const* hx, T const* hy, size_t n, double x_min, double x_max, double y_min,
+               double y_max, double scale, int max_depth, int32_t max_size, uint32_t const* hpo,
+               size_t npo, uint32_t const* hro, size_t nro, T const* hvx, T const* hvy,
+               size_t nv, cspt_method method, cspt_allocator const* mr, cudaStream_t s,
+               HostRows const& out, size_t* out_n, uint64_t* out_refined)
+{
+  cspt_dtype const dtype = std::is_same<T, double>::value ? CSPT_FLOAT64 : CSPT_FLOAT32;
+  bool const filtered    = method == CSPT_METHOD_FILTERED && std::is_same<T, double>::value;
+  size_t const np        = npo - 1;
+  Allocator const alloc(mr, s);
+  cudaStream_t const ps = side_stream(1);
+  Allocator const palloc(mr, ps);
+  // polygon columns, boxes and index: allocated and used on ps, read on s
+  // once s has waited for ps
+  Buffer<uint32_t> dpo(palloc, npo), dro(palloc, nro);
+  Buffer<T> dvx(palloc, nv), dvy(palloc, nv);
+  Buffer<T> bminx(palloc, np), bminy(palloc, np), bmaxx(palloc, np), bmaxy(palloc, np);
+  std::unique_ptr<PolygonIndex<T>> index;
+  // (declared after the polygon buffers: on every exit ps first waits for
+  // s, so the buffers are released on ps only after s's last use of them)
+  StreamJoin ps_after_s(ps, s);
+  Buffer<T> dx(alloc, n), dy(alloc, n), oxy(alloc, 2 * n);
+  std::function<void(cudaStream_t)> const after_points = [&](cudaStream_t copy) {
+    stream_wait(ps, copy);  // behind the points on the host link
+    CSPT_CUDA_TRY(cudaMemcpyAsync(dpo.data(), hpo, npo * sizeof(uint32_t),
+                                  cudaMemcpyHostToDevice, ps));
+    CSPT_CUDA_TRY(cudaMemcpyAsync(dro.data(), hro, nro * sizeof(uint32_t),
+                                  cudaMemcpyHostToDevice, ps));
+    CSPT_CUDA_TRY(cudaMemcpyAsync(dvx.data(), hvx, nv * sizeof(T), cudaMemcpyHostToDevice, ps));
+    CSPT_CUDA_TRY(cudaMemcpyAsync(dvy.data(), hvy, nv * sizeof(T), cudaMemcpyHostToDevice, ps));
+    polygon_bounding_boxes(dpo.data(), npo, dro.data(), nro, dvx.data(), dvy.data(), nv, dtype,
+                           0.0, bminx.data(), bminy.data(), bmaxx.data(), bmaxy.data(), palloc);
+    index.reset(new PolygonIndex<T>(dpo.data(), npo, dro.data(), nro, dvx.data(), dvy.data(), nv,
+                                    filtered, palloc, false, false));
+  };
+  uint32_t* pi_raw = nullptr;
+  cspt_quadtree tree{nullptr, nullptr, nullptr, nullptr, nullptr, 0};
+  quadtree_on_points_from_host(hx, hy, dx.data(), dy.data(), n, dtype, x_min, x_max, y_min,
+                               y_max, scale, max_depth, max_size, alloc, &pi_raw, &tree,
+                               oxy.data(), &after_points);
+  Buffer<uint32_t> pidx = Buffer<uint32_t>::adopt(alloc, pi_raw, n);
+  size_t const q        = tree.num_nodes;
+  Buffer<uint32_t> tkey = Buffer<uint32_t>::adopt(alloc, const_cast<uint32_t*>(tree.key), q);
+  Buffer<uint8_t> tlev  = Buffer<uint8_t>::adopt(alloc, const_cast<uint8_t*>(tree.level), q);
+  Buffer<uint8_t> tint = Buffer<uint8_t>::adopt(alloc, const_cast<uint8_t*>(tree.is_internal_node), q);
+  Buffer<uint32_t> tlen = Buffer<uint32_t>::adopt(alloc, const_cast<uint32_t*>(tree.length), q);
+  Buffer<uint32_t> toff = Buffer<uint32_t>::adopt(alloc, const_cast<uint32_t*>(tree.offset), q);
+  CSPT_EXPECTS(index != nullptr, "the polygons were not queued behind the points");
+  stream_wait(s, ps);  // boxes and index
+  uint32_t* pb_raw = nullptr;
+  uint32_t* pq_raw = nullptr;
+  size_t npairs    = 0;
+  if (q > 0)
+    join_quadtree_and_bounding_boxes(&tree, bminx.data(), bminy.data(), bmaxx.data(),
+                                     bmaxy.data(), np, dtype, x_min, y_min, scale, max_depth,
+                                     alloc, &pb_raw, &pq_raw, &npairs);
+  Buffer<uint32_t> pair_poly = Buffer<uint32_t>::adopt(alloc, pb_raw, npairs);
+  Buffer<uint32_t> pair_quad = Buffer<uint32_t>::adopt(alloc, pq_raw, npairs);
+  *out_n = 0;
+  if (npairs == 0) return;
+  run<T>(pair_poly.data(), pair_quad.data(), npairs, &tree, pidx.data(), n, dx.data(), dy.data(),
+         dpo.data(), npo, dro.data(), nro, dvx.data(), dvy.data(), nv, method, alloc, nullptr,
+         nullptr, out_n, out_refined, &out, oxy.data(), index.get(), pidx.data());
+}
+
+}  // namespace
+
+void point_in_polygon_join_host(void const* hx, void const* hy, size_t n, cspt_dtype dtype,
+                                double x_min, double x_max, double y_min, double y_max,
+                                double scale, int max_depth, int32_t max_size,
+                                uint32_t const* hpo, size_t npo, uint32_t const* hro,
+                                size_t nro, void const* hvx, void const* hvy, size_t nv,
+                                cspt_method method, cspt_allocator const* mr, cudaStream_t s,
+                                HostRows const& out, size_t* out_n, uint64_t* out_refined)
+{
+  if (dtype == CSPT_FLOAT64)
+    join_host<double>(static_cast<double const*>(hx), static_cast<double const*>(hy), n, x_min,
+                      x_max, y_min, y_max, scale, max_depth, max_size, hpo, npo, hro, nro,
+                      static_cast<double const*>(hvx), static_cast<double const*>(hvy), nv,
+                      method, mr, s, out, out_n, out_refined);
+  else
+    join_host<float>(static_cast<float const*>(hx), static_cast<float const*>(hy), n, x_min,
+                     x_max, y_min, y_max, scale, max_depth, max_size, hpo, npo, hro, nro,
+                     static_cast<float const*>(hvx), static_cast<float const*>(hvy), nv, method,
+                     mr, s, out, out_n, out_refined);
 }
 
 }  // namespace cspt

@@ -15,6 +15,7 @@
 // remove_unqualified_quads rule (phase_2.cuh:206-236).  Leaves keep the first
 // sorted position they cover, which is what the reference's flattened-key
 // scan (phase_2.cuh:98-141) produces.
+#include <functional>
 #include <limits>
 #include <vector>
 
@@ -244,13 +245,16 @@ __global__ void __launch_bounds__(256)
 // Host input: the points are copied from host memory (hx, hy) into the
 // caller's device arrays (dx, dy, which build() then reads as x and y) in
 // chunks on a second stream, and the Morton keys of each chunk are computed
-// as soon as its copy has landed.
+// as soon as its copy has landed.  after_copies (may be null) is called with
+// that stream once the points' copies are enqueued, so that a caller can
+// queue more work behind them.
 template <typename T>
 struct HostInput {
   T const* hx;
   T const* hy;
   T* dx;
   T* dy;
+  std::function<void(cudaStream_t)> const* after_copies;
 };
 constexpr size_t kHostChunks = 8;
 
@@ -311,6 +315,7 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
         xy0 ? xy0 + 2 * i0 : nullptr);
       CSPT_CHECK_LAUNCH();
     }
+    if (host->after_copies) (*host->after_copies)(copy);
     copies.join();
   }
   // cells reach 2^d + 2, so the key needs 2(d+1) bits (2(d+2) below d = 2)
@@ -562,17 +567,19 @@ void quadtree_on_points_from_host(void const* host_x, void const* host_y, void* 
                                   double x_max, double y_min, double y_max, double scale,
                                   int max_depth, int32_t max_size, Allocator const& alloc,
                                   uint32_t** out_point_indices, cspt_quadtree* out_tree,
-                                  void* ordered)
+                                  void* ordered,
+                                  std::function<void(cudaStream_t)> const* after_copies)
 {
   if (dtype == CSPT_FLOAT64) {
     HostInput<double> const h{static_cast<double const*>(host_x),
                               static_cast<double const*>(host_y), static_cast<double*>(dev_x),
-                              static_cast<double*>(dev_y)};
+                              static_cast<double*>(dev_y), after_copies};
     build<double>(h.dx, h.dy, n, x_min, x_max, y_min, y_max, scale, max_depth, max_size, alloc,
                   out_point_indices, out_tree, &h, static_cast<double*>(ordered));
   } else {
     HostInput<float> const h{static_cast<float const*>(host_x), static_cast<float const*>(host_y),
-                             static_cast<float*>(dev_x), static_cast<float*>(dev_y)};
+                             static_cast<float*>(dev_x), static_cast<float*>(dev_y),
+                             after_copies};
     build<float>(h.dx, h.dy, n, x_min, x_max, y_min, y_max, scale, max_depth, max_size, alloc,
                  out_point_indices, out_tree, &h, static_cast<float*>(ordered));
   }

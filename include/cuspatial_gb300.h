@@ -51,7 +51,11 @@ typedef enum { CSPT_FLOAT32 = 0, CSPT_FLOAT64 = 1 } cspt_dtype;
 typedef enum { CSPT_METHOD_EXACT = 0, CSPT_METHOD_FILTERED = 1 } cspt_method;
 
 /* Device allocator.  allocate must return 256-byte aligned device memory or
- * NULL; deallocate receives the same size and stream. */
+ * NULL; deallocate receives the same size and stream.  Memory is
+ * stream-ordered: a block allocated for `stream` is used only by work on that
+ * stream (or by work ordered after it), and once deallocated it may be handed
+ * out again only to work ordered after that stream's pending work (a call
+ * may allocate for more than one stream). */
 typedef struct {
   void* ctx;
   void* (*allocate)(void* ctx, size_t bytes, void* stream);
@@ -268,6 +272,31 @@ cspt_status cspt_quadtree_point_in_polygon(
   const void* poly_x, const void* poly_y, size_t num_poly_vertices, cspt_dtype dtype,
   cspt_method method, const cspt_allocator* mr, void* stream, uint32_t** out_polygon_index,
   uint32_t** out_point_index, size_t* out_num_pairs);
+
+/*
+ * The whole quadtree point-in-polygon join, host columns in and host rows
+ * out, in one call: cspt_quadtree_on_points_host, polygon bounding boxes,
+ * cspt_join_quadtree_and_bounding_boxes and
+ * cspt_quadtree_point_in_polygon_host with the corners ordered and the scale
+ * clamped as the reference's Python join does (join.py:163-180).  The
+ * polygons' copy, boxes and slab index run on a second stream while the
+ * quadtree is built from the points; rows go to host_polygon_index and
+ * host_point_index (host_capacity each) chunk by chunk.  Rows are those of
+ * the separate calls, in their order, except that the point column holds
+ * each point's row in the input columns (point_indices[point_index] of the
+ * separate calls; the quadtree itself stays internal).  *out_num_rows
+ * receives the row count; above host_capacity the call returns
+ * CSPT_INVALID_ARGUMENT.  Host arrays should be page-locked for the copies
+ * to overlap the work.  No counterpart in the reference.
+ */
+cspt_status cspt_point_in_polygon_join_host(
+  const void* host_x, const void* host_y, size_t num_points, cspt_dtype dtype, double x_min,
+  double x_max, double y_min, double y_max, double scale, int8_t max_depth, int32_t max_size,
+  const uint32_t* host_poly_offsets, size_t num_poly_offsets, const uint32_t* host_ring_offsets,
+  size_t num_ring_offsets, const void* host_poly_x, const void* host_poly_y,
+  size_t num_poly_vertices, cspt_method method, const cspt_allocator* mr, void* stream,
+  uint32_t* host_polygon_index, uint32_t* host_point_index, size_t host_capacity,
+  size_t* out_num_rows);
 
 /*
  * cspt_quadtree_point_in_polygon with the rows written to host memory, for a

@@ -497,3 +497,60 @@ def test_quadtree_from_host(dtype):
     with pytest.raises(TypeError):
         cs.quadtree_on_points_host(torch.zeros(3, dtype=torch.int32),
                                    torch.zeros(3, dtype=torch.int32), *args)
+
+
+@pytest.mark.parametrize("method", METHODS)
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_point_in_polygon_join_host(method, dtype):
+    # the whole join from host columns to host rows in one call: the
+    # oracle's rows, in order, with point ids mapped through its point_indices
+    w = D.precision_at_scale(n_points=1_500_000, n_polygons=8000, extent=3000.0,
+                             max_vertices=128)
+    P = w.polygons
+    px, py = P.x.astype(dtype), P.y.astype(dtype)
+    opi, ot = oracle_tree(w, dtype)
+    oj = O.join_quadtree_and_bounding_boxes(ot, O.polygon_bounding_boxes(
+        P.part_offset, P.ring_offset, px, py), w.x_min, w.x_max, w.y_min, w.y_max, w.scale,
+        w.max_depth)
+    orr = O.quadtree_point_in_polygon(oj, ot, opi, w.x.astype(dtype), w.y.astype(dtype),
+                                      P.part_offset, P.ring_offset, px, py)
+    expect_poly = orr["polygon_index"]
+    expect_point = opi.astype(np.int64)[orr["point_index"].astype(np.int64)].astype(np.uint32)
+    m = len(expect_poly)
+    assert m > 10_000
+
+    def host(a, pinned):
+        t = torch.from_numpy(np.ascontiguousarray(a))
+        return t.pin_memory() if pinned else t
+
+    for pinned in (True, False):
+        cols = [host(w.x.astype(dtype), pinned), host(w.y.astype(dtype), pinned),
+                host(P.part_offset.astype(np.int32), pinned),
+                host(P.ring_offset.astype(np.int32), pinned), host(px, pinned), host(py, pinned)]
+        hp = torch.full((m + 3,), -1, dtype=torch.int32, pin_memory=pinned)
+        hq = torch.full((m + 3,), -1, dtype=torch.int32, pin_memory=pinned)
+        # corners given swapped: ordered as join_quadtree_and_bounding_boxes does
+        n = cs.point_in_polygon_join_host(cols[0], cols[1], w.x_max, w.x_min, w.y_max, w.y_min,
+                                          w.scale, w.max_depth, w.max_size, *cols[2:], hp, hq,
+                                          method=method)
+        assert n == m
+        np.testing.assert_array_equal(hp[:n].numpy().view(np.uint32), expect_poly)
+        np.testing.assert_array_equal(hq[:n].numpy().view(np.uint32), expect_point)
+        assert hp[n:].tolist() == [-1] * 3
+    # too few rows: the count comes back with the error
+    small = torch.empty(m - 1, dtype=torch.int32)
+    with pytest.raises(cs.HostRowsTooFew) as e:
+        cs.point_in_polygon_join_host(cols[0], cols[1], w.x_min, w.x_max, w.y_min, w.y_max,
+                                      w.scale, w.max_depth, w.max_size, *cols[2:], small,
+                                      small.clone(), method=method)
+    assert e.value.rows == m
+    # no points, no polygons: nothing written
+    empty = torch.zeros(0, dtype=cols[0].dtype)
+    assert cs.point_in_polygon_join_host(empty, empty, w.x_min, w.x_max, w.y_min, w.y_max,
+                                         w.scale, w.max_depth, w.max_size, *cols[2:], small,
+                                         small.clone(), method=method) == 0
+    none = torch.zeros(1, dtype=torch.int32)
+    assert cs.point_in_polygon_join_host(cols[0], cols[1], w.x_min, w.x_max, w.y_min, w.y_max,
+                                         w.scale, w.max_depth, w.max_size, none, none,
+                                         cols[4][:0], cols[5][:0], small, small.clone(),
+                                         method=method) == 0
