@@ -566,6 +566,21 @@ def run_ours(args, dist):
             b.synchronize()
             if it > 0:
                 jms.append(a.elapsed_time(b))
+        # one more call with the library's stage timers on (per-stage device
+        # time; stages on the second stream overlap the others)
+        lib.cspt_profile_enable(1)
+        cs.point_in_polygon_join_host(hx, hy, w.x_min, w.x_max, w.y_min, w.y_max, w.scale,
+                                      w.max_depth, w.max_size, hpo32, hro32, hpx, hpy, o1, o2,
+                                      method=args.method)
+        torch.cuda.synchronize()
+        one_call_stages = {}
+        for name in ("quadtree_keys", "quadtree_sort", "quadtree_order", "quadtree_levels",
+                     "bounding_boxes", "polygon_index", "join_count", "join_write",
+                     "leaf_frames", "pip_bits", "pip_expand"):
+            sms, cnt = ctypes.c_double(), ctypes.c_uint64()
+            lib.cspt_profile_read(name.encode(), ctypes.byref(sms), ctypes.byref(cnt))
+            one_call_stages[name] = sms.value
+        lib.cspt_profile_enable(0)
         # its point column holds input point ids: point_indices[point_index]
         joined_same = bool(mj == M0 and torch.equal(o1[:mj], res["polygon_index"].cpu()) and
                            torch.equal(o2[:mj], pi.long()[res["point_index"].long()].int().cpu()))
@@ -589,6 +604,7 @@ def run_ours(args, dist):
                        "quadtree_on_points_host (ordered), polygon_bounding_boxes, "
                        "join_quadtree_and_bounding_boxes, quadtree_point_in_polygon_host"),
                "one_call_ms": join_ms, "one_call_rows_identical": joined_same,
+               "one_call_stages_ms": one_call_stages,
                "separate_calls_ms": sep_ms,
                "separate_calls_phases_ms": dict(zip(
                    ["polygons_h2d", "points_h2d_and_quadtree_build", "boxes_join",
