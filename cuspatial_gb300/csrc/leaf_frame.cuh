@@ -4,6 +4,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "f32_diff.cuh"
 
 namespace cspt {
 namespace {  // one copy per translation unit
@@ -23,8 +24,9 @@ __device__ inline float warp_min(float v)
 
 // Leaf frames: for every group of consecutive pairs that share a quadrant,
 // one warp rounds the quadrant's first point to the anchor grid and writes
-// u = fl32(p - A_l) for each of its points (indexed by sorted position), the
-// largest |u| and the u-range.  Non-finite points are flagged per leaf.
+// u = fl32(p - A_l) for each of its points (indexed by sorted position; one
+// rounding of the exact difference), the largest |u| and the u-range.
+// Non-finite points are flagged per leaf.
 struct LeafFrame {
   double ax, ay;
   long long ix, iy;               // anchor in grid steps
@@ -90,9 +92,11 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
         if (!ok[t]) continue;
+        // fl32(p - A), rounded once; on the integer pipe where the inputs
+        // allow, else through the float64 subtraction
         float2 v;
-        v.x                           = static_cast<float>(px[t] - ax);
-        v.y                           = static_cast<float>(py[t] - ay);
+        if (!f32_of_difference(px[t], ax, v.x)) v.x = static_cast<float>(px[t] - ax);
+        if (!f32_of_difference(py[t], ay, v.y)) v.y = static_cast<float>(py[t] - ay);
         u[off + c0 + t * 32 + lane]   = v;
         if (isfinite(v.x) && isfinite(v.y)) {
           m   = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
