@@ -136,8 +136,8 @@ class BatchedPip {
     CSPT_CHECK_LAUNCH();
     if (m_) {
       localize_kernel<<<grid_for(m_, kBlk, grid_cap()), kBlk, 0, s>>>(
-        op_.data(), oq_.data(), m_, f_.pt_begin_.data(), static_cast<uint32_t>(ni_),
-        f_.inst_.data(), true);
+        op_.data(), oq_.data(), m_, f_.pt_begin_.data(), f_.tile_inst_.data(), f_.inst_.data(),
+        true);
       CSPT_CHECK_LAUNCH();
     }
   }

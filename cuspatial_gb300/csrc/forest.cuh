@@ -65,14 +65,48 @@ __device__ inline uint32_t find_instance(uint32_t const* __restrict__ begins, ui
   for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < (n); \
        i += static_cast<size_t>(gridDim.x) * blockDim.x)
 
+// Point positions in tiles of 2^kTileShift: tile_inst[t] = the instance of
+// the tile's first position, tile_inst[ntiles] = ni - 1.  A position's
+// instance then lies in [tile_inst[t], tile_inst[t + 1]], usually one entry.
+constexpr int kTileShift = 10;
+inline size_t position_tiles(size_t n) { return (n + (size_t{1} << kTileShift) - 1) >> kTileShift; }
+
+__global__ void tile_instance_kernel(uint32_t const* __restrict__ begins, uint32_t ni, size_t ntiles,
+                                     uint32_t* __restrict__ tile_inst)
+{
+  CSPT_GRID_STRIDE(t, ntiles + 1)
+  {
+    tile_inst[t] = t < ntiles ? find_instance(begins, ni, static_cast<uint32_t>(t << kTileShift))
+                              : ni - 1u;
+  }
+}
+
+// find_instance narrowed by the tile table
+__device__ inline uint32_t instance_of(uint32_t const* __restrict__ begins,
+                                       uint32_t const* __restrict__ tile_inst, uint32_t v)
+{
+  uint32_t const t = v >> kTileShift;
+  uint32_t lo = tile_inst[t], hi = tile_inst[t + 1] + 1u;
+  while (hi - lo > 1) {
+    uint32_t const mid = (lo + hi) >> 1;
+    if (begins[mid] <= v)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
 // phase_1.cuh:73-85 per instance, tagged with the instance
+template <typename K>
 __global__ void keys_kernel(double const* __restrict__ x, double const* __restrict__ y, size_t n,
-                            uint32_t const* __restrict__ pt_begin, uint32_t ni,
-                            Inst const* __restrict__ inst, int kb, uint64_t* __restrict__ keys)
+                            uint32_t const* __restrict__ pt_begin,
+                            uint32_t const* __restrict__ tile_inst,
+                            Inst const* __restrict__ inst, int kb, K* __restrict__ keys)
 {
   CSPT_GRID_STRIDE(i, n)
   {
-    uint32_t const k = find_instance(pt_begin, ni, static_cast<uint32_t>(i));
+    uint32_t const k = instance_of(pt_begin, tile_inst, static_cast<uint32_t>(i));
     Inst const& I    = inst[k];
     double const px = x[i], py = y[i];
     uint32_t key;
@@ -83,18 +117,19 @@ __global__ void keys_kernel(double const* __restrict__ x, double const* __restri
       uint16_t const cy = cell_of_quotient(py - I.miny, I.scale, I.rscale);
       key               = (spread16(cy) << 1) | spread16(cx);
     }
-    keys[i] = (static_cast<uint64_t>(k) << kb) | key;
+    keys[i] = (static_cast<K>(k) << kb) | key;
   }
 }
 
-__global__ void start_level_kernel(uint64_t const* __restrict__ sk, size_t n, int kb,
+template <typename K>
+__global__ void start_level_kernel(K const* __restrict__ sk, size_t n, int kb,
                                    Inst const* __restrict__ inst, uint8_t* __restrict__ lvl,
                                    uint8_t* __restrict__ lim)
 {
-  uint64_t const mask = (uint64_t{1} << kb) - 1u;
+  K const mask = (K{1} << kb) - 1u;
   CSPT_GRID_STRIDE(i, n)
   {
-    uint64_t const c = sk[i];
+    K const c = sk[i];
     uint32_t const k = static_cast<uint32_t>(c >> kb);
     int const d      = static_cast<int>(inst[k].d);
     uint8_t l        = 0;
@@ -112,22 +147,55 @@ __global__ void start_level_kernel(uint64_t const* __restrict__ sk, size_t n, in
   }
 }
 
-struct StartFlag {
+// The candidate list: the positions that start a node at some level of their
+// instance (lvl below the instance's depth; a repeated key never does).
+// Every level's starts are a subsequence of it, so the levels are ranked
+// over this list instead of over all points.
+struct AnyStart {
   uint8_t const* lvl;
   uint8_t const* lim;
-  int l;
-  __device__ uint32_t operator()(size_t i) const
-  {
-    return (static_cast<int>(lvl[i]) <= l && l < static_cast<int>(lim[i])) ? 1u : 0u;
-  }
+  __device__ uint32_t operator()(size_t i) const { return lvl[i] < lim[i] ? 1u : 0u; }
 };
-struct RankStore {
-  uint32_t* rank;
-  uint32_t* starts;
+struct AnyStore {
+  uint8_t const* lvl;
+  uint8_t const* lim;
+  uint32_t* apos;
+  uint8_t* alvl;
+  uint8_t* alim;
   __device__ void operator()(size_t i, uint32_t e, uint32_t f) const
   {
-    rank[i] = e;
-    if (f) starts[e] = static_cast<uint32_t>(i);
+    if (f) {
+      apos[e] = static_cast<uint32_t>(i);
+      alvl[e] = lvl[i];
+      alim[e] = lim[i];
+    }
+  }
+};
+
+// level-l starts among the candidates
+struct StartFlag {
+  uint8_t const* alvl;
+  uint8_t const* alim;
+  int l;
+  __device__ uint32_t operator()(size_t j) const
+  {
+    return (static_cast<int>(alvl[j]) <= l && l < static_cast<int>(alim[j])) ? 1u : 0u;
+  }
+};
+// rank[j] = level-l starts before candidate j; a start's sorted position and
+// candidate index
+struct RankStore {
+  uint32_t const* apos;
+  uint32_t* rank;
+  uint32_t* starts;
+  uint32_t* starts_c;
+  __device__ void operator()(size_t j, uint32_t e, uint32_t f) const
+  {
+    rank[j] = e;
+    if (f) {
+      starts[e]   = apos[j];
+      starts_c[e] = static_cast<uint32_t>(j);
+    }
   }
 };
 
@@ -138,8 +206,9 @@ __device__ inline uint32_t node_end(uint32_t const* starts, size_t nl, size_t k,
 }
 
 // point counts and instances of one level's nodes
+template <typename K>
 __global__ void count_kernel(uint32_t const* __restrict__ starts, size_t nl,
-                             uint64_t const* __restrict__ sk, int kb,
+                             K const* __restrict__ sk, int kb,
                              Inst const* __restrict__ inst, uint32_t* __restrict__ count,
                              uint32_t* __restrict__ ninst)
 {
@@ -152,31 +221,33 @@ __global__ void count_kernel(uint32_t const* __restrict__ starts, size_t nl,
   }
 }
 
-__global__ void child_count_kernel(uint32_t const* __restrict__ prev_starts, size_t nprev,
-                                   uint32_t const* __restrict__ prev_inst,
-                                   Inst const* __restrict__ inst,
-                                   uint32_t const* __restrict__ rank_cur,
+// Children of the level-(l-1) nodes: the level-l starts from the node's
+// candidate to the next level-(l-1) node's (or the end of the list).  A node
+// ends earlier only at its instance's end, and the instances between it and
+// the next level-(l-1) node have no level-(l-1) node, hence no level-l one.
+__global__ void child_count_kernel(uint32_t const* __restrict__ prev_starts_c, size_t nprev,
+                                   uint32_t const* __restrict__ rank_cur, uint32_t ncand,
                                    uint32_t* __restrict__ child)
 {
   CSPT_GRID_STRIDE(p, nprev)
   {
-    uint32_t const e = node_end(prev_starts, nprev, p, inst[prev_inst[p]].pt_end);
-    child[p]         = rank_cur[e] - rank_cur[prev_starts[p]];
+    uint32_t const e = p + 1 < nprev ? prev_starts_c[p + 1] : ncand;
+    child[p]         = rank_cur[e] - rank_cur[prev_starts_c[p]];
   }
 }
 
 // phase_2.cuh:206-236 with the instance's max_size
-__global__ void keep_kernel(uint32_t const* __restrict__ starts, size_t nl,
-                            uint32_t const* __restrict__ ninst, uint8_t const* __restrict__ lvl,
+__global__ void keep_kernel(uint32_t const* __restrict__ starts_c, size_t nl,
+                            uint32_t const* __restrict__ ninst, uint8_t const* __restrict__ alvl,
                             int prev_level, uint32_t const* __restrict__ rank_prev,
                             uint32_t const* __restrict__ count_prev,
                             Inst const* __restrict__ inst, uint8_t* __restrict__ keep)
 {
   CSPT_GRID_STRIDE(k, nl)
   {
-    uint32_t const i      = starts[k];
-    uint32_t const is_beg = static_cast<int>(lvl[i]) <= prev_level ? 1u : 0u;
-    uint32_t const parent = rank_prev[i] + is_beg - 1u;
+    uint32_t const j      = starts_c[k];
+    uint32_t const is_beg = static_cast<int>(alvl[j]) <= prev_level ? 1u : 0u;
+    uint32_t const parent = rank_prev[j] + is_beg - 1u;
     keep[k]               = count_prev[parent] > inst[ninst[k]].max_size ? 1 : 0;
   }
 }
@@ -190,19 +261,20 @@ struct PosOut {
   __device__ void operator()(size_t k, uint32_t e, uint32_t) const { ps[k] = e; }
 };
 
+template <typename K>
 __global__ void compact_level_kernel(size_t nl, uint8_t const* __restrict__ kp,
                                      uint32_t const* __restrict__ ps,
                                      uint32_t const* __restrict__ starts,
                                      uint32_t const* __restrict__ cnt,
                                      uint32_t const* __restrict__ child,
                                      uint32_t const* __restrict__ ninst,
-                                     uint64_t const* __restrict__ sk, int kb,
+                                     K const* __restrict__ sk, int kb,
                                      Inst const* __restrict__ inst, int level,
                                      uint32_t* __restrict__ okey, uint32_t* __restrict__ ocount,
                                      uint32_t* __restrict__ ochild, uint32_t* __restrict__ ostart,
                                      uint32_t* __restrict__ oinst)
 {
-  uint64_t const mask = (uint64_t{1} << kb) - 1u;
+  K const mask = (K{1} << kb) - 1u;
   CSPT_GRID_STRIDE(k, nl)
   {
     if (kp && !kp[k]) continue;
@@ -310,8 +382,9 @@ __global__ void offsets_kernel(uint8_t const* __restrict__ internal,
   }
 }
 
+template <typename K>
 __global__ void local_indices_kernel(uint32_t const* __restrict__ sidx,
-                                     uint64_t const* __restrict__ sk, int kb,
+                                     K const* __restrict__ sk, int kb,
                                      Inst const* __restrict__ inst, size_t n,
                                      uint32_t* __restrict__ out)
 {
@@ -328,13 +401,14 @@ __global__ void row_offsets_kernel(uint32_t const* __restrict__ pair_begin,
 // rows -> instance-local point positions (and polygon indices when the
 // instances own polygon ranges)
 __global__ void localize_kernel(uint32_t* __restrict__ op, uint32_t* __restrict__ oq, size_t m,
-                                uint32_t const* __restrict__ pt_begin, uint32_t ni,
+                                uint32_t const* __restrict__ pt_begin,
+                                uint32_t const* __restrict__ tile_inst,
                                 Inst const* __restrict__ inst, bool local_polygons)
 {
   CSPT_GRID_STRIDE(j, m)
   {
     uint32_t const pos = oq[j];
-    Inst const& I      = inst[find_instance(pt_begin, ni, pos)];
+    Inst const& I      = inst[instance_of(pt_begin, tile_inst, pos)];
     oq[j]              = pos - I.pt_begin;
     if (local_polygons) op[j] = op[j] - I.poly_begin;
   }
@@ -414,6 +488,13 @@ class Forest {
                                   cudaMemcpyHostToDevice, s));
     CSPT_CUDA_TRY(cudaMemcpyAsync(poly_begin_.data(), h_pob.data(), (ni + 1) * 4,
                                   cudaMemcpyHostToDevice, s));
+    size_t const ntiles = position_tiles(n_);
+    tile_inst_          = Buffer<uint32_t>(a, ntiles + 1);
+    if (ni) {
+      tile_instance_kernel<<<grid_for(ntiles + 1, kBlk, grid_cap()), kBlk, 0, s>>>(
+        pt_begin_.data(), static_cast<uint32_t>(ni), ntiles, tile_inst_.data());
+      CSPT_CHECK_LAUNCH();
+    }
     // the host arrays above must outlive the copies
     CSPT_CUDA_TRY(cudaStreamSynchronize(s));
   }
@@ -422,7 +503,6 @@ class Forest {
   {
     Allocator const& a   = *alloc_;
     cudaStream_t const s = a.stream();
-    uint32_t const ni    = static_cast<uint32_t>(ni_);
     size_t const n       = n_;
     node_off_            = Buffer<uint64_t>(a, ni_ + 1);
     if (n == 0) {
@@ -430,31 +510,57 @@ class Forest {
       return;
     }
     KernelTimer timer("forest_build", s);
-    unsigned const grd   = grid_for(n, kBlk, grid_cap());
-    int const kb         = dmax_ >= 2 ? 2 * dmax_ + 2 : 2 * dmax_ + 4;
-    int ib               = 0;
+    int const kb = dmax_ >= 2 ? 2 * dmax_ + 2 : 2 * dmax_ + 4;
+    int ib       = 0;
     while ((uint64_t{1} << ib) < ni_) ++ib;
+    // 32-bit composite keys when the instance and Morton bits fit: a third
+    // less traffic in every sort pass
+    if (kb + ib < 32)
+      build_sorted<uint32_t>(x, y, kb, ib);
+    else
+      build_sorted<uint64_t>(x, y, kb, ib);
+  }
 
-    Buffer<uint64_t> keys(a, n), keys_alt(a, n);
+  template <typename K>
+  void build_sorted(double const* x, double const* y, int kb, int ib)
+  {
+    Allocator const& a   = *alloc_;
+    cudaStream_t const s = a.stream();
+    uint32_t const ni    = static_cast<uint32_t>(ni_);
+    size_t const n       = n_;
+    unsigned const grd   = grid_for(n, kBlk, grid_cap());
+
+    Buffer<K> keys(a, n), keys_alt(a, n);
     Buffer<uint32_t> idx(a, n), idx_alt(a, n);
-    keys_kernel<<<grd, kBlk, 0, s>>>(x, y, n, pt_begin_.data(), ni, inst_.data(), kb,
-                                     keys.data());
+    keys_kernel<K><<<grd, kBlk, 0, s>>>(x, y, n, pt_begin_.data(), tile_inst_.data(), inst_.data(),
+                                        kb, keys.data());
     CSPT_CHECK_LAUNCH();
-    bool const alt = radix_sort_pairs<uint64_t>(keys.data(), idx.data(), keys_alt.data(),
-                                                idx_alt.data(), n, 0, kb + ib, true, a);
-    Buffer<uint64_t>& sk = alt ? keys_alt : keys;
-    sidx_                = std::move(alt ? idx_alt : idx);
+    bool const alt = radix_sort_pairs<K>(keys.data(), idx.data(), keys_alt.data(), idx_alt.data(),
+                                         n, 0, kb + ib, true, a);
+    Buffer<K>& sk = alt ? keys_alt : keys;
+    sidx_         = std::move(alt ? idx_alt : idx);
     (alt ? keys : keys_alt).reset();
     (alt ? idx : idx_alt).reset();
 
     Buffer<uint8_t> lvl(a, n), lim(a, n);
-    start_level_kernel<<<grd, kBlk, 0, s>>>(sk.data(), n, kb, inst_.data(), lvl.data(),
-                                            lim.data());
+    start_level_kernel<K><<<grd, kBlk, 0, s>>>(sk.data(), n, kb, inst_.data(), lvl.data(),
+                                               lim.data());
     CSPT_CHECK_LAUNCH();
     pidx_ = Buffer<uint32_t>(a, n);
-    local_indices_kernel<<<grd, kBlk, 0, s>>>(sidx_.data(), sk.data(), kb, inst_.data(), n,
-                                              pidx_.data());
+    local_indices_kernel<K><<<grd, kBlk, 0, s>>>(sidx_.data(), sk.data(), kb, inst_.data(), n,
+                                                 pidx_.data());
     CSPT_CHECK_LAUNCH();
+
+    // the candidate list: one scan over all points, then every level over it
+    Buffer<uint32_t> total(a, 1);
+    Buffer<uint32_t> apos(a, n);
+    Buffer<uint8_t> alvl(a, n), alim(a, n);
+    scan_apply<uint32_t>(AnyStart{lvl.data(), lim.data()},
+                         AnyStore{lvl.data(), lim.data(), apos.data(), alvl.data(), alim.data()},
+                         n, total.data(), a);
+    size_t const nc = read_back(total.data(), s);
+    lvl.reset();
+    lim.reset();
 
     struct Level {
       Buffer<uint32_t> key, count, child, start, inst;
@@ -464,9 +570,9 @@ class Forest {
     Buffer<uint32_t> first(a, ni_ * kLevels), end(a, ni_ * kLevels);
     CSPT_CUDA_TRY(cudaMemsetAsync(first.data(), 0, ni_ * kLevels * 4, s));
     CSPT_CUDA_TRY(cudaMemsetAsync(end.data(), 0, ni_ * kLevels * 4, s));
-    Buffer<uint32_t> total(a, 1);
-    Buffer<uint32_t> rank_prev(a, n + 1), rank_cur(a, n + 1);
-    Buffer<uint32_t> starts_prev, starts_cur, count_prev, count_cur, inst_prev, inst_cur;
+    Buffer<uint32_t> rank_prev(a, nc + 1), rank_cur(a, nc + 1);
+    Buffer<uint32_t> starts_prev, starts_cur, startc_prev, startc_cur, count_prev, count_cur,
+      inst_prev, inst_cur;
     Buffer<uint8_t> keep_prev, keep_cur;
     size_t n_prev = 0;
 
@@ -485,7 +591,7 @@ class Forest {
       L.start        = Buffer<uint32_t>(a, m);
       L.inst         = Buffer<uint32_t>(a, m);
       if (nl) {
-        compact_level_kernel<<<grid_for(nl, kBlk, grid_cap()), kBlk, 0, s>>>(
+        compact_level_kernel<K><<<grid_for(nl, kBlk, grid_cap()), kBlk, 0, s>>>(
           nl, kp, pos.data(), starts.data(), counts.data(), childs ? childs->data() : nullptr,
           ninst.data(), sk.data(), kb, inst_.data(), lv, L.key.data(), L.count.data(),
           L.child.data(), L.start.data(), L.inst.data());
@@ -499,25 +605,27 @@ class Forest {
     };
 
     for (int l = 0; l < dmax_; ++l) {
-      starts_cur = Buffer<uint32_t>(a, n);
-      scan_apply<uint32_t>(StartFlag{lvl.data(), lim.data(), l},
-                           RankStore{rank_cur.data(), starts_cur.data()}, n,
-                           rank_cur.data() + n, a);
-      size_t const nl = read_back(rank_cur.data() + n, s);
+      starts_cur = Buffer<uint32_t>(a, nc);
+      startc_cur = Buffer<uint32_t>(a, nc);
+      scan_apply<uint32_t>(StartFlag{alvl.data(), alim.data(), l},
+                           RankStore{apos.data(), rank_cur.data(), starts_cur.data(),
+                                     startc_cur.data()},
+                           nc, rank_cur.data() + nc, a);
+      size_t const nl = read_back(rank_cur.data() + nc, s);
       count_cur       = Buffer<uint32_t>(a, nl);
       inst_cur        = Buffer<uint32_t>(a, nl);
       keep_cur        = Buffer<uint8_t>(a, nl);
       unsigned const g = grid_for(nl, kBlk, grid_cap());
       if (nl) {
-        count_kernel<<<g, kBlk, 0, s>>>(starts_cur.data(), nl, sk.data(), kb, inst_.data(),
-                                        count_cur.data(), inst_cur.data());
+        count_kernel<K><<<g, kBlk, 0, s>>>(starts_cur.data(), nl, sk.data(), kb, inst_.data(),
+                                           count_cur.data(), inst_cur.data());
         CSPT_CHECK_LAUNCH();
       }
       if (l == 0) {
         if (nl) CSPT_CUDA_TRY(cudaMemsetAsync(keep_cur.data(), 1, nl, s));
       } else {
         if (nl) {
-          keep_kernel<<<g, kBlk, 0, s>>>(starts_cur.data(), nl, inst_cur.data(), lvl.data(),
+          keep_kernel<<<g, kBlk, 0, s>>>(startc_cur.data(), nl, inst_cur.data(), alvl.data(),
                                          l - 1, rank_prev.data(), count_prev.data(),
                                          inst_.data(), keep_cur.data());
           CSPT_CHECK_LAUNCH();
@@ -525,7 +633,7 @@ class Forest {
         Buffer<uint32_t> child_prev(a, n_prev);
         if (n_prev) {
           child_count_kernel<<<grid_for(n_prev, kBlk, grid_cap()), kBlk, 0, s>>>(
-            starts_prev.data(), n_prev, inst_prev.data(), inst_.data(), rank_cur.data(),
+            startc_prev.data(), n_prev, rank_cur.data(), static_cast<uint32_t>(nc),
             child_prev.data());
           CSPT_CHECK_LAUNCH();
         }
@@ -534,6 +642,7 @@ class Forest {
       }
       std::swap(rank_prev, rank_cur);
       starts_prev = std::move(starts_cur);
+      startc_prev = std::move(startc_cur);
       count_prev  = std::move(count_cur);
       inst_prev   = std::move(inst_cur);
       keep_prev   = std::move(keep_cur);
@@ -542,13 +651,15 @@ class Forest {
     emit(dmax_ - 1, starts_prev, count_prev, nullptr, inst_prev, dmax_ - 1 == 0 ? nullptr : &keep_prev,
          n_prev);
     starts_prev.reset();
+    startc_prev.reset();
     count_prev.reset();
     inst_prev.reset();
     keep_prev.reset();
     rank_prev.reset();
     rank_cur.reset();
-    lvl.reset();
-    lim.reset();
+    apos.reset();
+    alvl.reset();
+    alim.reset();
     sk.reset();
 
     Buffer<long long> shift(a, ni_ * kLevels);
@@ -604,7 +715,7 @@ class Forest {
   size_t ni_ = 0, n_ = 0, q_ = 0;
   int dmax_  = 1;
   Buffer<Inst> inst_;
-  Buffer<uint32_t> pt_begin_, poly_begin_;
+  Buffer<uint32_t> pt_begin_, poly_begin_, tile_inst_;
   Buffer<uint32_t> sidx_, pidx_;
   Buffer<uint32_t> key_, length_, offset_, goff_;
   Buffer<uint8_t> level_, internal_;

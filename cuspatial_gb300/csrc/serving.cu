@@ -469,7 +469,8 @@ class ServingBatch {
     CSPT_CHECK_LAUNCH();
     if (m_) {
       localize_kernel<<<grid_for(m_, 256, sm_grid(16u)), 256, 0, s>>>(
-        op_.data(), oq_.data(), m_, f_.pt_begin_.data(), ni32, f_.inst_.data(), false);
+        op_.data(), oq_.data(), m_, f_.pt_begin_.data(), f_.tile_inst_.data(), f_.inst_.data(),
+        false);
       CSPT_CHECK_LAUNCH();
     }
     refined_ = read_back(pip.refined(), s);
