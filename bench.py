@@ -603,7 +603,9 @@ def run_ours(args, dist):
                "api": ("point_in_polygon_join_host (one call)" if join_ms <= sep_ms else
                        "quadtree_on_points_host (ordered), polygon_bounding_boxes, "
                        "join_quadtree_and_bounding_boxes, quadtree_point_in_polygon_host"),
-               "one_call_ms": join_ms, "one_call_rows_identical": joined_same,
+               "one_call_ms": join_ms, "one_call_ms_each": jms,
+               "separate_calls_ms_each": ems,
+               "one_call_rows_identical": joined_same,
                "one_call_stages_ms": one_call_stages,
                "separate_calls_ms": sep_ms,
                "separate_calls_phases_ms": dict(zip(
@@ -847,13 +849,19 @@ def run_batched(args, dist):
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
 
     def plan(method, ordered=True):
+        """The plan (which evaluates once to size the rows) and its first
+        run, which writes the rows from that evaluation; wall-clock ms."""
         torch.cuda.synchronize()
         t = time.perf_counter()
         pl = BatchedPointInPolygon(x, y, wl.point_offsets, polys, wl.polygon_offsets, params,
                                    method=method, block_threads=table.block_threads,
                                    ordered_index=ordered)
         torch.cuda.synchronize()
-        return pl, (time.perf_counter() - t) * 1e3
+        t1 = time.perf_counter()
+        pl.run(graph=False)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        return pl, (t1 - t) * 1e3, (t2 - t1) * 1e3
 
     def replays(pl, k, w, counted=None):
         for _ in range(w):
@@ -871,13 +879,13 @@ def run_batched(args, dist):
         torch.cuda.synchronize()
         return [a.elapsed_time(b) for a, b in out]
 
-    pl, _ = plan(args.method)  # warms the allocator
+    pl, _, _ = plan(args.method)  # warms the allocator
     pl.close()
     lib.cspt_profile_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
                                       ctypes.POINTER(ctypes.c_uint64)]
     lib.cspt_profile_enable.argtypes = [ctypes.c_int]
     lib.cspt_profile_enable(1)
-    pl, plan_ms = plan(args.method)
+    pl, plan_ms, first_ms = plan(args.method)
     plan_stages = {}
     for name in ("batched_tree", "batched_join", "polygon_index"):
         sms, cnt = ctypes.c_double(), ctypes.c_uint64()
@@ -901,7 +909,7 @@ def run_batched(args, dist):
 
     plain = None
     if args.plain_steps > 0 and args.method == "filtered":
-        pe, pe_plan_ms = plan("exact")
+        pe, pe_plan_ms, _ = plan("exact")
         pms = replays(pe, args.plain_steps, 1)
         er = pe.rows()
         plain = {"points_per_s": n / (statistics.mean(pms) / 1e3),
@@ -912,11 +920,15 @@ def run_batched(args, dist):
         pe.close()
 
     # the one-shot index (no slab ordering): the shortest plan + one run
-    pu, pu_plan_ms = plan(args.method, ordered=False)
+    pu, pu_plan_ms, pu_first_ms = plan(args.method, ordered=False)
+    ur0 = [t.clone() for t in pu.rows()]
     ums = replays(pu, args.steps, args.warmup)
     ur = pu.rows()
     pu_ms = statistics.mean(ums)
-    one_shot = {"plan_ms": pu_plan_ms, "ms_per_step": pu_ms,
+    one_shot = {"plan_ms": pu_plan_ms, "ms_per_step": pu_ms, "first_run_ms": pu_first_ms,
+                "plan_plus_first_run_points_per_s": n / ((pu_plan_ms + pu_first_ms) / 1e3),
+                "first_run_rows_identical_to_replay": bool(
+                    all(torch.equal(a, b) for a, b in zip(ur0, ur))),
                 "plan_plus_step_points_per_s": n / ((pu_plan_ms + pu_ms) / 1e3),
                 "rows_identical_to_ordered": bool(
                     torch.equal(ur[1], rows[0]) and torch.equal(ur[2], rows[1]) and
@@ -967,7 +979,8 @@ def run_batched(args, dist):
             mismatches += 1
     single_pps = single_pts / single_s if single_s > 0 else None
 
-    # end to end from pinned host buffers: copies, plan, one evaluation, rows back
+    # end to end from pinned host buffers: copies, plan (one-shot index, one
+    # evaluation), its first run (the rows), rows back
     e2e = None
     if args.e2e_steps > 0:
         hx = torch.from_numpy(wl.x).pin_memory()
@@ -984,7 +997,7 @@ def run_batched(args, dist):
                                                    P.geometry_offset)
             ep = BatchedPointInPolygon(dx, dy, wl.point_offsets, epolys, wl.polygon_offsets,
                                        params, method=args.method,
-                                       block_threads=table.block_threads)
+                                       block_threads=table.block_threads, ordered_index=False)
             ep.run(graph=False)
             ero, erp, erq = ep.rows()
             h_ro = ero.cpu()
@@ -1024,6 +1037,8 @@ def run_batched(args, dist):
                    "l2": "inputs larger than L2 (%.1f GB of points resident)" % (16 * n / 1e9)},
         "plan_ms": plan_ms, "plan_stages_ms": plan_stages,
         "plan_plus_step_points_per_s": n / ((plan_ms + ms) / 1e3),
+        "first_run_ms": first_ms,
+        "plan_plus_first_run_points_per_s": n / ((plan_ms + first_ms) / 1e3),
         "one_shot_index": one_shot,
         "nodes": inf.num_nodes, "pairs": inf.num_pairs, "rows": inf.num_rows,
         "refined_candidates": refined, "kernels_per_step": inf.kernels_per_run,

@@ -90,7 +90,10 @@ class BatchedPointInPolygon:
 
     # -- execution ---------------------------------------------------------
     def run(self, graph=True, stream=None):
-        """Evaluates all instances (asynchronous on the current stream)."""
+        """Evaluates all instances (asynchronous on the current stream).  The
+        first run after the plan writes the rows from the plan's sizing
+        evaluation; later runs evaluate again (graph replays with
+        ``graph=True``)."""
         _lib.check(self._lib.cspt_batched_pip_run(self._handle(), 1 if graph else 0,
                                                   _lib.stream_ptr(stream)), self._lib)
         self._row_offsets_host = None

@@ -95,6 +95,13 @@ class BatchedPip {
   {
     if (!pip_) return;
     KernelTimer timer("batched_pip", s);
+    if (evaluated_) {
+      // the plan's sizing evaluation already holds this batch's bits and
+      // row offsets: the first run only writes the rows
+      evaluated_ = false;
+      finish(s);
+      return;
+    }
     if (use_graph) {
       if (!exec_) capture();
       CSPT_CUDA_TRY(cudaGraphLaunch(exec_, s));
@@ -129,7 +136,15 @@ class BatchedPip {
  private:
   void execute(cudaStream_t s)
   {
-    pip_->execute(s, op_.data(), oq_.data(), m_);
+    pip_->evaluate(s);
+    finish(s);
+  }
+
+  // rows, per-instance row offsets and instance-local indices from the
+  // evaluated bits
+  void finish(cudaStream_t s)
+  {
+    pip_->expand(s, op_.data(), oq_.data(), m_);
     unsigned const g1 = grid_for(ni_ + 1, kBlk, grid_cap());
     row_offsets_kernel<<<g1, kBlk, 0, s>>>(pair_begin_.data(), pip_->pair_out_offsets(),
                                             static_cast<uint32_t>(ni_), row_off_.data());
@@ -220,6 +235,7 @@ class BatchedPip {
     m_  = read_back(pip_->total(), s);
     op_ = Buffer<uint32_t>(a, m_);
     oq_ = Buffer<uint32_t>(a, m_);
+    evaluated_ = true;
   }
 
   void join(uint32_t ni)
@@ -287,6 +303,7 @@ class BatchedPip {
   cudaGraph_t graph_           = nullptr;
   cudaGraphExec_t exec_        = nullptr;
   uint64_t kernels_per_run_    = 0;
+  bool evaluated_              = false;  // no run since the plan's evaluation
 };
 
 }  // namespace cspt

@@ -334,6 +334,26 @@ __host__ __device__ inline uint32_t gather16(uint32_t v)
   return v;
 }
 
+// v < lo || v > hi for bounds that are not NaN, on the integer pipe (GB300's
+// float64 pipe runs comparisons at a small fraction of the integer rate).
+// Non-NaN doubles order as their sign-magnitude bits read as a signed
+// integer after negating the negative ones (both zeros map to 0); a NaN v
+// compares false, as the float64 comparisons do.
+__device__ inline long long ordered_bits(double v)
+{
+  long long const b = __double_as_longlong(v);
+  long long const m = b & 0x7FFFFFFFFFFFFFFFll;
+  return b < 0 ? -m : m;
+}
+__device__ inline bool outside_closed(double v, double lo, double hi)
+{
+  long long const m = __double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFll;
+  if (m > 0x7FF0000000000000ll) return false;  // NaN
+  long long const k = ordered_bits(v);
+  return k < ordered_bits(lo) || k > ordered_bits(hi);
+}
+__device__ inline bool outside_closed(float v, float lo, float hi) { return v < lo || v > hi; }
+
 // static_cast<uint16_t>(t / s) for t >= 0 (the reference's cell index,
 // phase_1.cuh:73-85) without a float64 division in the common case.  With
 // r = fl(1/s) (host-rounded) and q0 = fl(t * r):

@@ -110,7 +110,7 @@ __global__ void keys_kernel(double const* __restrict__ x, double const* __restri
     Inst const& I    = inst[k];
     double const px = x[i], py = y[i];
     uint32_t key;
-    if (px < I.minx || px > I.maxx || py < I.miny || py > I.maxy) {
+    if (outside_closed(px, I.minx, I.maxx) || outside_closed(py, I.miny, I.maxy)) {
       key = (1u << (2 * I.d)) - 1u;
     } else {
       uint16_t const cx = cell_of_quotient(px - I.minx, I.scale, I.rscale);

@@ -45,7 +45,7 @@ __global__ void morton_keys_kernel(T const* __restrict__ x, T const* __restrict_
         reinterpret_cast<float2*>(xy)[i] = make_float2(px, py);
     }
     uint32_t k;
-    if (px < minx || px > maxx || py < miny || py > maxy) {
+    if (outside_closed(px, minx, maxx) || outside_closed(py, miny, maxy)) {
       k = static_cast<uint32_t>((1 << (2 * d)) - 1);
     } else {
       uint16_t const cx = cell_of_quotient(px - minx, scale, rscale);

@@ -634,8 +634,10 @@ cspt_status cspt_batched_pip_plan(
   void* stream, cspt_batched_pip** out_plan);
 
 /* Evaluates all instances on `stream` (asynchronous; allocates nothing).
- * With use_graph != 0 the evaluation is recorded into a CUDA graph on the
- * first such call and replayed as one graph launch afterwards. */
+ * The first run after the plan reuses the plan's sizing evaluation and only
+ * writes the rows; later runs evaluate again.  With use_graph != 0 a full
+ * evaluation is recorded into a CUDA graph on the first such call that
+ * evaluates and replayed as one graph launch afterwards. */
 cspt_status cspt_batched_pip_run(cspt_batched_pip* plan, int use_graph, void* stream);
 
 cspt_status cspt_batched_pip_get_info(const cspt_batched_pip* plan, cspt_batched_pip_info* out);

@@ -112,10 +112,15 @@ def test_batched_matches_single_instance_calls(method, ordered):
     plan = BatchedPointInPolygon(torch.from_numpy(wl.x).cuda(), torch.from_numpy(wl.y).cuda(),
                                  wl.point_offsets, _polygons(wl), wl.polygon_offsets, params,
                                  method=method, ordered_index=ordered)
+    # the first run writes the rows from the plan's own evaluation
     plan.run(graph=False)
     torch.cuda.synchronize()
     expect = _check_plan(plan, wl, params, method)
     assert plan.info().num_rows > 500
+    # a second direct run evaluates again
+    plan.run(graph=False)
+    torch.cuda.synchronize()
+    _check_plan(plan, wl, params, method, expect)
     # graph capture, then two replays: same rows each time
     for _ in range(2):
         plan.run(graph=True)

@@ -331,6 +331,15 @@ def test_quadtree_edge_cases_vs_oracle(dtype):
     x = np.clip(rng.normal(500, 3, 20000), 0, 999.9)
     y = np.clip(rng.normal(500, 3, 20000), 0, 999.9)
     cases.append((x, y, 0, 1000, 0, 1000, 1000 / 32768, 15, 32))
+    # the box test at its edges: points on the bounds and one ulp either side,
+    # both zeros, the smallest subnormals, infinities, a box bound of -0.0
+    for x0, x1 in ((-10.0, 10.0), (-0.0, 10.0)):
+        edge = np.array([x0, np.nextafter(x0, -np.inf), np.nextafter(x0, np.inf), x1,
+                         np.nextafter(x1, np.inf), np.nextafter(x1, -np.inf), -0.0, 0.0,
+                         5e-324, -5e-324, np.inf, -np.inf])
+        x = np.concatenate([rng.choice(edge, 3000), rng.uniform(-12, 12, 3000)])
+        y = np.concatenate([rng.choice(edge, 3000), rng.uniform(-12, 12, 3000)])
+        cases.append((x, y, x0, x1, x0, x1, (x1 - x0) / 256, 8, 16))
     for x, y, x0, x1, y0, y1, scale, depth, size in cases:
         pts = cs.GeoSeries.from_points(x.astype(dtype), y.astype(dtype))
         import warnings
