@@ -11,9 +11,11 @@
 // Each instance's part equals what quadtree_on_points returns for it alone
 // (cpp/include/cuspatial/detail/point_quadtree.cuh:237-272).
 //
-// Points are sorted once by the composite key (instance << kb) | morton key,
-// which keeps instances contiguous and each instance's points in its own
-// stable Morton order.  The single-tree construction (quadtree.cu) carries
+// Points carry the composite key (instance << kb) | morton key and are
+// sorted once, each instance's points within their own range (they are
+// instance-major already, so a segmented radix sort of the Morton bits
+// gives the composite order): instances stay contiguous and each instance's
+// points take their own stable Morton order.  The single-tree construction (quadtree.cu) carries
 // over level by level with three changes: a sorted position starts a node at
 // every level when it is the first point of its instance, a level-l node
 // exists only for instances with max_depth > l, and node ends are clipped to
@@ -488,6 +490,17 @@ class Forest {
                                   cudaMemcpyHostToDevice, s));
     CSPT_CUDA_TRY(cudaMemcpyAsync(poly_begin_.data(), h_pob.data(), (ni + 1) * 4,
                                   cudaMemcpyHostToDevice, s));
+    // radix sort tiles within instances: the points are instance-major
+    // already, so only the Morton bits are sorted
+    std::vector<uint64_t> bounds{0};
+    for (size_t i = 1; i < ni; ++i) bounds.push_back(h_pt_off[i]);
+    bounds.push_back(n_);
+    std::vector<SortTile> hs;
+    segment_sort_tiles(bounds, hs);
+    sort_tiles_ = Buffer<SortTile>(a, hs.size());
+    if (!hs.empty())
+      CSPT_CUDA_TRY(cudaMemcpyAsync(sort_tiles_.data(), hs.data(), hs.size() * sizeof(SortTile),
+                                    cudaMemcpyHostToDevice, s));
     size_t const ntiles = position_tiles(n_);
     tile_inst_          = Buffer<uint32_t>(a, ntiles + 1);
     if (ni) {
@@ -516,13 +529,13 @@ class Forest {
     // 32-bit composite keys when the instance and Morton bits fit: a third
     // less traffic in every sort pass
     if (kb + ib < 32)
-      build_sorted<uint32_t>(x, y, kb, ib);
+      build_sorted<uint32_t>(x, y, kb);
     else
-      build_sorted<uint64_t>(x, y, kb, ib);
+      build_sorted<uint64_t>(x, y, kb);
   }
 
   template <typename K>
-  void build_sorted(double const* x, double const* y, int kb, int ib)
+  void build_sorted(double const* x, double const* y, int kb)
   {
     Allocator const& a   = *alloc_;
     cudaStream_t const s = a.stream();
@@ -535,8 +548,9 @@ class Forest {
     keys_kernel<K><<<grd, kBlk, 0, s>>>(x, y, n, pt_begin_.data(), tile_inst_.data(), inst_.data(),
                                         kb, keys.data());
     CSPT_CHECK_LAUNCH();
-    bool const alt = radix_sort_pairs<K>(keys.data(), idx.data(), keys_alt.data(), idx_alt.data(),
-                                         n, 0, kb + ib, true, a);
+    bool const alt = radix_sort_segments<K>(keys.data(), idx.data(), keys_alt.data(),
+                                            idx_alt.data(), n, 0, kb, true, sort_tiles_.data(),
+                                            static_cast<unsigned>(sort_tiles_.size()), a);
     Buffer<K>& sk = alt ? keys_alt : keys;
     sidx_         = std::move(alt ? idx_alt : idx);
     (alt ? keys : keys_alt).reset();
@@ -716,6 +730,7 @@ class Forest {
   int dmax_  = 1;
   Buffer<Inst> inst_;
   Buffer<uint32_t> pt_begin_, poly_begin_, tile_inst_;
+  Buffer<SortTile> sort_tiles_;
   Buffer<uint32_t> sidx_, pidx_;
   Buffer<uint32_t> key_, length_, offset_, goff_;
   Buffer<uint8_t> level_, internal_;
