@@ -292,10 +292,37 @@ __global__ void compact_level_kernel(size_t nl, uint8_t const* __restrict__ kp,
   }
 }
 
-// first / one-past-last compacted index of each instance within a level
-__global__ void level_span_kernel(uint32_t const* __restrict__ oinst, size_t m, int level,
-                                  uint32_t* __restrict__ first, uint32_t* __restrict__ end)
+// Node counts per level: hist[v * 16 + w] = candidates with start level v
+// in an instance of depth w; level l has the candidates with v <= l < w.
+// Equal (v, w) codes of a warp are added once (they cluster).
+__global__ void level_pair_histogram_kernel(uint8_t const* __restrict__ alvl,
+                                            uint8_t const* __restrict__ alim, size_t nc,
+                                            uint32_t* __restrict__ hist)
 {
+  __shared__ uint32_t sh[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  unsigned const lane = threadIdx.x & 31u;
+  for (size_t b = blockIdx.x * static_cast<size_t>(blockDim.x); b < nc;
+       b += static_cast<size_t>(gridDim.x) * blockDim.x) {  // uniform per warp
+    size_t const j       = b + threadIdx.x;
+    unsigned const code  = j < nc ? (alvl[j] & 15u) * 16u + (alim[j] & 15u) : 0xFFFFu;
+    unsigned const peers = __match_any_sync(0xFFFFFFFFu, code);
+    if (code != 0xFFFFu && static_cast<unsigned>(__ffs(peers) - 1) == lane)
+      atomicAdd(&sh[code], static_cast<uint32_t>(__popc(peers)));
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 256; i += blockDim.x)
+    if (sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+
+// first / one-past-last compacted index of each instance within a level of
+// *mp nodes (device count)
+__global__ void level_span_kernel(uint32_t const* __restrict__ oinst, uint32_t const* mp,
+                                  int level, uint32_t* __restrict__ first,
+                                  uint32_t* __restrict__ end)
+{
+  size_t const m = *mp;
   CSPT_GRID_STRIDE(k, m)
   {
     uint32_t const i = oinst[k];
@@ -590,30 +617,46 @@ class Forest {
     Buffer<uint8_t> keep_prev, keep_cur;
     size_t n_prev = 0;
 
+    // every level's node count from one histogram of the candidates
+    std::vector<size_t> level_size(dmax_, 0);
+    {
+      Buffer<uint32_t> hist(a, 256);
+      CSPT_CUDA_TRY(cudaMemsetAsync(hist.data(), 0, 256 * sizeof(uint32_t), s));
+      if (nc) {
+        level_pair_histogram_kernel<<<grid_for(nc, kBlk, grid_cap()), kBlk, 0, s>>>(
+          alvl.data(), alim.data(), nc, hist.data());
+        CSPT_CHECK_LAUNCH();
+      }
+      uint32_t h[256];
+      CSPT_CUDA_TRY(cudaMemcpyAsync(h, hist.data(), sizeof(h), cudaMemcpyDeviceToHost, s));
+      CSPT_CUDA_TRY(cudaStreamSynchronize(s));
+      for (int l = 0; l < dmax_; ++l)
+        for (int v = 0; v <= l; ++v)
+          for (int w = l + 1; w < 16; ++w) level_size[l] += h[v * 16 + w];
+    }
+    // kept nodes per level, counted on the device; the level arrays hold up
+    // to the level's node count
+    Buffer<uint32_t> kept(a, dmax_);
     auto emit = [&](int lv, Buffer<uint32_t>& starts, Buffer<uint32_t>& counts,
                     Buffer<uint32_t>* childs, Buffer<uint32_t>& ninst, Buffer<uint8_t>* keep,
                     size_t nl) {
       Level& L          = levels[lv];
       uint8_t const* kp = keep ? keep->data() : nullptr;
       Buffer<uint32_t> pos(a, nl);
-      scan_apply<uint32_t>(KeepIn{kp}, PosOut{pos.data()}, nl, total.data(), a);
-      size_t const m = read_back(total.data(), s);
-      L.size         = m;
-      L.key          = Buffer<uint32_t>(a, m);
-      L.count        = Buffer<uint32_t>(a, m);
-      L.child        = Buffer<uint32_t>(a, m);
-      L.start        = Buffer<uint32_t>(a, m);
-      L.inst         = Buffer<uint32_t>(a, m);
+      scan_apply<uint32_t>(KeepIn{kp}, PosOut{pos.data()}, nl, kept.data() + lv, a);
+      L.key   = Buffer<uint32_t>(a, nl);
+      L.count = Buffer<uint32_t>(a, nl);
+      L.child = Buffer<uint32_t>(a, nl);
+      L.start = Buffer<uint32_t>(a, nl);
+      L.inst  = Buffer<uint32_t>(a, nl);
       if (nl) {
         compact_level_kernel<K><<<grid_for(nl, kBlk, grid_cap()), kBlk, 0, s>>>(
           nl, kp, pos.data(), starts.data(), counts.data(), childs ? childs->data() : nullptr,
           ninst.data(), sk.data(), kb, inst_.data(), lv, L.key.data(), L.count.data(),
           L.child.data(), L.start.data(), L.inst.data());
         CSPT_CHECK_LAUNCH();
-      }
-      if (m) {
-        level_span_kernel<<<grid_for(m, kBlk, grid_cap()), kBlk, 0, s>>>(L.inst.data(), m, lv,
-                                                                       first.data(), end.data());
+        level_span_kernel<<<grid_for(nl, kBlk, grid_cap()), kBlk, 0, s>>>(
+          L.inst.data(), kept.data() + lv, lv, first.data(), end.data());
         CSPT_CHECK_LAUNCH();
       }
     };
@@ -625,7 +668,7 @@ class Forest {
                            RankStore{apos.data(), rank_cur.data(), starts_cur.data(),
                                      startc_cur.data()},
                            nc, rank_cur.data() + nc, a);
-      size_t const nl = read_back(rank_cur.data() + nc, s);
+      size_t const nl = level_size[l];
       count_cur       = Buffer<uint32_t>(a, nl);
       inst_cur        = Buffer<uint32_t>(a, nl);
       keep_cur        = Buffer<uint8_t>(a, nl);
@@ -682,10 +725,15 @@ class Forest {
     layout_kernel<<<1, 1024, 0, s>>>(first.data(), end.data(), ni, inst_.data(), shift.data(),
                                      node_off_.data(), err.data());
     CSPT_CHECK_LAUNCH();
+    int herr = 0;
+    std::vector<uint32_t> hk(dmax_);
+    CSPT_CUDA_TRY(cudaMemcpyAsync(&herr, err.data(), sizeof(int), cudaMemcpyDeviceToHost, s));
+    CSPT_CUDA_TRY(cudaMemcpyAsync(hk.data(), kept.data(), dmax_ * sizeof(uint32_t),
+                                  cudaMemcpyDeviceToHost, s));
+    CSPT_CUDA_TRY(cudaStreamSynchronize(s));
+    CSPT_EXPECTS(herr == 0, "an instance's quadtree has too many nodes for the batched form");
     size_t q = 0;
-    for (auto& L : levels) q += L.size;
-    CSPT_EXPECTS(read_back(err.data(), s) == 0,
-                 "an instance's quadtree has too many nodes for the batched form");
+    for (int l = 0; l < dmax_; ++l) q += levels[l].size = hk[l];
     q_        = q;
     key_      = Buffer<uint32_t>(a, q);
     length_   = Buffer<uint32_t>(a, q);

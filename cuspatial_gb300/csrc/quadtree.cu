@@ -88,6 +88,41 @@ __global__ void node_count_kernel(uint32_t const* __restrict__ starts, size_t nl
 }
 
 // finest level (d-1): every position whose key differs from its predecessor
+// Histogram of the start levels: hist[v] = positions whose coarsest start
+// level is v (kNoStart is not counted; v < d <= 16).  Level l has
+// sum_{v <= l} hist[v] nodes, so one read gives every level's size.
+__global__ void __launch_bounds__(256)
+  level_histogram_kernel(uint8_t const* __restrict__ lvl, size_t n, uint32_t* __restrict__ hist)
+{
+  uint32_t c[16];
+#pragma unroll
+  for (int b = 0; b < 16; ++b) c[b] = 0;
+  size_t const stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+  size_t const tid    = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x;
+  size_t const n4     = n / 4;
+  uint32_t const* l4  = reinterpret_cast<uint32_t const*>(lvl);
+  for (size_t i = tid; i < n4; i += stride) {
+    uint32_t const w = l4[i];
+#pragma unroll
+    for (int b = 0; b < 16; ++b) c[b] += __popc(__vcmpeq4(w, 0x01010101u * b)) >> 3;
+  }
+  for (size_t i = n4 * 4 + tid; i < n; i += stride) {
+    uint32_t const v = lvl[i];
+#pragma unroll
+    for (int b = 0; b < 16; ++b) c[b] += v == static_cast<uint32_t>(b) ? 1u : 0u;
+  }
+  __shared__ uint32_t sh[16];
+  if (threadIdx.x < 16) sh[threadIdx.x] = 0;
+  __syncthreads();
+#pragma unroll
+  for (int b = 0; b < 16; ++b) {
+    uint32_t const w = __reduce_add_sync(0xFFFFFFFFu, c[b]);
+    if ((threadIdx.x & 31) == 0 && w) atomicAdd(&sh[b], w);
+  }
+  __syncthreads();
+  if (threadIdx.x < 16 && sh[threadIdx.x]) atomicAdd(&hist[threadIdx.x], sh[threadIdx.x]);
+}
+
 struct FinestStart {
   uint8_t const* lvl;
   __device__ uint32_t operator()(size_t i) const { return lvl[i] != kNoStart ? 1u : 0u; }
@@ -387,7 +422,22 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
   // level is ranked by a scan over the next finer level only (about 1.3 N
   // elements in all instead of d N).  For a level-l node j: S = first sorted
   // position, X = its index among the level-(l+1) starts; for a level-(l+1)
-  // start k: P = the level-l node holding it (its parent).
+  // start k: P = the level-l node holding it (its parent).  Every level's
+  // size comes from one histogram of lvl, and the kept nodes of all levels
+  // are counted on the device and read once: the host waits twice in all.
+  std::vector<size_t> level_size(d);
+  {
+    Buffer<uint32_t> hist(alloc, 16);
+    CSPT_CUDA_TRY(cudaMemsetAsync(hist.data(), 0, 16 * sizeof(uint32_t), s));
+    level_histogram_kernel<<<grid_for((n + 3) / 4, blk, sm_grid(8u)), blk, 0, s>>>(lv, n,
+                                                                                  hist.data());
+    CSPT_CHECK_LAUNCH();
+    uint32_t h[16];
+    CSPT_CUDA_TRY(cudaMemcpyAsync(h, hist.data(), sizeof(h), cudaMemcpyDeviceToHost, s));
+    CSPT_CUDA_TRY(cudaStreamSynchronize(s));
+    size_t run = 0;
+    for (int l = 0; l < d; ++l) level_size[l] = run += h[l];
+  }
   struct Raw {
     Buffer<uint32_t> S, X, P, count;
     Buffer<uint8_t> LV;
@@ -396,29 +446,30 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
   std::vector<Raw> raw(d);
   {
     Raw& R = raw[d - 1];
-    R.S    = Buffer<uint32_t>(alloc, n);
-    R.LV   = Buffer<uint8_t>(alloc, n);
+    R.S    = Buffer<uint32_t>(alloc, level_size[d - 1]);
+    R.LV   = Buffer<uint8_t>(alloc, level_size[d - 1]);
     scan_apply<uint32_t>(FinestStart{lv}, FinestStore{lv, R.S.data(), R.LV.data()}, n,
-                         total.data(), alloc);
-    R.n = read_back(total.data(), s);
+                         static_cast<uint32_t*>(nullptr), alloc);
+    R.n = level_size[d - 1];
   }
   for (int l = d - 2; l >= 0; --l) {
     Raw& F = raw[l + 1];
     Raw& R = raw[l];
-    R.S    = Buffer<uint32_t>(alloc, F.n);
-    R.X    = Buffer<uint32_t>(alloc, F.n);
-    R.LV   = Buffer<uint8_t>(alloc, F.n);
+    R.n    = level_size[l];
+    R.S    = Buffer<uint32_t>(alloc, R.n);
+    R.X    = Buffer<uint32_t>(alloc, R.n);
+    R.LV   = Buffer<uint8_t>(alloc, R.n);
     F.P    = Buffer<uint32_t>(alloc, F.n);
     scan_apply<uint32_t>(CoarserStart{F.LV.data(), l},
                          CoarserStore{F.S.data(), F.LV.data(), R.S.data(), R.X.data(),
                                       R.LV.data(), F.P.data()},
-                         F.n, total.data(), alloc);
-    R.n = read_back(total.data(), s);
+                         F.n, static_cast<uint32_t*>(nullptr), alloc);
     F.LV.reset();
   }
   raw[0].LV.reset();
   size_t const level_1_size = raw[0].n;
   std::vector<LevelNodes> levels(d);
+  Buffer<uint32_t> kept(alloc, d);  // kept nodes per level
   for (int l = 0; l < d; ++l) {
     Raw& R        = raw[l];
     size_t const nl = R.n;
@@ -432,20 +483,18 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
         l + 1 < d ? child.data() : nullptr, keep.data());
       CSPT_CHECK_LAUNCH();
     }
-    // compact the kept nodes of the level
+    // compact the kept nodes of the level (at most nl of them)
     LevelNodes& L = levels[l];
     Buffer<uint32_t> pos(alloc, nl);
     uint8_t const* kp = keep.data();
     uint32_t* ps      = pos.data();
     scan_apply<uint32_t>([kp] __device__(size_t k) { return static_cast<uint32_t>(kp[k]); },
                          [ps] __device__(size_t k, uint32_t e, uint32_t) { ps[k] = e; }, nl,
-                         total.data(), alloc);
-    size_t const m = read_back(total.data(), s);
-    L.size         = m;
-    L.key          = Buffer<uint32_t>(alloc, m);
-    L.count        = Buffer<uint32_t>(alloc, m);
-    L.child        = Buffer<uint32_t>(alloc, m);
-    L.start        = Buffer<uint32_t>(alloc, m);
+                         kept.data() + l, alloc);
+    L.key   = Buffer<uint32_t>(alloc, nl);
+    L.count = Buffer<uint32_t>(alloc, nl);
+    L.child = Buffer<uint32_t>(alloc, nl);
+    L.start = Buffer<uint32_t>(alloc, nl);
     if (nl) {
       compact_nodes_kernel<<<grid_for(nl, blk, sm_grid(16u)), blk, 0, s>>>(
         nl, kp, ps, R.S.data(), R.count.data(), l + 1 < d ? child.data() : nullptr,
@@ -464,6 +513,13 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
   }
   raw.clear();
   lvl.reset();
+  {
+    std::vector<uint32_t> hk(d);
+    CSPT_CUDA_TRY(
+      cudaMemcpyAsync(hk.data(), kept.data(), d * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    CSPT_CUDA_TRY(cudaStreamSynchronize(s));
+    for (int l = 0; l < d; ++l) levels[l].size = hk[l];
+  }
 
   size_t q = 0;
   for (auto& L : levels) q += L.size;
