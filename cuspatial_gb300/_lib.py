@@ -91,6 +91,7 @@ def _declare(lib):
                                             ctypes.POINTER(ctypes.c_uint64)]
     lib.cspt_last_nearest_stats.restype = None
     lib.cspt_free.argtypes = [ctypes.POINTER(CsptAllocator), _vp, _sz, _vp]
+    lib.cspt_pool_trim.argtypes = [_sz]
     lib.cspt_quadtree_free.argtypes = [ctypes.POINTER(CsptAllocator),
                                        ctypes.POINTER(CsptQuadtree), _vp]
     lib.cspt_quadtree_on_points.argtypes = [

@@ -138,6 +138,31 @@ int num_sms()
   return n;
 }
 
+cudaMemPool_t library_pool()
+{
+  constexpr int kMaxDevices = 64;
+  static std::atomic<cudaMemPool_t> pools[kMaxDevices];
+  static std::mutex mu;
+  int dev = 0;
+  CSPT_CUDA_TRY(cudaGetDevice(&dev));
+  CSPT_EXPECTS(dev >= 0 && dev < kMaxDevices, "device ordinal out of range");
+  cudaMemPool_t p = pools[dev].load(std::memory_order_acquire);
+  if (p) return p;
+  std::lock_guard<std::mutex> lk(mu);
+  p = pools[dev].load(std::memory_order_relaxed);
+  if (p) return p;
+  cudaMemPoolProps props{};
+  props.allocType     = cudaMemAllocationTypePinned;
+  props.handleTypes   = cudaMemHandleTypeNone;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id   = dev;
+  CSPT_CUDA_TRY(cudaMemPoolCreate(&p, &props));
+  uint64_t keep = std::numeric_limits<uint64_t>::max();
+  CSPT_CUDA_TRY(cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep));
+  pools[dev].store(p, std::memory_order_release);
+  return p;
+}
+
 cudaStream_t side_stream(int k)
 {
   struct Streams {
@@ -259,6 +284,14 @@ const char* cspt_version(void) { return "cuspatial_gb300 0.1 (sm_103a)"; }
 // event timing of the named kernels (pip_bits, pip_expand, join_count,
 // join_write, nearest, quadtree_build).
 uint64_t cspt_launch_count(void) { return g_launches.load(); }
+
+cspt_status cspt_pool_trim(size_t min_bytes_to_keep)
+{
+  return guarded([&] {
+    CSPT_CUDA_TRY(cudaDeviceSynchronize());
+    CSPT_CUDA_TRY(cudaMemPoolTrimTo(library_pool(), min_bytes_to_keep));
+  });
+}
 
 void cspt_profile_enable(int on)
 {

@@ -93,9 +93,14 @@ cspt_status guarded(F&& body)
 }
 
 // ---------------------------------------------------------------------------
-// memory: every device allocation goes through the caller's allocator, or
-// cudaMallocAsync/cudaFreeAsync when none is given.
+// memory: every device allocation goes through the caller's allocator, or,
+// when none is given, the library's own stream-ordered pool on the current
+// device.  The pool keeps what is freed for later calls (its release
+// threshold is unbounded), where the device's default pool hands memory back
+// to the driver at every synchronisation and maps it again on the next call.
 // ---------------------------------------------------------------------------
+cudaMemPool_t library_pool();
+
 class Allocator {
  public:
   Allocator(cspt_allocator const* mr, cudaStream_t stream) : mr_(mr), stream_(stream) {}
@@ -108,7 +113,7 @@ class Allocator {
       if (!p) throw Error{CSPT_OUT_OF_MEMORY, "allocation of " + std::to_string(bytes) +
                                                  " bytes failed (caller allocator)"};
     } else {
-      cudaError_t const e = cudaMallocAsync(&p, bytes, stream_);
+      cudaError_t const e = cudaMallocFromPoolAsync(&p, bytes, library_pool(), stream_);
       if (e != cudaSuccess) {
         (void)cudaGetLastError();
         throw Error{CSPT_OUT_OF_MEMORY,

@@ -502,7 +502,8 @@ struct Budget {
     while (now > p && !b->peak.compare_exchange_weak(p, now)) {
     }
     void* ptr = nullptr;
-    if (cudaMallocAsync(&ptr, bytes, static_cast<cudaStream_t>(stream)) != cudaSuccess) {
+    if (cudaMallocFromPoolAsync(&ptr, bytes, library_pool(), static_cast<cudaStream_t>(stream)) !=
+        cudaSuccess) {
       (void)cudaGetLastError();
       b->in_use.fetch_sub(bytes);
       return nullptr;

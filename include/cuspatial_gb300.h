@@ -12,7 +12,9 @@
  *     reference's message text available from cspt_last_error_message();
  *   - outputs whose size is only known on the device are allocated through a
  *     caller-supplied allocator (rmm's device_async_resource_ref in the
- *     reference); passing NULL uses cudaMallocAsync / cudaFreeAsync;
+ *     reference); passing NULL uses the library's own stream-ordered pool
+ *     (one per device; freed memory stays in it for later calls until
+ *     cspt_pool_trim);
  *   - every call takes an explicit stream (a cudaStream_t passed as void*).
  *     Calls that return a size the host must know (quadtree node count, pair
  *     counts) synchronise that stream once; the others are asynchronous.
@@ -115,6 +117,11 @@ int cspt_profile_read(const char* name, double* total_ms, uint64_t* launches);
 
 /* Releases a buffer returned by this library (same allocator as the call). */
 void cspt_free(const cspt_allocator* mr, void* ptr, size_t bytes, void* stream);
+
+/* Returns memory of the library's pool on the current device (used when a
+ * call gets no allocator) to the driver, keeping at most min_bytes_to_keep;
+ * synchronises the device first.  No reference counterpart. */
+cspt_status cspt_pool_trim(size_t min_bytes_to_keep);
 
 /* Releases the five columns of a quadtree returned by cspt_quadtree_on_points. */
 void cspt_quadtree_free(const cspt_allocator* mr, cspt_quadtree* tree, void* stream);
