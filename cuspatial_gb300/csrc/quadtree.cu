@@ -364,17 +364,24 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
   Buffer<uint32_t>& skeys = alt ? keys_alt : keys;
   Buffer<uint32_t>& sidx  = alt ? idx_alt : idx;
   (alt ? keys : keys_alt).reset();
+  // The ordered copy needs only the permutation: the gather (bound by
+  // memory) runs on a second stream beside the levels (a chain of small
+  // launches), and the caller's stream waits for it before the build returns
+  // and before the interleaved input is released (order_join is destroyed
+  // before xy_in, also on an exception).
+  cudaStream_t const os = ordered ? side_stream() : nullptr;
+  StreamJoin order_join(s, os);
   if (ordered) {
-    KernelTimer kt("quadtree_order", s);
+    stream_wait(os, s);  // the permutation and the interleaved input are on s
+    KernelTimer kt("quadtree_order", os);
     unsigned const og = grid_for((n + 3) / 4, 256, sm_grid(8u));
     if constexpr (sizeof(T) == 8)
-      gather_rows_kernel<double2><<<og, 256, 0, s>>>(
+      gather_rows_kernel<double2><<<og, 256, 0, os>>>(
         sidx.data(), n, reinterpret_cast<double2 const*>(xy0), reinterpret_cast<double2*>(ordered));
     else
-      gather_rows_kernel<float2><<<og, 256, 0, s>>>(
+      gather_rows_kernel<float2><<<og, 256, 0, os>>>(
         sidx.data(), n, reinterpret_cast<float2 const*>(xy0), reinterpret_cast<float2*>(ordered));
     CSPT_CHECK_LAUNCH();
-    xy_in.reset();
   }
 
   KernelTimer levels_timer("quadtree_levels", s);
