@@ -1001,9 +1001,13 @@ def run_batched(args, dist):
                                        block_threads=table.block_threads, ordered_index=False)
             ep.run(graph=False)
             ero, erp, erq = ep.rows()
-            h_ro = ero.cpu()
-            h_p = erp.cpu()
-            h_q = erq.cpu()
+            if it == 0:  # pinned row buffers, sized by the untimed first pass
+                h_ro = torch.empty(ero.shape, dtype=ero.dtype).pin_memory()
+                h_p = torch.empty(erp.shape, dtype=erp.dtype).pin_memory()
+                h_q = torch.empty(erq.shape, dtype=erq.dtype).pin_memory()
+            h_ro.copy_(ero, non_blocking=True)
+            h_p.copy_(erp, non_blocking=True)
+            h_q.copy_(erq, non_blocking=True)
             torch.cuda.synchronize()
             if it > 0:
                 ems.append((time.perf_counter() - t) * 1e3)
