@@ -767,6 +767,11 @@ def run_plain_small(args, dist):
     t2 = time.perf_counter()
     exact_ms = statistics.mean(times["exact"])
     filt_ms = statistics.mean(times["filtered"])
+    # the join phase's algorithmic bytes: points, vertices, boxes, pairs, rows
+    K, M, V = int(len(oj["bbox_offset"])), int(len(orr["polygon_index"])), int(len(P.x))
+    alg_bytes = 20 * n + 16 * V + 32 * P.num_polygons + 8 * K + 8 * M
+    peak, peak_kind = measured_peak_hbm()
+    achieved = alg_bytes / (exact_ms / 1e3) / 1e9
     same = {m: bool(np.array_equal(r["polygon_index"].cpu().numpy().view(np.uint32),
                                    orr["polygon_index"]) and
                     np.array_equal(r["point_index"].cpu().numpy().view(np.uint32),
@@ -779,6 +784,12 @@ def run_plain_small(args, dist):
         "p50_ms": percentile(times["exact"], 0.5), "p99_ms": percentile(times["exact"], 0.99),
         "filtered": {"points_per_s": n / (filt_ms / 1e3), "ms_per_step": filt_ms,
                      "p99_ms": percentile(times["filtered"], 0.99)},
+        "roofline": {"bound": "hbm", "kernel": "join step (boxes, join, point-in-polygon), "
+                                               "exact method", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes": alg_bytes,
+                     "note": "launch- and host-bound at this size: 1M points, 256 polygons"},
         "pairs_identical_to_oracle": same, "pairs": int(len(oj["bbox_offset"])),
         "hits": int(len(orr["polygon_index"])),
         "cpu_baseline": {"value": n / (t2 - t1), "unit": "points/s", "cores": O.num_threads(),
@@ -819,6 +830,80 @@ def other_configs(args, dist):
             out[name]["wall_s"] = time.time() - t0
         gc.collect()
     return out
+
+
+def batched_cpu_sample(wl, P, params, rows, ro_h, budget_s=8.0, max_instances=64):
+    """The oracle's whole pipeline (quadtree, boxes, join, point-in-polygon)
+    on instances taken in a seeded random order until about budget_s of CPU
+    time; points/s over the sample and whether its rows equal the batched
+    GPU rows of those instances."""
+    from oracle import oracle as O
+    order = np.random.default_rng(11).permutation(wl.num_instances)
+    po = wl.point_offsets.astype(np.int64)
+    qo = wl.polygon_offsets.astype(np.int64)
+    gp = rows[0].cpu().numpy().view(np.uint32)
+    gq = rows[1].cpu().numpy().view(np.uint32)
+    spent, pts, used, same = 0.0, 0, 0, True
+    for i in order:
+        if spent >= budget_s or used >= max_instances:
+            break
+        a, b, pa, pb = po[i], po[i + 1], qo[i], qo[i + 1]
+        if a == b or pa == pb:
+            continue
+        r0, r1 = int(P.part_offset[pa]), int(P.part_offset[pb])
+        v0, v1 = int(P.ring_offset[r0]), int(P.ring_offset[r1])
+        part = (P.part_offset[pa:pb + 1] - r0).astype(np.uint32)
+        ring = (P.ring_offset[r0:r1 + 1] - v0).astype(np.uint32)
+        vx, vy = np.ascontiguousarray(P.x[v0:v1]), np.ascontiguousarray(P.y[v0:v1])
+        x, y = np.ascontiguousarray(wl.x[a:b]), np.ascontiguousarray(wl.y[a:b])
+        p = params[i]
+        box = (p["x_min"], p["x_max"], p["y_min"], p["y_max"])
+        t = time.perf_counter()
+        opi, ot = O.quadtree_on_points(x, y, *box, p["scale"], p["max_depth"], p["max_size"])
+        obb = O.polygon_bounding_boxes(part, ring, vx, vy)
+        oj = O.join_quadtree_and_bounding_boxes(ot, obb, *box, p["scale"], p["max_depth"])
+        orr = O.quadtree_point_in_polygon(oj, ot, opi, x, y, part, ring, vx, vy)
+        spent += time.perf_counter() - t
+        pts += int(b - a)
+        used += 1
+        same = same and bool(np.array_equal(gp[ro_h[i]:ro_h[i + 1]], orr["polygon_index"]) and
+                             np.array_equal(gq[ro_h[i]:ro_h[i + 1]], orr["point_index"]))
+    return {"value": pts / spent if spent > 0 else None, "unit": "points/s",
+            "cores": O.num_threads(), "kind": "port",
+            "sample": "%d instances in a seeded random order (%d points), each through the "
+                      "oracle's quadtree, boxes, join and point-in-polygon: %.2f s"
+                      % (used, pts, spent),
+            "sample_rows_identical_to_gpu": same}
+
+
+def serving_cpu_sample(P, reqs, params, budget_s=8.0, max_requests=64):
+    """The oracle answering requests taken in a seeded random order against
+    the whole polygon set (its boxes computed once, untimed, as the resident
+    set's are) until about budget_s of CPU time."""
+    from oracle import oracle as O
+    obb = O.polygon_bounding_boxes(P.part_offset, P.ring_offset, P.x, P.y)
+    order = np.random.default_rng(12).permutation(len(reqs))
+    spent, pts, used = 0.0, 0, 0
+    for i in order:
+        if spent >= budget_s or used >= max_requests:
+            break
+        r, p = reqs[i], params[i]
+        if len(r.x) == 0:
+            continue
+        x, y = np.ascontiguousarray(r.x), np.ascontiguousarray(r.y)
+        box = (p["x_min"], p["x_max"], p["y_min"], p["y_max"])
+        t = time.perf_counter()
+        opi, ot = O.quadtree_on_points(x, y, *box, p["scale"], p["max_depth"], p["max_size"])
+        oj = O.join_quadtree_and_bounding_boxes(ot, obb, *box, p["scale"], p["max_depth"])
+        O.quadtree_point_in_polygon(oj, ot, opi, x, y, P.part_offset, P.ring_offset, P.x, P.y)
+        spent += time.perf_counter() - t
+        pts += len(x)
+        used += 1
+    return {"value": pts / spent if spent > 0 else None, "unit": "points/s",
+            "cores": O.num_threads(), "kind": "port",
+            "sample": "%d requests in a seeded random order (%d points), each through the "
+                      "oracle's quadtree, join against all %d polygons and point-in-polygon: "
+                      "%.2f s" % (used, pts, P.num_polygons, spent)}
 
 
 def run_batched(args, dist):
@@ -979,6 +1064,9 @@ def run_batched(args, dist):
         if not (torch.equal(got_p, ir["polygon_index"]) and torch.equal(got_q, ir["point_index"])):
             mismatches += 1
     single_pps = single_pts / single_s if single_s > 0 else None
+    cpu = None
+    if dist.rank == 0 and args.gpus == 1 and not args.no_cpu:
+        cpu = batched_cpu_sample(wl, P, params, rows, ro_h)
 
     # end to end from pinned host buffers: copies, plan (one-shot index, one
     # evaluation), its first run (the rows), rows back
@@ -1056,7 +1144,8 @@ def run_batched(args, dist):
         "roofline": {"bound": "hbm", "kernel": "batched evaluation graph", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": None},
-        "e2e": e2e, "gpu_launches": launches, "clocks": clock_info, "generation_s": gen_s,
+        "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clock_info,
+        "generation_s": gen_s,
     }
     pl.close()
     return line
@@ -1118,6 +1207,15 @@ def run_serving(args, dist):
                        "launches_live": int(l1 - l0), "stages_saturated": stages}
     f = out[args.method]
     value = f["saturated"]["points_per_s"] * args.gpus
+    # algorithmic bytes at saturation: every request's points read (16 B)
+    # and sorted-index read (4 B), every row written (8 B); the resident set
+    # is not counted
+    alg_bytes = 20 * f["saturated"]["points"] + 8 * f["saturated"]["rows"]
+    peak, peak_kind = measured_peak_hbm()
+    achieved = alg_bytes / f["saturated"]["span_s"] / 1e9
+    cpu = None
+    if dist.rank == 0 and args.gpus == 1 and not args.no_cpu:
+        cpu = serving_cpu_sample(P, reqs, params)
     line = {
         "metric": METRIC, "workload": "serving", "value": value, "unit": "points/s",
         "n_gpus": args.gpus, "steps": args.requests, "warmup": len(warm),
@@ -1140,6 +1238,11 @@ def run_serving(args, dist):
         "stages_saturated_ms": f["stages_saturated"],
         "plain_fp64": ({"live": out["exact"]["live"], "saturated": out["exact"]["saturated"]}
                        if "exact" in out and args.method != "exact" else None),
+        "roofline": {"bound": "hbm", "kernel": "serving, all requests queued at once",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes": alg_bytes},
+        "cpu_baseline": cpu,
         "gpu_launches": f["launches_live"], "clocks": f["clocks"], "generation_s": gen_s,
     }
     pset.close()
