@@ -832,7 +832,7 @@ def other_configs(args, dist):
     return out
 
 
-def batched_cpu_sample(wl, P, params, rows, ro_h, budget_s=8.0, max_instances=64):
+def batched_cpu_sample(wl, P, params, rows, ro_h, budget_s=8.0, max_instances=256):
     """The oracle's whole pipeline (quadtree, boxes, join, point-in-polygon)
     on instances taken in a seeded random order until about budget_s of CPU
     time; points/s over the sample and whether its rows equal the batched
