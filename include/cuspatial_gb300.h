@@ -13,8 +13,9 @@
  *   - outputs whose size is only known on the device are allocated through a
  *     caller-supplied allocator (rmm's device_async_resource_ref in the
  *     reference); passing NULL uses the library's own stream-ordered pool
- *     (one per device; freed memory stays in it for later calls until
- *     cspt_pool_trim);
+ *     (one per device, created on first use; freed memory stays in it for
+ *     later calls until cspt_pool_trim; like the library's other per-device
+ *     state it does not survive cudaDeviceReset);
  *   - every call takes an explicit stream (a cudaStream_t passed as void*).
  *     Calls that return a size the host must know (quadtree node count, pair
  *     counts) synchronise that stream once; the others are asynchronous.
