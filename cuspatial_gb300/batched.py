@@ -27,14 +27,20 @@ _METHODS = {"exact": _lib.METHOD_EXACT, "filtered": _lib.METHOD_FILTERED}
 PARAM_FIELDS = ("x_min", "x_max", "y_min", "y_max", "scale", "max_depth", "max_size")
 
 
+# cspt_instance_params as a numpy record: five doubles, two int32 (48 bytes)
+_PARAMS_DTYPE = np.dtype([(k, "<f8") for k in PARAM_FIELDS[:5]] +
+                         [(k, "<i4") for k in PARAM_FIELDS[5:]])
+assert _PARAMS_DTYPE.itemsize == ctypes.sizeof(_lib.CsptInstanceParams)
+
+
 def _params_array(params):
-    """Sequence of dicts or tuples in PARAM_FIELDS order -> ctypes array."""
-    arr = (_lib.CsptInstanceParams * len(params))()
-    for i, p in enumerate(params):
-        vals = [p[k] for k in PARAM_FIELDS] if isinstance(p, dict) else list(p)
-        arr[i] = _lib.CsptInstanceParams(float(vals[0]), float(vals[1]), float(vals[2]),
-                                         float(vals[3]), float(vals[4]), int(vals[5]),
-                                         int(vals[6]))
+    """Sequence of dicts or tuples in PARAM_FIELDS order -> a contiguous
+    array laid out as cspt_instance_params (filled column by column)."""
+    rows = [[p[k] for k in PARAM_FIELDS] if isinstance(p, dict) else list(p) for p in params]
+    arr = np.empty(len(rows), dtype=_PARAMS_DTYPE)
+    if rows:
+        for j, k in enumerate(PARAM_FIELDS):
+            arr[k] = [r[j] for r in rows]
     return arr
 
 
@@ -82,7 +88,9 @@ class BatchedPointInPolygon:
             ni, po.ctypes.data_as(u64p), _lib.ptr(x), _lib.ptr(y), qo.ctypes.data_as(u64p),
             _lib.ptr(poly.part_offset), int(poly.part_offset.numel()), _lib.ptr(poly.ring_offset),
             int(poly.ring_offset.numel()), _lib.ptr(poly.x), _lib.ptr(poly.y),
-            int(poly.x.numel()), self._params, _lib.FLOAT64, _METHODS[method],
+            int(poly.x.numel()),
+            self._params.ctypes.data_as(ctypes.POINTER(_lib.CsptInstanceParams)), _lib.FLOAT64,
+            _METHODS[method],
             1 if ordered_index else 0, int(block_threads), self._alloc.ref, _lib.stream_ptr(),
             ctypes.byref(h)), lib)
         self._h = h
