@@ -78,18 +78,18 @@ class BatchedPip {
              size_t nro, double const* vx, double const* vy, size_t nv,
              cspt_instance_params const* params, cspt_method method, bool ordered, int block,
              cspt_allocator const* mr, cudaStream_t stream)
-    : mr_copy_(mr ? *mr : cspt_allocator{}), alloc_(mr ? &mr_copy_ : nullptr, stream), ni_(ni),
-      f_(alloc_)
+    : mr_copy_(mr ? *mr : cspt_allocator{}), alloc_(mr ? &mr_copy_ : nullptr, stream),
+      palloc_(mr ? &mr_copy_ : nullptr, nullptr), ni_(ni), f_(alloc_)
   {
-    plan(h_pt_off, x, y, h_poly_off, po, npo, ro, nro, vx, vy, nv, params, method, ordered,
-         block);
+    try {
+      plan(h_pt_off, x, y, h_poly_off, po, npo, ro, nro, vx, vy, nv, params, method, ordered,
+           block);
+    } catch (...) {
+      release();
+      throw;
+    }
   }
-  ~BatchedPip()
-  {
-    if (exec_) cudaGraphExecDestroy(exec_);
-    if (graph_) cudaGraphDestroy(graph_);
-    if (capture_stream_) cudaStreamDestroy(capture_stream_);
-  }
+  ~BatchedPip() { release(); }
 
   void run(bool use_graph, cudaStream_t s)
   {
@@ -180,6 +180,29 @@ class BatchedPip {
     CSPT_CUDA_TRY(cudaGraphInstantiate(&exec_, graph_, 0));
   }
 
+  // Frees the polygon-side buffers on their stream once the plan's stream
+  // has caught up, then the graph and its stream.
+  void release()
+  {
+    if (poly_stream_) {
+      StreamJoin after(poly_stream_, alloc_.stream());
+      after.join();
+    }
+    pip_.reset();
+    index_.reset();
+    bminx_.reset();
+    bminy_.reset();
+    bmaxx_.reset();
+    bmaxy_.reset();
+    poly_stream_ = nullptr;
+    if (exec_) cudaGraphExecDestroy(exec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    if (capture_stream_) cudaStreamDestroy(capture_stream_);
+    exec_           = nullptr;
+    graph_          = nullptr;
+    capture_stream_ = nullptr;
+  }
+
   void plan(uint64_t const* h_pt_off, double const* x, double const* y,
             uint64_t const* h_poly_off, uint32_t const* po, size_t npo, uint32_t const* ro,
             size_t nro, double const* vx, double const* vy, size_t nv,
@@ -192,23 +215,40 @@ class BatchedPip {
     f_.setup(ni_, h_pt_off, params, h_poly_off);
     uint32_t const ni = static_cast<uint32_t>(ni_);
     row_off_          = Buffer<uint64_t>(a, ni_ + 1);
+    bool const filtered = method == CSPT_METHOD_FILTERED;
+    // the ordered index's windows serve small blocks; the one-shot index's
+    // quadrant fast path keeps per-warp lists sized for blocks of 256
+    bool const order_slabs = filtered && ordered;
+
+    // The boxes and the polygon index need only the polygons: they are built
+    // on a private stream beside the forest build (which is bound by memory
+    // and short launches; the index by the float64 pipe), from memory
+    // ordered on that stream, and the plan's stream waits for them before
+    // the join.  Every polygon must have vertices so that the rows stay
+    // aligned with the polygons (empty geometries shift rows).
+    if (np_ > 0) {
+      poly_stream_ = library_stream();
+      palloc_      = Allocator(alloc_.resource(), poly_stream_);
+      stream_wait(poly_stream_, s);  // the polygon columns were written on s
+      Allocator const& pa = palloc_;
+      bminx_              = Buffer<double>(pa, np_);
+      bminy_              = Buffer<double>(pa, np_);
+      bmaxx_              = Buffer<double>(pa, np_);
+      bmaxy_              = Buffer<double>(pa, np_);
+      polygon_bounding_boxes(po, np_ + 1, ro, nro, vx, vy, nv, CSPT_FLOAT64, 0.0, bminx_.data(),
+                             bminy_.data(), bmaxx_.data(), bmaxy_.data(), pa);
+      index_.reset(new PolygonIndex<double>(po, np_ + 1, ro, nro, vx, vy, nv, filtered, pa,
+                                            order_slabs));
+    }
     {
       KernelTimer timer("batched_tree", s);
       f_.build(x, y);
     }
+    if (poly_stream_) stream_wait(s, poly_stream_);
     if (f_.n_ == 0 || np_ == 0 || f_.q_ == 0) {
       CSPT_CUDA_TRY(cudaMemsetAsync(row_off_.data(), 0, (ni_ + 1) * 8, s));
       return;
     }
-
-    // boxes of all polygons; every polygon must have vertices so that the
-    // rows stay aligned with the polygons (empty geometries shift rows)
-    bminx_ = Buffer<double>(a, np_);
-    bminy_ = Buffer<double>(a, np_);
-    bmaxx_ = Buffer<double>(a, np_);
-    bmaxy_ = Buffer<double>(a, np_);
-    polygon_bounding_boxes(po, np_ + 1, ro, nro, vx, vy, nv, CSPT_FLOAT64, 0.0, bminx_.data(),
-                           bminy_.data(), bmaxx_.data(), bmaxy_.data(), a);
     double const last = read_back(bminx_.data() + np_ - 1, s);
     CSPT_EXPECTS(!(last != last),
                  "the batched form requires every polygon to have at least one vertex");
@@ -220,12 +260,6 @@ class BatchedPip {
       CSPT_CUDA_TRY(cudaMemsetAsync(row_off_.data(), 0, (ni_ + 1) * 8, s));
       return;
     }
-    bool const filtered = method == CSPT_METHOD_FILTERED;
-    // the ordered index's windows serve small blocks; the one-shot index's
-    // quadrant fast path keeps per-warp lists sized for blocks of 256
-    bool const order_slabs = filtered && ordered;
-    index_.reset(new PolygonIndex<double>(po, np_ + 1, ro, nro, vx, vy, nv, filtered, a,
-                                          order_slabs));
     unsigned const pair_block = order_slabs || !filtered ? static_cast<unsigned>(block) : 256u;
     pip_.reset(new PipExec(pair_poly_.data(), pair_quad_.data(), k_, f_.length_.data(),
                            f_.goff_.data(), f_.sidx_.data(), f_.n_, x, y, index_->view(),
@@ -290,6 +324,8 @@ class BatchedPip {
 
   cspt_allocator mr_copy_;
   Allocator alloc_;
+  Allocator palloc_;  // the polygon side's memory, ordered on poly_stream_
+  cudaStream_t poly_stream_ = nullptr;  // library_stream(), not owned
   size_t ni_;
   Forest f_;
   size_t np_ = 0, k_ = 0, m_ = 0;

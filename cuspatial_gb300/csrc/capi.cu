@@ -163,6 +163,24 @@ cudaMemPool_t library_pool()
   return p;
 }
 
+cudaStream_t library_stream()
+{
+  constexpr int kMaxDevices = 64;
+  static std::atomic<cudaStream_t> streams[kMaxDevices];
+  static std::mutex mu;
+  int dev = 0;
+  CSPT_CUDA_TRY(cudaGetDevice(&dev));
+  CSPT_EXPECTS(dev >= 0 && dev < kMaxDevices, "device ordinal out of range");
+  cudaStream_t st = streams[dev].load(std::memory_order_acquire);
+  if (st) return st;
+  std::lock_guard<std::mutex> lk(mu);
+  st = streams[dev].load(std::memory_order_relaxed);
+  if (st) return st;
+  CSPT_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  streams[dev].store(st, std::memory_order_release);
+  return st;
+}
+
 cudaStream_t side_stream(int k)
 {
   struct Streams {

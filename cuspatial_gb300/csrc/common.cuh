@@ -101,6 +101,13 @@ cspt_status guarded(F&& body)
 // ---------------------------------------------------------------------------
 cudaMemPool_t library_pool();
 
+// A stream of the library on the current device (created on first use,
+// non-blocking, kept for the life of the process), for work a long-lived
+// object issues beside its caller's stream: memory ordered on it stays
+// reusable across objects and threads, where a stream per object or per
+// thread would leave the caching allocator's blocks on a dead stream.
+cudaStream_t library_stream();
+
 class Allocator {
  public:
   Allocator(cspt_allocator const* mr, cudaStream_t stream) : mr_(mr), stream_(stream) {}
@@ -133,6 +140,7 @@ class Allocator {
     }
   }
   cudaStream_t stream() const { return stream_; }
+  cspt_allocator const* resource() const { return mr_; }
 
  private:
   cspt_allocator const* mr_;
