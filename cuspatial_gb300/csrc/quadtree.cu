@@ -328,6 +328,11 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
   // (input order), so the gather after the sort reads one vector per point
   Buffer<T> xy_in(alloc, ordered ? 2 * n : 0);
   T* const xy0 = ordered ? xy_in.data() : nullptr;
+  // cells reach 2^d + 2, so the key needs 2(d+1) bits (2(d+2) below d = 2)
+  int const key_bits = d >= 2 ? 2 * d + 2 : 2 * d + 4;
+  int const sort_bits = key_bits > 32 ? 32 : key_bits;
+  bool alt = false;
+  bool sorted = false;
   if (!host) {
     KernelTimer kt("quadtree_keys", s);
     morton_keys_kernel<T><<<grd, blk, 0, s>>>(x, y, n, minx, miny, maxx, maxy, scale,
@@ -338,6 +343,12 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
     StreamJoin copies(s, copy);  // before `keys` is released, also on an exception
     stream_wait(copy, s);        // the destinations may come from work on s
     size_t const nch = std::max<size_t>(1, std::min<size_t>(kHostChunks, n >> 20));
+    // With several chunks each is sorted as soon as its keys exist, while
+    // the next chunks are still crossing the link; the sorted chunks are
+    // then merged (stable: equal keys keep their input order), which leaves
+    // a short merge instead of the whole sort after the last copy.
+    std::vector<size_t> runs{0};
+    bool chunk_alt = false;
     for (size_t c = 0; c < nch; ++c) {
       size_t const i0 = n * c / nch, m = n * (c + 1) / nch - i0;
       CSPT_CUDA_TRY(cudaMemcpyAsync(host->dx + i0, host->hx + i0, m * sizeof(T),
@@ -349,17 +360,33 @@ void build(T const* x, T const* y, size_t n, double x1d, double x2d, double y1d,
         x + i0, y + i0, m, minx, miny, maxx, maxy, scale, T{1} / scale, d, keys.data() + i0,
         xy0 ? xy0 + 2 * i0 : nullptr);
       CSPT_CHECK_LAUNCH();
+      if (nch > 1) {
+        chunk_alt = radix_sort_pairs<uint32_t>(keys.data() + i0, idx.data() + i0,
+                                               keys_alt.data() + i0, idx_alt.data() + i0, m, 0,
+                                               sort_bits, true, alloc,
+                                               static_cast<uint32_t>(i0));
+        runs.push_back(i0 + m);
+      }
     }
     if (host->after_copies) (*host->after_copies)(copy);
     copies.join();
+    if (nch > 1) {
+      KernelTimer kt("quadtree_sort", s);
+      // every chunk took the same number of passes, so all runs sit in the
+      // same pair of buffers
+      bool const moved = chunk_alt ? merge_sorted_runs<uint32_t>(keys_alt.data(), idx_alt.data(),
+                                                                keys.data(), idx.data(), runs, s)
+                                   : merge_sorted_runs<uint32_t>(keys.data(), idx.data(),
+                                                                keys_alt.data(), idx_alt.data(),
+                                                                runs, s);
+      alt    = chunk_alt != moved;
+      sorted = true;
+    }
   }
-  // cells reach 2^d + 2, so the key needs 2(d+1) bits (2(d+2) below d = 2)
-  int const key_bits = d >= 2 ? 2 * d + 2 : 2 * d + 4;
-  bool alt;
-  {
+  if (!sorted) {
     KernelTimer kt("quadtree_sort", s);
     alt = radix_sort_pairs<uint32_t>(keys.data(), idx.data(), keys_alt.data(), idx_alt.data(), n,
-                                     0, key_bits > 32 ? 32 : key_bits, true, alloc);
+                                     0, sort_bits, true, alloc);
   }
   Buffer<uint32_t>& skeys = alt ? keys_alt : keys;
   Buffer<uint32_t>& sidx  = alt ? idx_alt : idx;

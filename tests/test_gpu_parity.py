@@ -483,13 +483,20 @@ def test_host_rows(method):
 @pytest.mark.parametrize("dtype", DTYPES)
 def test_quadtree_from_host(dtype):
     # quadtree_on_points_host: 9M points copied in 8 chunks (page-locked and
-    # pageable), 1000 points in one chunk, and none; the same tree and
-    # permutation as quadtree_on_points on the device copy, and the device
-    # copy equals the input
-    for n, pinned in ((9_000_000, True), (9_000_000, False), (1000, True), (0, True)):
+    # pageable), 3 chunks (an unpaired sorted run in the merge), 5M points on
+    # a coarse lattice in 5 chunks (equal keys in every chunk: the merge
+    # must keep them in input order), 1000 points in one chunk, and none;
+    # the same tree and permutation as quadtree_on_points on the device copy,
+    # and the device copy equals the input
+    for n, pinned, lattice in ((9_000_000, True, False), (9_000_000, False, False),
+                               (3 * (1 << 20) + 5, True, False), (5_000_000, True, True),
+                               (1000, True, False), (0, True, False)):
         rng = np.random.default_rng(n + int(pinned))
-        x = torch.from_numpy(rng.normal(500, 150, n).astype(dtype))
-        y = torch.from_numpy(rng.normal(500, 150, n).astype(dtype))
+        xs, ys = rng.normal(500, 150, n), rng.normal(500, 150, n)
+        if lattice:
+            xs, ys = np.round(xs / 25) * 25, np.round(ys / 25) * 25
+        x = torch.from_numpy(xs.astype(dtype))
+        y = torch.from_numpy(ys.astype(dtype))
         if pinned:
             x, y = x.pin_memory(), y.pin_memory()
         args = (0.0, 1000.0, 0.0, 1000.0, 1000.0 / (1 << 12), 12, 64)
