@@ -602,28 +602,48 @@ __global__ void __launch_bounds__(256)
                     uint32_t* __restrict__ out_poly, uint32_t* __restrict__ out_point,
                     uint64_t cap, uint32_t const* __restrict__ id_map)
 {
+  // A warp takes 32 consecutive pairs at a time: lane j loads pair j's
+  // header, and each pair's bitmask words are loaded 32 at a time, one per
+  // lane, then broadcast word by word, so the loads of a batch are issued
+  // together instead of one dependent load per word.
   int const lane     = threadIdx.x & 31;
   unsigned const lt  = (1u << lane) - 1u;
   size_t const warps = (static_cast<size_t>(gridDim.x) * blockDim.x) >> 5;
-  for (size_t k = (blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5; k < npairs;
-       k += warps) {
-    uint32_t const poly = pair_poly[k];
-    uint32_t const len  = qlen[pair_quad[k]];
-    uint32_t const off  = qoff[pair_quad[k]];
-    uint64_t const wb   = word_off[k];
-    uint64_t o          = out_off[k];
-    for (uint32_t c = 0; c < len; c += 32) {
-      unsigned const w = bits[wb + (c >> 5)];
-      if (w == 0) continue;
-      if (w & (1u << lane)) {
-        uint64_t const d = o + __popc(w & lt);
-        if (d < cap) {
-          uint32_t const pos = off + c + lane;
-          out_poly[d]        = poly;
-          out_point[d]       = id_map ? id_map[pos] : pos;
+  for (size_t k0 = ((blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x) >> 5) * 32;
+       k0 < npairs; k0 += warps * 32) {
+    size_t const kl     = k0 + lane;
+    bool const have     = kl < npairs;
+    uint32_t const q    = have ? pair_quad[kl] : 0u;
+    uint32_t const hp   = have ? pair_poly[kl] : 0u;
+    uint32_t const hlen = have ? qlen[q] : 0u;
+    uint32_t const hoff = have ? qoff[q] : 0u;
+    uint64_t const hwb  = have ? word_off[kl] : 0u;
+    uint64_t const ho   = have ? out_off[kl] : 0u;
+    uint32_t const nk   = npairs - k0 < 32 ? static_cast<uint32_t>(npairs - k0) : 32u;
+    for (uint32_t j = 0; j < nk; ++j) {
+      uint32_t const poly = __shfl_sync(0xFFFFFFFFu, hp, j);
+      uint32_t const len  = __shfl_sync(0xFFFFFFFFu, hlen, j);
+      uint32_t const off  = __shfl_sync(0xFFFFFFFFu, hoff, j);
+      uint64_t const wb   = __shfl_sync(0xFFFFFFFFu, hwb, j);
+      uint64_t o          = __shfl_sync(0xFFFFFFFFu, ho, j);
+      uint32_t const nw   = (len + 31u) >> 5;
+      for (uint32_t w0 = 0; w0 < nw; w0 += 32) {
+        uint32_t const cnt  = nw - w0 < 32u ? nw - w0 : 32u;
+        unsigned const mine = static_cast<uint32_t>(lane) < cnt ? bits[wb + w0 + lane] : 0u;
+        for (uint32_t c = 0; c < cnt; ++c) {
+          unsigned const w = __shfl_sync(0xFFFFFFFFu, mine, c);
+          if (w == 0) continue;
+          if (w & (1u << lane)) {
+            uint64_t const d = o + __popc(w & lt);
+            if (d < cap) {
+              uint32_t const pos = off + ((w0 + c) << 5) + lane;
+              out_poly[d]        = poly;
+              out_point[d]       = id_map ? id_map[pos] : pos;
+            }
+          }
+          o += __popc(w);
         }
       }
-      o += __popc(w);
     }
   }
 }
@@ -746,7 +766,7 @@ void run(uint32_t const* pair_poly, uint32_t const* pair_quad, size_t npairs,
   auto expand = [&](size_t k0, size_t n, Buffer<uint64_t> const& out_off, uint32_t* op,
                     uint32_t* oq, size_t m) {
     KernelTimer timer("pip_expand", s);
-    pip_expand_kernel<<<grid_for(n * 32, blk, sm_grid(8u * 4u)), blk, 0, s>>>(
+    pip_expand_kernel<<<grid_for(n, blk, sm_grid(8u * 4u)), blk, 0, s>>>(
       pair_poly + k0, pair_quad + k0, n, qlen, qoff, word_off.data() + k0, bits.data(),
       out_off.data(), op, oq, m, id_map);
     CSPT_CHECK_LAUNCH();
@@ -936,7 +956,7 @@ class PipExec::Impl {
   void expand(cudaStream_t s, uint32_t* op, uint32_t* oq, uint64_t cap)
   {
     unsigned const blk = blk_;
-    unsigned const grd = grid_for(np_ * 32, blk, sm_grid(8u * 1024u / blk));
+    unsigned const grd = grid_for(np_, blk, sm_grid(8u * 1024u / blk));  // a warp per 32 pairs
     pip_expand_kernel<<<grd, blk, 0, s>>>(pp_, pq_, np_, qlen_, qoff_, word_off_.data(),
                                           bits_.data(), out_off_.data(), op, oq, cap, nullptr);
     CSPT_CHECK_LAUNCH();
