@@ -97,7 +97,8 @@ cspt_status guarded(F&& body)
 // when none is given, the library's own stream-ordered pool on the current
 // device.  The pool keeps what is freed for later calls (its release
 // threshold is unbounded), where the device's default pool hands memory back
-// to the driver at every synchronisation and maps it again on the next call.
+// to the CUDA driver at every synchronisation and maps it again on the next
+// call.
 // ---------------------------------------------------------------------------
 cudaMemPool_t library_pool();
 

@@ -120,7 +120,7 @@ int cspt_profile_read(const char* name, double* total_ms, uint64_t* launches);
 void cspt_free(const cspt_allocator* mr, void* ptr, size_t bytes, void* stream);
 
 /* Returns memory of the library's pool on the current device (used when a
- * call gets no allocator) to the driver, keeping at most min_bytes_to_keep;
+ * call gets no allocator) to the CUDA driver, keeping at most min_bytes_to_keep;
  * synchronises the device first.  No reference counterpart. */
 cspt_status cspt_pool_trim(size_t min_bytes_to_keep);
 
