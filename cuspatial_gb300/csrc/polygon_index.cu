@@ -186,6 +186,20 @@ __device__ inline uint32_t edge_span(T ax, T ay, T bx, T by, float fa, float fb,
   return j0 | (j1 << 12) | (ex ? kSpanVertical : 0u);
 }
 
+// A double cut to float32 on the integer pipe (mantissa truncated; below
+// float32's normal range -> 0, beyond it or non-finite -> infinity), for the
+// slab-count heuristic only: any slab count gives a valid index.
+__device__ inline float truncated_f32(double v)
+{
+  unsigned long long const b = static_cast<unsigned long long>(__double_as_longlong(v));
+  uint32_t const sign        = static_cast<uint32_t>(b >> 32) & 0x80000000u;
+  int const e                = static_cast<int>((b >> 52) & 0x7FFull) - 1023 + 127;
+  if (e <= 0) return __uint_as_float(sign);
+  if (e >= 255) return __uint_as_float(sign | 0x7F800000u);
+  return __uint_as_float(sign | (static_cast<uint32_t>(e) << 23) |
+                         static_cast<uint32_t>((b >> 29) & 0x7FFFFFull));
+}
+
 // Order-preserving integer image of a non-NaN double (min/max on the
 // integer pipe; float64 comparisons run at a small fraction of that rate).
 __device__ inline long long order_key(double v)
@@ -251,6 +265,7 @@ __global__ void __launch_bounds__(kIdxBlock)
   __shared__ T shT[kIdxBlock / 32];
   __shared__ long long shL[kIdxBlock / 32];
   __shared__ double shD[kIdxBlock / 32];
+  __shared__ float shF[kIdxBlock / 32];
   __shared__ uint32_t shU[kIdxBlock / 32];
   __shared__ T s_ymin, s_ih;
   __shared__ uint32_t s_ns;
@@ -261,6 +276,9 @@ __global__ void __launch_bounds__(kIdxBlock)
     double sum_rise = 0.0;
     uint32_t bad    = 0;
     if constexpr (std::is_same<T, double>::value) {
+      // the edges' rises for the slab count summed in float32 from
+      // truncated vertices: the float64 pipe is this pass's bound
+      float rise = 0.0f;
       long long kx0 = order_key(INFINITY), ky0 = order_key(INFINITY);
       long long kx1 = order_key(-INFINITY), ky1 = order_key(-INFINITY);
       for (uint32_t v = vb + threadIdx.x; v < ve; v += kIdxBlock) {
@@ -278,12 +296,13 @@ __global__ void __launch_bounds__(kIdxBlock)
         }
         uint32_t const pv = prev_in_ring(ro, r0, r1, v);
         prev_out[v]       = pv;
-        sum_rise += fabs(vy[pv] - y);
+        rise += fabsf(truncated_f32(vy[pv]) - truncated_f32(y));
       }
-      mnx = from_order_key(block_min_ll(kx0, shL));
-      mny = from_order_key(block_min_ll(ky0, shL));
-      mxx = from_order_key(block_max_ll(kx1, shL));
-      mxy = from_order_key(block_max_ll(ky1, shL));
+      mnx      = from_order_key(block_min_ll(kx0, shL));
+      mny      = from_order_key(block_min_ll(ky0, shL));
+      mxx      = from_order_key(block_max_ll(kx1, shL));
+      mxy      = from_order_key(block_max_ll(ky1, shL));
+      sum_rise = static_cast<double>(block_sum(rise, shF));
     } else {
       mnx = INFINITY;
       mny = INFINITY;
@@ -300,12 +319,12 @@ __global__ void __launch_bounds__(kIdxBlock)
         prev_out[v]       = pv;
         sum_rise += fabs(static_cast<double>(vy[pv]) - static_cast<double>(y));
       }
-      mnx = block_min(mnx, shT);
-      mny = block_min(mny, shT);
-      mxx = block_max(mxx, shT);
-      mxy = block_max(mxy, shT);
+      mnx      = block_min(mnx, shT);
+      mny      = block_min(mny, shT);
+      mxx      = block_max(mxx, shT);
+      mxy      = block_max(mxy, shT);
+      sum_rise = block_sum(sum_rise, shD);
     }
-    sum_rise = block_sum(sum_rise, shD);
     if (threadIdx.x == 0) {
       uint32_t const ns = choose_slabs(
         ve - vb, static_cast<double>(mxy) - static_cast<double>(mny), sum_rise, density);
