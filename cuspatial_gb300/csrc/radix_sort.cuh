@@ -17,10 +17,10 @@ namespace cspt {
 
 constexpr int kSortBlock = 256;  // one thread per 8-bit digit in the scatter
 constexpr int kSortWarps = kSortBlock / 32;
-#ifndef CSPT_SORT_ROUND
-#define CSPT_SORT_ROUND 8
-#endif
-constexpr int kSortRound = CSPT_SORT_ROUND;  // rounds of 32 items per warp
+// Rounds of 32 items per warp.  A fixed constant, not a build option: the
+// sort's templates are instantiated in several translation units, and one
+// program must see one tile size in all of them.
+constexpr int kSortRound = 8;
 constexpr int kSortTile  = kSortBlock * kSortRound;
 constexpr unsigned kNoDigit = 0xFFFFu;
 
